@@ -1,0 +1,144 @@
+"""Pin the CPU oracle (oracle/ofx.c) to the reference.
+
+* against the reference's own hot-path code (oracle/_ref harness) on seeded
+  inputs, bit for bit, over the scheme matrix the reference tests
+  (test/MHD/OrszagTang/testme.py:16-21, OrszagTang3D, LinearWaveTest);
+* against the golden fixtures that the harness produced (these run on any
+  machine, the reference tree is not needed);
+* against the reference's analytic known-answer test for linear waves
+  (test/MHD/LinearWaveTest/python/testidefix.py:23-64).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle.pyofx as P
+from idefix_gb300 import ic
+from mhd_state import embed, extract
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+MATRIX = []
+for dims in (2, 3):
+    for order in ("order1", "plm", "limo3", "ppm"):
+        for solver in ("hlld", "hll", "roe", "tvdlf"):
+            for emf in ("uct_contact", "arithmetic", "uct0", "uct_hll", "uct_hlld"):
+                if emf == "uct_hlld" and solver in ("hll", "tvdlf"):
+                    continue
+                MATRIX.append((dims, order, solver, emf))
+
+
+def _initial(dims, small=True):
+    if dims == 2:
+        n = (24, 24)
+        Vc, Vs = ic.orszag_tang_2d(n[0], nghost=2)
+    else:
+        n = (10, 10, 10)
+        Vc, Vs = ic.turbulence_3d(n[0], seed=5, nghost=2, kmax=4)
+    return n, extract(dims, n, 2, Vc, Vs)
+
+
+def _run(kind, dims, n, state, cycles, **scheme):
+    o = P.Oracle(dims, n, kind=kind, **scheme)
+    o.set_prim(*embed(dims, n, o.ng, *state))
+    st = o.run(max_cycles=cycles)
+    return st, extract(dims, n, o.ng, *o.get_prim()), o.get_time()
+
+
+def _same(a, b):
+    return all(np.array_equal(x, y) for x, y in zip([a[0]] + a[1], [b[0]] + b[1]))
+
+
+@pytest.mark.parametrize("dims,order,solver,emf", MATRIX)
+def test_oracle_matches_reference_bit_for_bit(oracle_lib, reference_libs, dims, order, solver, emf):
+    n, state = _initial(dims)
+    P.LIB_REF = os.path.join(reference_libs, f"libofx_ref_d{dims}_o{P.ORDER[order]}.so")
+    scheme = dict(order=order, solver=solver, emf=emf, cfl=0.6 if dims == 2 else 0.4)
+    port = _run("port", dims, n, state, 5, **scheme)
+    ref = _run("ref", dims, n, state, 5, **scheme)
+    assert port[0] == ref[0] == 0
+    assert port[2] == ref[2]
+    assert _same(port[1], ref[1])
+
+
+@pytest.mark.parametrize("nstages", [1, 3])
+def test_oracle_matches_reference_rk_variants(oracle_lib, reference_libs, nstages):
+    n, state = _initial(2)
+    P.LIB_REF = os.path.join(reference_libs, "libofx_ref_d2_o2.so")
+    scheme = dict(order="plm", solver="hlld", emf="uct_contact", nstages=nstages, cfl=0.4)
+    port = _run("port", 2, n, state, 8, **scheme)
+    ref = _run("ref", 2, n, state, 8, **scheme)
+    assert port[2] == ref[2] and _same(port[1], ref[1])
+
+
+def test_oracle_matches_reference_to_tstop_with_cfl_limited_dt(oracle_lib, reference_libs):
+    """OT 2-D to t=0.1: the CFL reduction and the t_stop clamp are exercised"""
+    dims, n = 2, (24, 24)
+    Vc, Vs = ic.orszag_tang_2d(n[0])
+    state = extract(dims, n, 2, Vc, Vs)
+    P.LIB_REF = os.path.join(reference_libs, "libofx_ref_d2_o2.so")
+    res = []
+    for kind in ("port", "ref"):
+        o = P.Oracle(dims, n, kind=kind)
+        o.set_prim(*embed(dims, n, o.ng, *state))
+        o.set_checks(log_period=10, check_nan_period=10)
+        assert o.run(tstop=0.1) == 0
+        res.append((extract(dims, n, o.ng, *o.get_prim()), o.get_time(), o.check_divb()))
+    assert res[0][1] == res[1][1]
+    assert res[0][1][0] == 0.1
+    assert _same(res[0][0], res[1][0])
+    assert res[0][2] == res[1][2]
+
+
+def _golden_cases():
+    return sorted(glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+@pytest.mark.parametrize("path", _golden_cases(), ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_matches_golden_fixture(oracle_lib, path):
+    z = np.load(path)
+    meta = eval(str(z["meta"]))  # fixture written by tests/golden/make_golden.py
+    dims, n = meta["dims"], tuple(meta["n"])
+    state = (z["vc0"], [z[f"vs0_{c}"] for c in range(dims)])
+    st, out, tm = _run("port", dims, n, state, meta["cycles"], order=meta["order"],
+                       solver=meta["solver"], emf=meta["emf"], nstages=meta["nstages"],
+                       cfl=meta["cfl"])
+    assert st == 0
+    assert tm == (float(z["t"]), float(z["dt"]), int(z["ncycles"]))
+    assert np.array_equal(out[0], z["vc1"])
+    for c in range(dims):
+        assert np.array_equal(out[1][c], z[f"vs1_{c}"])
+
+
+def test_golden_fixtures_present():
+    assert len(_golden_cases()) >= 10
+
+
+def test_oracle_linear_fast_wave_known_answer(oracle_lib):
+    """LinearWaveTest (fast mode, Roe, PLM, CFL 0.9): after one period the
+    mean-removed L1 error x 1e6 must stay below 3e-2
+    (test/MHD/LinearWaveTest/python/testidefix.py:23-64, idefix-fast.ini)."""
+    n = (64, 32, 32)
+    Vc, Vs = ic.linear_wave_3d(mode=1, nx=n[0], ny=n[1], nz=n[2])
+    o = P.Oracle(3, n, xbeg=(0, 0, 0), xend=(3.0, 1.5, 1.5), order="plm", solver="roe",
+                 emf="uct_contact", cfl=0.9, first_dt=1e-4, threads=os.cpu_count() or 1)
+    o.set_prim(Vc, Vs)
+    vc0, vs0 = extract(3, n, 2, Vc, Vs)
+    assert o.run(tstop=0.5) == 0
+    vc1, vs1 = extract(3, n, 2, *o.get_prim())
+    # fields as in the reference dump: Vc RHO,VX1..3,PRS and the face fields
+    # on the active cells (the dump holds n faces per direction)
+    pairs = [(vc0[q], vc1[q]) for q in (0, 1, 2, 3, 4)]
+    for c in range(3):
+        s = [slice(None)] * 3
+        s[2 - c] = slice(0, n[c])
+        pairs.append((vs0[c][tuple(s)], vs1[c][tuple(s)]))
+    err = 0.0
+    for q0, q1 in pairs:
+        q0 = q0 - np.mean(q0)
+        q1 = q1 - np.mean(q1)
+        err += np.mean(np.abs(q0 - q1)) ** 2
+    err = np.sqrt(err / len(pairs))
+    assert err * 1e6 < 3e-2, err * 1e6
