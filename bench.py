@@ -1,0 +1,309 @@
+"""Throughput of the ideal-MHD Godunov step on GB300: zone-cycles/s.
+
+Workload (one "step" = one RK2 TimeIntegrator cycle): 3-D decaying MHD
+turbulence, 256^3 periodic unit box, HLLD + PLM (van Leer) + CT
+(uct_contact), RK2, CFL 0.6, FP64 — seeded synthetic initial state (Gaussian
+velocity and vector-potential fields, k^-2 on 1 <= |k| <= 8, rms Mach 1,
+B = (0.1,0,0) + curl A, beta ~ 10).  The state (1.5 GB) is far larger than
+the 129 MB L2, so no flush is needed between cycles.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank advances its own 256^3 box (replicas: the
+single-GPU path has no data exchange), value = sum over ranks.  The
+reference arm times the CPU implementation of the same path on the host
+cores (the oracle restatement, pinned bit for bit to the reference's own
+kernels; the reference itself needs Kokkos, absent on the GPU host) on a
+bounded 128^3 sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "zone-cycles/s (256^3 MHD)"
+UNIT = "zone-cycles/s"
+H100_PUBLISHED = 3.079643e8  # doc/source/bench.json:84-90 (128^3 per GPU, FP64, H100)
+BYTES_PER_ZONE_CYCLE = 320.0  # 8 FP64 state values x 5 transfers per RK2 cycle
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--size", type=int, default=256)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region"""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_baseline(size=128, cycles=4, seed=1):
+    """the CPU path (oracle restatement, OpenMP on every host core) on a
+    bounded sample: a size^3 box of the same workload for `cycles` cycles"""
+    from idefix_gb300 import build, ic
+    from oracle.pyofx import Oracle
+
+    build.build_oracle()
+    threads = os.cpu_count() or 1
+    Vc, Vs = ic.turbulence_3d(size, seed=seed)
+    o = Oracle(3, (size,) * 3, order="plm", solver="hlld", emf="uct_contact", cfl=0.6,
+               first_dt=1e-4, threads=threads)
+    o.set_prim(Vc, Vs)
+    o.run(max_cycles=1)  # warm-up
+    t0 = time.perf_counter()
+    o.run(max_cycles=cycles)
+    el = time.perf_counter() - t0
+    return {"value": size**3 * cycles / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{size}^3 box of the same workload, {cycles} RK2 cycles after 1 warm-up cycle, "
+                      f"{el:.2f} s wall on {threads} threads"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from idefix_gb300 import build, ic
+    from oracle.pyofx import Oracle
+
+    build.build_oracle()
+    threads = os.cpu_count() or 1
+    size = 128
+    Vc, Vs = ic.turbulence_3d(size, seed=1)
+    o = Oracle(3, (size,) * 3, order="plm", solver="hlld", emf="uct_contact", cfl=0.6,
+               first_dt=1e-4, threads=threads)
+    o.set_prim(Vc, Vs)
+    o.run(max_cycles=args.warmup)
+    t0 = time.perf_counter()
+    o.run(max_cycles=args.steps)
+    el = time.perf_counter() - t0
+    value = size**3 * args.steps / el
+    sample = (f"each step = one RK2 cycle of a {size}^3 sample of the 256^3 workload on the host "
+              f"CPU ({threads} threads, CPU restatement pinned bit-for-bit to the reference kernels)")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": value / H100_PUBLISHED,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"3-D MHD decaying turbulence {size}^3 sample (of 256^3), HLLD+PLM+CT "
+                                   "uct_contact, RK2, CFL 0.6", "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import idefix_gb300 as ig
+    from idefix_gb300 import build, ic
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    build.build_library()
+    n = (args.size,) * 3
+    Vc, Vs = ic.turbulence_3d(args.size, seed=1 + rank)
+    stream = torch.cuda.Stream()
+    blk = ig.GpuBlock(3, n, order="plm", solver="hlld", emf="uct_contact", nstages=2, cfl=0.6,
+                      first_dt=1e-4, log_period=100, check_nan_period=100,
+                      stream=stream.cuda_stream)
+    blk.upload(Vc, Vs)
+    blk.run(max_cycles=args.warmup)
+    cells = args.size**3
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident throughput --------------------------------------
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    blk.run(max_cycles=args.steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = cells * args.steps * world / (ms * 1e-3)
+    ms_step = ms / args.steps
+
+    # ---- end to end through the C ABI with host buffers ------------------
+    hVc = torch.empty(blk.vc_shape, dtype=torch.float64, pin_memory=True).numpy()
+    hVs = torch.empty(blk.vs_shape, dtype=torch.float64, pin_memory=True).numpy()
+    blk.download((hVc, hVs))
+    e2e_steps = max(2, min(args.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        blk.upload(hVc, hVs)   # host -> device (pinned), synchronous
+        blk.cycle()            # one TimeIntegrator::Cycle (synchronous)
+        blk.download((hVc, hVs))  # device -> host
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = cells * e2e_steps * world / e2e_s
+    state_bytes = hVc.nbytes + hVs.nbytes
+
+    # ---- per-kernel timing (separate run, events around each launch) -----
+    blk.profile(True)
+    blk.run(max_cycles=3)
+    prof = blk.profile_read()
+    blk.profile(False)
+    prof_cycles = 3
+    sweep_classes = ["sweep_x", "sweep_y", "sweep_z"]
+    dom = max(prof, key=lambda k: prof[k][0])
+    # kernels of the timed cycles: cycle begin/end + per stage: face ghosts,
+    # stage begin, 3 sweeps, CT corner, CT faces, stage end; diagnostics on
+    # cycles that are multiples of 100 (divB: 2 kernels, NaN: 2 per stage)
+    first = args.warmup
+    checks = sum(1 for c in range(first, first + args.steps) if c % 100 == 0)
+    gpu_launches = args.steps * (2 + 2 * 8) + checks * (2 + 2 * 2)
+
+    hbm_peak, peak_kind = measured_peaks()
+    # algorithmic bytes of one launch of a sweep kernel: per active cell it
+    # must read the 7 transverse-reconstructed primitives and the normal face
+    # field, read and write the 5 conserved hydro variables, and write the
+    # two face EMFs and the upwind flag (InvDt is stage-0 only)
+    sweep_bytes_per_cell = 8.0 * (7 + 1 + 2 * 5 + 3)
+    dom_ms, dom_n = prof[dom]
+    dom_avg_s = dom_ms / max(dom_n, 1) * 1e-3
+    achieved_gbs = sweep_bytes_per_cell * cells / dom_avg_s / 1e9 if dom in sweep_classes else None
+    cycle_gbs = BYTES_PER_ZONE_CYCLE * cells / (ms_step * 1e-3) / 1e9
+
+    out = None
+    if rank == 0:
+        cpu = None if args.no_cpu_baseline else cpu_baseline()
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"3-D MHD decaying turbulence {args.size}^3 periodic, HLLD+PLM "
+                                   "(van Leer)+CT uct_contact, RK2, CFL 0.6, FP64 bit-identical to the "
+                                   "reference", "cells_per_gpu": cells, "l2": "inputs larger than L2 "
+                                   "(1.5 GB state), no flush", "ic": "seeded Gaussian k^-2, Mach 1, beta 10"},
+            "clocks": clocks,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
+                    "d2h_bytes_per_step": state_bytes,
+                    "how": "per step: upload Vc+Vs from pinned host, one idfx_gpu_cycle, download Vc+Vs"},
+            "gpu_launches": gpu_launches,
+            "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": (achieved_gbs / hbm_peak) if achieved_gbs else None,
+                         "traffic": None, "kernel": dom, "peak_kind": peak_kind,
+                         "bytes_per_cell": sweep_bytes_per_cell,
+                         "note": "FP64-issue bound (GB300 FP64 ~1.2 TFLOP/s); see fp64 fields"},
+            "cycle_hbm": {"achieved": cycle_gbs, "unit": "GB/s", "frac": cycle_gbs / hbm_peak,
+                          "bytes_per_zone_cycle": BYTES_PER_ZONE_CYCLE},
+            "kernel_ms_per_cycle": {k: v[0] / prof_cycles for k, v in prof.items() if v[1]},
+            "reference_h100_published": H100_PUBLISHED,
+        }
+        if cpu:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out), flush=True)
+    blk.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return out
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,310 @@
+"""idefix_gb300: the ideal-MHD Godunov stage of Idefix on one GB300 GPU.
+
+Host-side mirror of the reference interface for this path, over the C ABI
+of ``libidefix_gb300.so`` (declared in include/idefix_gb300.h):
+
+* :class:`GpuBlock` — one periodic Cartesian block on the GPU: state
+  upload/download in the reference layout, ``cycle`` / ``run`` with the
+  semantics of ``TimeIntegrator::Cycle`` and the main loop, and the
+  building blocks (``set_boundaries``, ``prim_to_cons``, ``evolve_stage``,
+  ``compute_timestep``, ``cons_to_prim``, ``check_divb``, ``check_nan``).
+* :class:`Fluid`, :class:`TimeIntegrator` — thin facades carrying the
+  reference's class and method names (src/fluid/fluid.hpp:53-247,
+  src/timeIntegrator.hpp:25).
+
+Errors follow the reference: numerical failures (NaN, divB, dt too small)
+raise ``RuntimeError`` like the ``std::runtime_error`` that main.cpp
+catches; invalid setups and a too large first_dt raise :class:`IdefixError`
+(the reference's ``IDEFIX_ERROR``).  The library must be built
+(``__graft_entry__.build()``); there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["GpuBlock", "Fluid", "TimeIntegrator", "IdefixError", "load_library", "LIB_PATH"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libidefix_gb300.so")
+
+ORDER = {"order1": 1, "plm": 2, "limo3": 3, "ppm": 4}
+SOLVER = {"hlld": 0, "hll": 1, "roe": 2, "tvdlf": 3}
+EMF = {"uct_contact": 0, "arithmetic": 1, "uct0": 2, "uct_hll": 3, "uct_hlld": 4}
+
+OK, ERR_CONFIG, ERR_NAN, ERR_DIVB, ERR_DT_SMALL, ERR_FIRST_DT, ERR_CUDA, ERR_STATE = range(8)
+
+
+class IdefixError(Exception):
+    """Fatal error of the reference (IDEFIX_ERROR): invalid setup, first_dt."""
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("dims", ctypes.c_int),
+        ("n", ctypes.c_int * 3),
+        ("xbeg", ctypes.c_double * 3),
+        ("xend", ctypes.c_double * 3),
+        ("order", ctypes.c_int),
+        ("solver", ctypes.c_int),
+        ("emf", ctypes.c_int),
+        ("nstages", ctypes.c_int),
+        ("gamma", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("cfl_max_var", ctypes.c_double),
+        ("first_dt", ctypes.c_double),
+        ("maxdivb", ctypes.c_double),
+        ("log_period", ctypes.c_int),
+        ("check_nan_period", ctypes.c_int),
+        ("precision", ctypes.c_int),
+    ]
+
+
+EXPORTS = [
+    "idfx_gpu_default_config", "idfx_gpu_create", "idfx_gpu_destroy", "idfx_gpu_last_error",
+    "idfx_gpu_sizes", "idfx_gpu_upload_prim", "idfx_gpu_download_prim", "idfx_gpu_download_cons",
+    "idfx_gpu_upload_prim_device", "idfx_gpu_download_prim_device", "idfx_gpu_set_time",
+    "idfx_gpu_get_time", "idfx_gpu_cycle", "idfx_gpu_run", "idfx_gpu_set_boundaries",
+    "idfx_gpu_prim_to_cons", "idfx_gpu_cons_to_prim", "idfx_gpu_reset_stage",
+    "idfx_gpu_evolve_stage", "idfx_gpu_compute_timestep", "idfx_gpu_check_divb",
+    "idfx_gpu_check_nan", "idfx_gpu_profile", "idfx_gpu_profile_read",
+]
+
+KERNEL_CLASSES = ["fill_faces", "stage_begin", "sweep_x", "sweep_y", "sweep_z", "ct_corner",
+                  "ct_faces", "stage_end", "control", "checks"]
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+    lib = ctypes.CDLL(path)
+    P, D, I, LL = ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_longlong
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.idfx_gpu_default_config.restype = None
+    lib.idfx_gpu_default_config.argtypes = [ctypes.POINTER(Config), I, I, I, I]
+    lib.idfx_gpu_create.argtypes = [ctypes.POINTER(Config), P, ctypes.POINTER(P)]
+    lib.idfx_gpu_destroy.argtypes = [P]
+    lib.idfx_gpu_last_error.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+    lib.idfx_gpu_sizes.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(LL),
+                                   ctypes.POINTER(LL)]
+    for f in ("idfx_gpu_upload_prim", "idfx_gpu_download_prim", "idfx_gpu_upload_prim_device",
+              "idfx_gpu_download_prim_device"):
+        getattr(lib, f).argtypes = [P, P, P]
+    lib.idfx_gpu_download_cons.argtypes = [P, P]
+    lib.idfx_gpu_set_time.argtypes = [P, D, D, LL]
+    lib.idfx_gpu_get_time.argtypes = [P, dp, dp, ctypes.POINTER(LL)]
+    lib.idfx_gpu_cycle.argtypes = [P]
+    lib.idfx_gpu_run.argtypes = [P, D, LL]
+    for f in ("idfx_gpu_set_boundaries", "idfx_gpu_prim_to_cons", "idfx_gpu_cons_to_prim",
+              "idfx_gpu_reset_stage"):
+        getattr(lib, f).argtypes = [P]
+    lib.idfx_gpu_evolve_stage.argtypes = [P, D, D]
+    lib.idfx_gpu_compute_timestep.argtypes = [P, dp]
+    lib.idfx_gpu_check_divb.argtypes = [P, dp]
+    lib.idfx_gpu_check_nan.argtypes = [P, ctypes.POINTER(LL)]
+    lib.idfx_gpu_profile.argtypes = [P, I]
+    lib.idfx_gpu_profile_read.argtypes = [P, dp, ctypes.POINTER(LL), I]
+    for f in EXPORTS:
+        if f != "idfx_gpu_default_config":
+            getattr(lib, f).restype = I
+    _lib = lib
+    return lib
+
+
+def _as_ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class GpuBlock:
+    """One periodic Cartesian block advanced on the GPU.
+
+    Arguments mirror the reference's input file: [Grid] (dims, n, xbeg,
+    xend), [Hydro] (solver, emf, gamma), [TimeIntegrator] (nstages, CFL,
+    CFL_max_var, first_dt, maxdivB, check_nan), [Output] log, and the
+    build-time reconstruction order.
+    """
+
+    def __init__(self, dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm",
+                 solver="hlld", emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.9,
+                 cfl_max_var=1.1, first_dt=1.0e-10, maxdivb=1e-6, log_period=0,
+                 check_nan_period=0, stream=None):
+        self.lib = load_library()
+        n = list(n) + [1] * (3 - len(n))
+        cfg = Config()
+        self.lib.idfx_gpu_default_config(ctypes.byref(cfg), dims, n[0], n[1], n[2])
+        for d in range(3):
+            cfg.xbeg[d] = float(xbeg[d]) if d < len(xbeg) else 0.0
+            cfg.xend[d] = float(xend[d]) if d < len(xend) else 1.0
+        try:
+            cfg.order, cfg.solver, cfg.emf = ORDER[order], SOLVER[solver], EMF[emf]
+        except KeyError as exc:
+            raise IdefixError(f"unknown scheme option {exc}") from None
+        cfg.nstages = nstages
+        cfg.gamma, cfg.cfl, cfg.cfl_max_var = gamma, cfl, cfl_max_var
+        cfg.first_dt, cfg.maxdivb = first_dt, maxdivb
+        cfg.log_period, cfg.check_nan_period = log_period, check_nan_period
+        h = ctypes.c_void_p()
+        rc = self.lib.idfx_gpu_create(ctypes.byref(cfg), ctypes.c_void_p(stream), ctypes.byref(h))
+        if rc != OK:
+            raise IdefixError(f"idfx_gpu_create failed with status {rc}")
+        self.h = h
+        self.dims, self.n = dims, n
+        nvar, ng, vcl, vsl = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
+        self.lib.idfx_gpu_sizes(self.h, ctypes.byref(nvar), ctypes.byref(ng), ctypes.byref(vcl),
+                                ctypes.byref(vsl))
+        self.nvar, self.ng = nvar.value, ng.value
+        g = self.ng
+        self.nt = [n[d] + 2 * g if d < dims else 1 for d in range(3)]
+        self.ntv = [self.nt[d] + (1 if d < dims else 0) for d in range(3)]
+        self.vc_shape = (self.nvar, self.nt[2], self.nt[1], self.nt[0])
+        self.vs_shape = (dims, self.ntv[2], self.ntv[1], self.ntv[0])
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.idfx_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    # -- errors ---------------------------------------------------------
+    def _check(self, rc):
+        if rc == OK:
+            return
+        buf = ctypes.create_string_buffer(512)
+        self.lib.idfx_gpu_last_error(self.h, buf, 512)
+        msg = buf.value.decode(errors="replace")
+        if rc in (ERR_NAN, ERR_DIVB, ERR_DT_SMALL):
+            raise RuntimeError(msg)
+        raise IdefixError(f"status {rc}: {msg}")
+
+    # -- state ------------------------------------------------------------
+    def upload(self, Vc, Vs):
+        Vc = np.ascontiguousarray(Vc, dtype=np.float64)
+        Vs = np.ascontiguousarray(Vs, dtype=np.float64)
+        if Vc.shape != self.vc_shape or Vs.shape != self.vs_shape:
+            raise IdefixError(f"state shapes {Vc.shape}/{Vs.shape} != {self.vc_shape}/{self.vs_shape}")
+        self._check(self.lib.idfx_gpu_upload_prim(self.h, _as_ptr(Vc), _as_ptr(Vs)))
+
+    def download(self, out=None):
+        Vc = np.empty(self.vc_shape) if out is None else out[0]
+        Vs = np.empty(self.vs_shape) if out is None else out[1]
+        self._check(self.lib.idfx_gpu_download_prim(self.h, _as_ptr(Vc), _as_ptr(Vs)))
+        return Vc, Vs
+
+    def download_cons(self):
+        Uc = np.empty(self.vc_shape)
+        self._check(self.lib.idfx_gpu_download_cons(self.h, _as_ptr(Uc)))
+        return Uc
+
+    def upload_device(self, vc_ptr, vs_ptr):
+        """state from device pointers (e.g. torch tensors' data_ptr())"""
+        self._check(self.lib.idfx_gpu_upload_prim_device(self.h, ctypes.c_void_p(vc_ptr),
+                                                         ctypes.c_void_p(vs_ptr)))
+
+    def download_device(self, vc_ptr, vs_ptr):
+        self._check(self.lib.idfx_gpu_download_prim_device(self.h, ctypes.c_void_p(vc_ptr),
+                                                           ctypes.c_void_p(vs_ptr)))
+
+    def set_time(self, t, dt, ncycles=0):
+        self._check(self.lib.idfx_gpu_set_time(self.h, t, dt, ncycles))
+
+    def get_time(self):
+        t, dt, nc = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        self._check(self.lib.idfx_gpu_get_time(self.h, ctypes.byref(t), ctypes.byref(dt),
+                                               ctypes.byref(nc)))
+        return t.value, dt.value, nc.value
+
+    # -- time integration -------------------------------------------------
+    def cycle(self):
+        self._check(self.lib.idfx_gpu_cycle(self.h))
+
+    def run(self, tstop=-1.0, max_cycles=-1):
+        self._check(self.lib.idfx_gpu_run(self.h, tstop, max_cycles))
+
+    # -- building blocks --------------------------------------------------
+    def set_boundaries(self):
+        self._check(self.lib.idfx_gpu_set_boundaries(self.h))
+
+    def prim_to_cons(self):
+        self._check(self.lib.idfx_gpu_prim_to_cons(self.h))
+
+    def cons_to_prim(self):
+        self._check(self.lib.idfx_gpu_cons_to_prim(self.h))
+
+    def reset_stage(self):
+        self._check(self.lib.idfx_gpu_reset_stage(self.h))
+
+    def evolve_stage(self, t, dt):
+        self._check(self.lib.idfx_gpu_evolve_stage(self.h, t, dt))
+
+    def compute_timestep(self):
+        v = ctypes.c_double()
+        self._check(self.lib.idfx_gpu_compute_timestep(self.h, ctypes.byref(v)))
+        return v.value
+
+    def check_divb(self):
+        v = ctypes.c_double()
+        self._check(self.lib.idfx_gpu_check_divb(self.h, ctypes.byref(v)))
+        return v.value
+
+    def check_nan(self):
+        v = ctypes.c_longlong()
+        self._check(self.lib.idfx_gpu_check_nan(self.h, ctypes.byref(v)))
+        return v.value
+
+
+    # -- per-kernel timing --------------------------------------------------
+    def profile(self, enable=True):
+        self._check(self.lib.idfx_gpu_profile(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        n = len(KERNEL_CLASSES)
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_longlong * n)()
+        self._check(self.lib.idfx_gpu_profile_read(self.h, ms, cnt, n))
+        return {k: (ms[i], cnt[i]) for i, k in enumerate(KERNEL_CLASSES)}
+
+
+class Fluid:
+    """Reference-named facade (Fluid<DefaultPhysics>, src/fluid/fluid.hpp)."""
+
+    def __init__(self, block):
+        self.block = block
+
+    def ConvertPrimToCons(self):
+        self.block.prim_to_cons()
+
+    def ConvertConsToPrim(self):
+        self.block.cons_to_prim()
+
+    def ResetStage(self):
+        self.block.reset_stage()
+
+    def EvolveStage(self, t, dt):
+        self.block.evolve_stage(t, dt)
+
+    def CheckDivB(self):
+        return self.block.check_divb()
+
+    def CheckNan(self):
+        return self.block.check_nan()
+
+
+class TimeIntegrator:
+    """Reference-named facade (src/timeIntegrator.hpp)."""
+
+    def __init__(self, block):
+        self.block = block
+
+    def Cycle(self):
+        self.block.cycle()
+
+    def GetNCycles(self):
+        return self.block.get_time()[2]

@@ -1,0 +1,696 @@
+// C ABI and host driver of the GB300 ideal-MHD stage (see include/idefix_gb300.h).
+//
+// The driver mirrors TimeIntegrator::Cycle (timeIntegrator.cpp:246-414) with
+// the time-step state kept on the device, so that successive cycles are
+// queued without host synchronisation; the host mirrors only the cycle count
+// (to schedule the divB / NaN diagnostics exactly when the reference does).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/idefix_gb300.h"
+#include "engine.hpp"
+
+using namespace idfx;
+
+struct idfx_gpu {
+  Engine e;
+};
+
+namespace idfx {
+
+cudaEvent_t take_event(Engine& e) {
+  if (!e.free_events.empty()) {
+    cudaEvent_t ev = e.free_events.back();
+    e.free_events.pop_back();
+    return ev;
+  }
+  cudaEvent_t ev;
+  cudaEventCreate(&ev);
+  return ev;
+}
+
+void mark_begin(Engine& e, int cls) {
+  if (!e.profile) return;
+  Engine::Mark m;
+  m.cls = cls;
+  m.a = take_event(e);
+  m.b = take_event(e);
+  cudaEventRecord(m.a, e.stream);
+  e.marks.push_back(m);
+}
+
+void mark_end(Engine& e) {
+  if (!e.profile || e.marks.empty()) return;
+  cudaEventRecord(e.marks.back().b, e.stream);
+}
+
+}  // namespace idfx
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned nblocks(long long n, int t = kThreads) { return (unsigned)((n + t - 1) / t); }
+
+int fail(Engine& e, int code, const std::string& msg) {
+  e.err = msg;
+  return code;
+}
+
+int cuda_check(Engine& e, cudaError_t rc, const char* what) {
+  if (rc != cudaSuccess) return fail(e, IDFX_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(rc));
+  return IDFX_OK;
+}
+
+#define IDFX_CK(call)                                        \
+  do {                                                       \
+    int idfx_rc_ = cuda_check(e, (call), #call);             \
+    if (idfx_rc_ != IDFX_OK) return idfx_rc_;                \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// auxiliary whole-block kernels used by the building-block entry points
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_prim_to_cons_all(Geo g, Fields f) {
+  using v = Var<D>;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.ncell) return;
+  double V[v::NV], U[v::NV];
+  for (int n = 0; n < v::NV; n++) V[n] = f.Vc[n * g.ncell + c];
+  prim_to_cons<D>(g.gm1, U, V);
+  for (int n = 0; n < v::NV; n++) f.Uc[n * g.ncell + c] = U[n];
+}
+
+// ReconstructVcField on Uc (boundary.hpp:388-404), optionally followed by
+// ConvertConsToPrim (convertConsToPrim.hpp:104-149), over the whole block
+template <int D>
+__global__ void k_uc_field_all(Geo g, Fields f, int to_prim) {
+  using v = Var<D>;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.ncell) return;
+  const int i = (int)(c % g.nt[0]);
+  const long long r = c / g.nt[0];
+  const int j = (int)(r % g.nt[1]);
+  const int k = (int)(r / g.nt[1]);
+  const long long fc = fidx(g, k, j, i);
+  double U[v::NV], V[v::NV];
+  for (int n = 0; n < v::BX1; n++) U[n] = f.Uc[n * g.ncell + c];
+  for (int d = 0; d < D; d++) {
+    const double* vs = f.Vs + d * g.nface;
+    U[v::BX1 + d] = 0.5 * (vs[fc] + vs[fc + g.fs[d]]);
+    f.Uc[(v::BX1 + d) * g.ncell + c] = U[v::BX1 + d];
+  }
+  if (!to_prim) return;
+  cons_to_prim<D>(g.gm1, V, U);
+  for (int n = 0; n < v::NV; n++) f.Vc[n * g.ncell + c] = V[n];
+}
+
+template <int D>
+__global__ void k_cell_emf_all(Geo g, Fields f) {
+  using v = Var<D>;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.ncell) return;
+  const double vx1 = f.Vc[v::MX1 * g.ncell + c], vx2 = f.Vc[v::MX2 * g.ncell + c];
+  const double Bx1 = f.Vc[v::BX1 * g.ncell + c], Bx2 = f.Vc[v::BX2 * g.ncell + c];
+  if constexpr (D == 3) {
+    const double vx3 = f.Vc[v::MX3 * g.ncell + c], Bx3 = f.Vc[v::BX3 * g.ncell + c];
+    f.Ex1[c] = (vx3 * Bx2 - vx2 * Bx3);
+    f.Ex2[c] = (vx1 * Bx3 - vx3 * Bx1);
+  }
+  f.Ex3[c] = (vx2 * Bx1 - vx1 * Bx2);
+}
+
+template <int D>
+__global__ void k_invdt_max(Geo g, Fields f, Ctl* ctl) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)g.n[0] * g.n[1] * (D == 3 ? g.n[2] : 1);
+  if (tid >= tot) return;
+  const int i = g.beg[0] + (int)(tid % g.n[0]);
+  const long long r = tid / g.n[0];
+  const int j = g.beg[1] + (int)(r % g.n[1]);
+  const int k = (D == 3) ? g.beg[2] + (int)(r / g.n[1]) : 0;
+  atomic_max_pos(&ctl->invdt_max_bits, f.InvDt[cidx(g, k, j, i)]);
+}
+
+__global__ void k_set_stage_dt(Geo g, Ctl* ctl, double dt) {
+  double dV = g.dx[0] * g.dx[1];
+  if (g.D == 3) dV = dV * g.dx[2];
+  ctl->dtdV = dt / dV;
+  for (int d = 0; d < 3; d++) ctl->dtdx[d] = dt / g.dx[d];
+}
+
+__global__ void k_faces_combine(Geo g, Fields f, Ctl* ctl, double wc, double w0) {
+  if (ctl->done) return;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = g.nface * g.D;
+  if (tid >= tot) return;
+  f.Vs[tid] = wc * f.Vs[tid] + w0 * f.Vs0[tid];
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+void launch_sweeps(Engine& e, int invdt, int fold_max) {
+  switch (e.g.solver) {
+    case kHLLD: launch_sweeps_hlld(e, invdt, fold_max); break;
+    case kHLL: launch_sweeps_hll(e, invdt, fold_max); break;
+    case kROE: launch_sweeps_roe(e, invdt, fold_max); break;
+    default: launch_sweeps_tvdlf(e, invdt, fold_max); break;
+  }
+}
+
+long long n_active(const Geo& g) { return (long long)g.n[0] * g.n[1] * g.n[2]; }
+long long n_edges(const Geo& g) {
+  return (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.D == 3 ? g.n[2] + 1 : 1);
+}
+
+#define IDFX_DISPATCH_D(K, GRID, BLOCK, ...)                                \
+  do {                                                                      \
+    if (e.g.D == 2) K<2><<<GRID, BLOCK, 0, e.stream>>>(__VA_ARGS__);        \
+    else K<3><<<GRID, BLOCK, 0, e.stream>>>(__VA_ARGS__);                   \
+  } while (0)
+
+void launch_fill_faces(Engine& e, int save_begin) {
+  dim3 grid(nblocks(e.g.nface), e.g.D);
+  mark_begin(e, kKFillFaces);
+  IDFX_DISPATCH_D(k_fill_faces, grid, kThreads, e.g, e.f, e.ctl, save_begin);
+  mark_end(e);
+}
+void launch_stage_begin(Engine& e, int flags) {
+  mark_begin(e, kKStageBegin);
+  IDFX_DISPATCH_D(k_stage_begin, nblocks(e.g.ncell), kThreads, e.g, e.f, e.ctl, flags);
+  mark_end(e);
+}
+void launch_ct(Engine& e, int combine, double wc, double w0) {
+  mark_begin(e, kKCtCorner);
+  IDFX_DISPATCH_D(k_ct_corner, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
+  mark_end(e);
+  mark_begin(e, kKCtFaces);
+  IDFX_DISPATCH_D(k_ct_faces, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl, combine, wc, w0);
+  mark_end(e);
+}
+void launch_nan_check(Engine& e) {
+  cudaMemsetAsync(&e.ctl->nan_count, 0, sizeof(unsigned long long), e.stream);
+  IDFX_DISPATCH_D(k_nan_count, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
+  k_check_nan<<<1, 1, 0, e.stream>>>(e.ctl);
+}
+void launch_divb_check(Engine& e) {
+  cudaMemsetAsync(&e.ctl->divb_bits, 0, sizeof(unsigned long long), e.stream);
+  IDFX_DISPATCH_D(k_divb, nblocks(n_active(e.g)), kThreads, e.g, e.f, e.ctl);
+  k_check_divb<<<1, 1, 0, e.stream>>>(e.ctl);
+}
+
+// queue one TimeIntegrator::Cycle
+void queue_cycle(Engine& e, int use_tstop) {
+  const Geo& g = e.g;
+  const bool cell_emf = (g.emf == kEmfContact || g.emf == kEmfUct0);
+  k_cycle_begin<<<1, 1, 0, e.stream>>>(g, e.ctl, use_tstop);
+  if (e.log_period > 0 && e.ncycles % e.log_period == 0) launch_divb_check(e);
+  const bool nan_check = e.check_nan_period > 0 && e.ncycles % e.check_nan_period == 0;
+  for (int stage = 0; stage < e.nstages; stage++) {
+    const int save = (e.nstages > 1 && stage == 0);
+    launch_fill_faces(e, save);
+    launch_stage_begin(e, kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
+    launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
+    const int combine = stage > 0;
+    const double wc = combine ? e.wc[stage - 1] : 1.0, w0 = combine ? e.w0[stage - 1] : 0.0;
+    if (nan_check) {
+      launch_ct(e, 0, 1.0, 0.0);
+      launch_nan_check(e);
+      if (combine) k_faces_combine<<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
+    } else {
+      launch_ct(e, combine, wc, w0);
+    }
+    mark_begin(e, kKStageEnd);
+    IDFX_DISPATCH_D(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0);
+    mark_end(e);
+  }
+  k_cycle_end<<<1, 1, 0, e.stream>>>(e.ctl);
+  e.ncycles++;
+}
+
+int read_ctl(Engine& e) {
+  IDFX_CK(cudaMemcpyAsync(e.ctl_host, e.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e.stream));
+  IDFX_CK(cudaStreamSynchronize(e.stream));
+  return IDFX_OK;
+}
+
+const char* status_text(int s) {
+  switch (s) {
+    case kErrNan: return "Nan found after integration cycle";
+    case kErrDivB: return "divB too large, check your calculation";
+    case kErrDtSmall: return "dt is too small";
+    case kErrFirstDt: return "Your guessed first_dt is too large. Try to reduce first_dt.";
+    default: return "error";
+  }
+}
+
+int choose_segments(Engine& e) {
+  // enough marching columns x segments to fill the GPU (>= ~512 threads/SM)
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (long long)sms * 512;
+  for (int d = 1; d < e.g.D; d++) {
+    const long long cols = (long long)(e.g.n[0] + 2 * e.g.ext) * (e.g.D == 3 ? e.g.n[3 - d] + 2 * e.g.ext : 1);
+    int s = 64;
+    while (s > 2 && cols * ((e.g.n[d] + s - 1) / s) < want) s /= 2;
+    e.seg[d] = s;
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+void idfx_gpu_default_config(idfx_gpu_config* c, int dims, int nx, int ny, int nz) {
+  std::memset(c, 0, sizeof(*c));
+  c->dims = dims;
+  c->n[0] = nx;
+  c->n[1] = ny;
+  c->n[2] = dims == 3 ? nz : 1;
+  for (int d = 0; d < 3; d++) {
+    c->xbeg[d] = 0.0;
+    c->xend[d] = 1.0;
+  }
+  c->order = IDFX_PLM;
+  c->solver = IDFX_HLLD;
+  c->emf = IDFX_EMF_UCT_CONTACT;
+  c->nstages = 2;
+  c->gamma = 5.0 / 3.0;
+  c->cfl = 0.9;
+  c->cfl_max_var = 1.1;   // timeIntegrator.cpp:40
+  c->first_dt = 1.0e-10;  // timeIntegrator.cpp:41
+  c->maxdivb = 1e-6;      // timeIntegrator.cpp:56
+  c->log_period = 100;    // timeIntegrator.cpp:44
+  c->check_nan_period = 100;
+  c->precision = IDFX_FP64;
+}
+
+int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
+  if (!cfg || !out) return IDFX_ERR_STATE;
+  *out = nullptr;
+  if (cfg->dims != 2 && cfg->dims != 3) return IDFX_ERR_CONFIG;
+  if (cfg->order < 1 || cfg->order > 4 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
+  if (cfg->emf < 0 || cfg->emf > 4 || cfg->nstages < 1 || cfg->nstages > 3) return IDFX_ERR_CONFIG;
+  if (cfg->precision != IDFX_FP64) return IDFX_ERR_CONFIG;
+  // constrainedTransport.hpp:256-261
+  if (cfg->emf == IDFX_EMF_UCT_HLLD && (cfg->solver == IDFX_HLL || cfg->solver == IDFX_TVDLF))
+    return IDFX_ERR_CONFIG;
+  for (int d = 0; d < cfg->dims; d++)
+    if (cfg->n[d] < 2 || !(cfg->xend[d] > cfg->xbeg[d])) return IDFX_ERR_CONFIG;
+  idfx_gpu* h = new (std::nothrow) idfx_gpu();
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  Geo& g = e.g;
+  g.D = cfg->dims;
+  g.order = cfg->order;
+  g.solver = cfg->solver;
+  g.emf = cfg->emf;
+  g.nstages = cfg->nstages;
+  g.ng = (cfg->order == 4) ? 3 : 2;  // grid.cpp:60-65
+  for (int d = 0; d < 3; d++) {
+    const bool act = d < g.D;
+    const int gd = act ? g.ng : 0;
+    g.n[d] = act ? cfg->n[d] : 1;
+    g.nt[d] = g.n[d] + 2 * gd;
+    g.ntv[d] = g.nt[d] + (act ? 1 : 0);
+    g.beg[d] = gd;
+    g.end[d] = gd + g.n[d];
+    const double xb = act ? cfg->xbeg[d] : 0.0, xe = act ? cfg->xend[d] : 1.0;
+    g.dx[d] = (xe - xb) / (g.n[d]);  // gridHost.cpp:80-86
+  }
+  g.s[0] = 1;
+  g.s[1] = g.nt[0];
+  g.s[2] = (long long)g.nt[0] * g.nt[1];
+  g.fs[0] = 1;
+  g.fs[1] = g.ntv[0];
+  g.fs[2] = (long long)g.ntv[0] * g.ntv[1];
+  g.ncell = (long long)g.nt[0] * g.nt[1] * g.nt[2];
+  g.nface = (long long)g.ntv[0] * g.ntv[1] * g.ntv[2];
+  if (g.D == 2) {  // makeGeometry.cpp (Cartesian): D_EXPAND products
+    g.A[0] = 1.0 * g.dx[1];
+    g.A[1] = g.dx[0] * 1.0;
+    g.A[2] = 1.0;
+  } else {
+    g.A[0] = 1.0 * g.dx[1] * g.dx[2];
+    g.A[1] = g.dx[0] * 1.0 * g.dx[2];
+    g.A[2] = g.dx[0] * g.dx[1] * 1.0;
+  }
+  g.gamma = cfg->gamma;
+  g.gm1 = cfg->gamma - 1.0;
+  g.ext = 1;  // hlldMHD.hpp:30-49: uct_hll(d) with HLLD/HLL needs nghost cells
+  if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
+  e.nstages = cfg->nstages;
+  if (e.nstages == 2) {  // timeIntegrator.cpp:62-71
+    e.wc[0] = 0.5;
+    e.w0[0] = 0.5;
+  }
+  if (e.nstages == 3) {
+    e.wc[0] = 0.25;
+    e.w0[0] = 0.75;
+    e.wc[1] = 2.0 / 3.0;
+    e.w0[1] = 1.0 / 3.0;
+  }
+  e.log_period = cfg->log_period;
+  e.check_nan_period = cfg->check_nan_period;
+
+  // device buffers: one pool, zero-initialised like Kokkos views
+  const int NV = 2 * g.D + 2;
+  const size_t nc = (size_t)g.ncell, nf = (size_t)g.nface;
+  const bool hll_emf = (g.emf == kEmfUctHll || g.emf == kEmfUctHlld);
+  size_t len = 3 * NV * nc + 2 * g.D * nf + nc  // Vc, Uc, Uc0, Vs, Vs0, InvDt
+               + 6 * nc + 3 * nc + 3 * nc + 3 * nc  // face EMFs, sv, cell EMFs, corner EMFs
+               + (hll_emf ? 12 * nc : 0);
+  int rc = IDFX_OK;
+  if (stream) {
+    e.stream = (cudaStream_t)stream;
+  } else {
+    rc = cuda_check(e, cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    e.own_stream = (rc == IDFX_OK);
+  }
+  if (rc == IDFX_OK) rc = cuda_check(e, cudaMalloc(&e.pool, len * sizeof(double)), "cudaMalloc(fields)");
+  if (rc == IDFX_OK) rc = cuda_check(e, cudaMemsetAsync(e.pool, 0, len * sizeof(double), e.stream), "cudaMemset");
+  if (rc == IDFX_OK) rc = cuda_check(e, cudaMalloc(&e.ctl, sizeof(Ctl)), "cudaMalloc(ctl)");
+  if (rc == IDFX_OK) rc = cuda_check(e, cudaMallocHost(&e.ctl_host, sizeof(Ctl)), "cudaMallocHost(ctl)");
+  if (rc != IDFX_OK) {
+    std::fprintf(stderr, "idfx_gpu_create: %s\n", e.err.c_str());
+    idfx_gpu_destroy(h);
+    return rc;
+  }
+  e.pool_len = len;
+  double* p = e.pool;
+  auto take = [&](size_t n) { double* q = p; p += n; return q; };
+  Fields& f = e.f;
+  f.Vc = take(NV * nc);
+  f.Uc = take(NV * nc);
+  f.Uc0 = take(NV * nc);
+  f.Vs = take(g.D * nf);
+  f.Vs0 = take(g.D * nf);
+  f.InvDt = take(nc);
+  f.ezi = take(nc); f.ezj = take(nc); f.exj = take(nc); f.exk = take(nc); f.eyi = take(nc); f.eyk = take(nc);
+  f.svx = take(nc); f.svy = take(nc); f.svz = take(nc);
+  f.Ex1 = take(nc); f.Ex2 = take(nc); f.Ex3 = take(nc);
+  f.ex = take(nc); f.ey = take(nc); f.ez = take(nc);
+  for (int d = 0; d < 3; d++) {
+    f.aL[d] = hll_emf ? take(nc) : nullptr;
+    f.aR[d] = hll_emf ? take(nc) : nullptr;
+    f.dL[d] = hll_emf ? take(nc) : nullptr;
+    f.dR[d] = hll_emf ? take(nc) : nullptr;
+  }
+  Ctl c{};
+  c.t = 0.0;
+  c.dt = cfg->first_dt;
+  c.tstop = -1.0;
+  c.cfl = cfg->cfl;
+  c.cflmax = cfg->cfl_max_var;
+  c.maxdivb = cfg->maxdivb;
+  *e.ctl_host = c;
+  rc = cuda_check(e, cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream), "ctl");
+  if (rc == IDFX_OK) rc = cuda_check(e, cudaStreamSynchronize(e.stream), "sync");
+  if (rc != IDFX_OK) {
+    idfx_gpu_destroy(h);
+    return rc;
+  }
+  choose_segments(e);
+  *out = h;
+  return IDFX_OK;
+}
+
+int idfx_gpu_profile(idfx_gpu* h, int enable) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  IDFX_CK(cudaStreamSynchronize(e.stream));
+  for (auto& m : e.marks) {
+    e.free_events.push_back(m.a);
+    e.free_events.push_back(m.b);
+  }
+  e.marks.clear();
+  e.profile = enable != 0;
+  return IDFX_OK;
+}
+
+int idfx_gpu_profile_read(idfx_gpu* h, double* ms, long long* launches, int nclasses) {
+  if (!h || !ms || !launches) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  IDFX_CK(cudaStreamSynchronize(e.stream));
+  for (int c = 0; c < nclasses; c++) {
+    ms[c] = 0.0;
+    launches[c] = 0;
+  }
+  for (auto& m : e.marks) {
+    float t = 0.f;
+    IDFX_CK(cudaEventElapsedTime(&t, m.a, m.b));
+    if (m.cls < nclasses) {
+      ms[m.cls] += t;
+      launches[m.cls] += 1;
+    }
+  }
+  return IDFX_OK;
+}
+
+int idfx_gpu_destroy(idfx_gpu* h) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  if (e.stream) cudaStreamSynchronize(e.stream);
+  for (auto& m : e.marks) {
+    cudaEventDestroy(m.a);
+    cudaEventDestroy(m.b);
+  }
+  for (auto ev : e.free_events) cudaEventDestroy(ev);
+  if (e.pool) cudaFree(e.pool);
+  if (e.ctl) cudaFree(e.ctl);
+  if (e.ctl_host) cudaFreeHost(e.ctl_host);
+  if (e.own_stream && e.stream) cudaStreamDestroy(e.stream);
+  delete h;
+  return IDFX_OK;
+}
+
+int idfx_gpu_last_error(const idfx_gpu* h, char* buf, size_t len) {
+  if (!h || !buf || len == 0) return IDFX_ERR_STATE;
+  std::snprintf(buf, len, "%s", h->e.err.c_str());
+  return IDFX_OK;
+}
+
+int idfx_gpu_sizes(const idfx_gpu* h, int* nvar, int* nghost, long long* vc_len, long long* vs_len) {
+  if (!h) return IDFX_ERR_STATE;
+  const Geo& g = h->e.g;
+  if (nvar) *nvar = 2 * g.D + 2;
+  if (nghost) *nghost = g.ng;
+  if (vc_len) *vc_len = (2 * g.D + 2) * g.ncell;
+  if (vs_len) *vs_len = g.D * g.nface;
+  return IDFX_OK;
+}
+
+static int copy_state(idfx_gpu* h, const double* Vc, const double* Vs, cudaMemcpyKind kind, bool up) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  const size_t bc = sizeof(double) * (2 * e.g.D + 2) * e.g.ncell;
+  const size_t bs = sizeof(double) * e.g.D * e.g.nface;
+  if (up) {
+    if (Vc) IDFX_CK(cudaMemcpyAsync(e.f.Vc, Vc, bc, kind, e.stream));
+    if (Vs) IDFX_CK(cudaMemcpyAsync(e.f.Vs, Vs, bs, kind, e.stream));
+  } else {
+    if (Vc) IDFX_CK(cudaMemcpyAsync((void*)Vc, e.f.Vc, bc, kind, e.stream));
+    if (Vs) IDFX_CK(cudaMemcpyAsync((void*)Vs, e.f.Vs, bs, kind, e.stream));
+  }
+  IDFX_CK(cudaStreamSynchronize(e.stream));
+  return IDFX_OK;
+}
+
+int idfx_gpu_upload_prim(idfx_gpu* h, const double* Vc, const double* Vs) {
+  return copy_state(h, Vc, Vs, cudaMemcpyHostToDevice, true);
+}
+int idfx_gpu_download_prim(idfx_gpu* h, double* Vc, double* Vs) {
+  return copy_state(h, Vc, Vs, cudaMemcpyDeviceToHost, false);
+}
+int idfx_gpu_upload_prim_device(idfx_gpu* h, const double* Vc, const double* Vs) {
+  return copy_state(h, Vc, Vs, cudaMemcpyDeviceToDevice, true);
+}
+int idfx_gpu_download_prim_device(idfx_gpu* h, double* Vc, double* Vs) {
+  return copy_state(h, Vc, Vs, cudaMemcpyDeviceToDevice, false);
+}
+int idfx_gpu_download_cons(idfx_gpu* h, double* Uc) {
+  if (!h || !Uc) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  IDFX_CK(cudaMemcpyAsync(Uc, e.f.Uc, sizeof(double) * (2 * e.g.D + 2) * e.g.ncell, cudaMemcpyDeviceToHost,
+                          e.stream));
+  IDFX_CK(cudaStreamSynchronize(e.stream));
+  return IDFX_OK;
+}
+
+int idfx_gpu_set_time(idfx_gpu* h, double t, double dt, long long ncycles) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  int rc = read_ctl(e);
+  if (rc) return rc;
+  e.ctl_host->t = t;
+  e.ctl_host->dt = dt;
+  e.ctl_host->ncycles = ncycles;
+  e.ctl_host->done = 0;
+  e.ctl_host->status = 0;
+  e.ncycles = ncycles;
+  IDFX_CK(cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream));
+  IDFX_CK(cudaStreamSynchronize(e.stream));
+  return IDFX_OK;
+}
+
+int idfx_gpu_get_time(idfx_gpu* h, double* t, double* dt, long long* ncycles) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  int rc = read_ctl(e);
+  if (rc) return rc;
+  if (t) *t = e.ctl_host->t;
+  if (dt) *dt = e.ctl_host->dt;
+  if (ncycles) *ncycles = e.ctl_host->ncycles;
+  return IDFX_OK;
+}
+
+// run cycles; the device flags `done` when t reaches tstop or on error
+static int run_cycles(idfx_gpu* h, double tstop, long long max_cycles) {
+  Engine& e = h->e;
+  int rc = read_ctl(e);
+  if (rc) return rc;
+  e.ctl_host->tstop = tstop;
+  e.ctl_host->done = 0;
+  e.ctl_host->status = 0;
+  e.ncycles = e.ctl_host->ncycles;
+  IDFX_CK(cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream));
+  const int use_tstop = tstop >= 0.0;
+  long long done = 0;
+  const long long chunk = 64;  // host polls t / status every chunk of queued cycles
+  while (max_cycles < 0 || done < max_cycles) {
+    long long n = chunk;
+    if (max_cycles >= 0 && max_cycles - done < n) n = max_cycles - done;
+    for (long long q = 0; q < n; q++) queue_cycle(e, use_tstop);
+    done += n;
+    IDFX_CK(cudaGetLastError());
+    rc = read_ctl(e);
+    if (rc) return rc;
+    e.ncycles = e.ctl_host->ncycles;
+    if (e.ctl_host->status) return fail(e, e.ctl_host->status, status_text(e.ctl_host->status));
+    if (e.ctl_host->done) break;
+    if (!use_tstop && max_cycles < 0) break;
+  }
+  return IDFX_OK;
+}
+
+int idfx_gpu_cycle(idfx_gpu* h) {
+  if (!h) return IDFX_ERR_STATE;
+  return run_cycles(h, -1.0, 1);
+}
+
+int idfx_gpu_run(idfx_gpu* h, double tstop, long long max_cycles) {
+  if (!h) return IDFX_ERR_STATE;
+  if (tstop < 0.0 && max_cycles < 0) return fail(h->e, IDFX_ERR_CONFIG, "run needs tstop or max_cycles");
+  return run_cycles(h, tstop, max_cycles);
+}
+
+// ---------------------------------------------------------------------------
+// building blocks
+// ---------------------------------------------------------------------------
+// the building blocks run whatever the time-integrator control says
+static void clear_done(Engine& e) { cudaMemsetAsync(&e.ctl->done, 0, sizeof(int), e.stream); }
+
+static int sync_status(Engine& e) {
+  IDFX_CK(cudaGetLastError());
+  IDFX_CK(cudaStreamSynchronize(e.stream));
+  return IDFX_OK;
+}
+
+int idfx_gpu_set_boundaries(idfx_gpu* h) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  clear_done(e);
+  launch_fill_faces(e, 0);
+  launch_stage_begin(e, 0);
+  return sync_status(e);
+}
+
+int idfx_gpu_prim_to_cons(idfx_gpu* h) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  clear_done(e);
+  IDFX_DISPATCH_D(k_prim_to_cons_all, nblocks(e.g.ncell), kThreads, e.g, e.f);
+  return sync_status(e);
+}
+
+int idfx_gpu_cons_to_prim(idfx_gpu* h) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  clear_done(e);
+  IDFX_DISPATCH_D(k_uc_field_all, nblocks(e.g.ncell), kThreads, e.g, e.f, 1);
+  return sync_status(e);
+}
+
+int idfx_gpu_reset_stage(idfx_gpu* h) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  IDFX_CK(cudaMemsetAsync(e.f.InvDt, 0, sizeof(double) * e.g.ncell, e.stream));
+  return sync_status(e);
+}
+
+int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt) {
+  (void)t;
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  clear_done(e);
+  k_set_stage_dt<<<1, 1, 0, e.stream>>>(e.g, e.ctl, dt);
+  if (e.g.emf == kEmfContact || e.g.emf == kEmfUct0)
+    IDFX_DISPATCH_D(k_cell_emf_all, nblocks(e.g.ncell), kThreads, e.g, e.f);
+  launch_sweeps(e, 2, 0);
+  launch_ct(e, 0, 1.0, 0.0);
+  IDFX_DISPATCH_D(k_uc_field_all, nblocks(e.g.ncell), kThreads, e.g, e.f, 0);
+  return sync_status(e);
+}
+
+int idfx_gpu_compute_timestep(idfx_gpu* h, double* dt) {
+  if (!h || !dt) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  IDFX_CK(cudaMemsetAsync(&e.ctl->invdt_max_bits, 0, sizeof(unsigned long long), e.stream));
+  IDFX_DISPATCH_D(k_invdt_max, nblocks(n_active(e.g)), kThreads, e.g, e.f, e.ctl);
+  int rc = sync_status(e);
+  if (rc) return rc;
+  rc = read_ctl(e);
+  if (rc) return rc;
+  unsigned long long b = e.ctl_host->invdt_max_bits;
+  double m;
+  std::memcpy(&m, &b, sizeof(m));
+  *dt = 1.0 / m;
+  return IDFX_OK;
+}
+
+int idfx_gpu_check_divb(idfx_gpu* h, double* divb) {
+  if (!h || !divb) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  IDFX_CK(cudaMemsetAsync(&e.ctl->divb_bits, 0, sizeof(unsigned long long), e.stream));
+  IDFX_DISPATCH_D(k_divb, nblocks(n_active(e.g)), kThreads, e.g, e.f, e.ctl);
+  int rc = read_ctl(e);
+  if (rc) return rc;
+  unsigned long long b = e.ctl_host->divb_bits;
+  std::memcpy(divb, &b, sizeof(double));
+  return IDFX_OK;
+}
+
+int idfx_gpu_check_nan(idfx_gpu* h, long long* count) {
+  if (!h || !count) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  IDFX_CK(cudaMemsetAsync(&e.ctl->nan_count, 0, sizeof(unsigned long long), e.stream));
+  IDFX_DISPATCH_D(k_nan_count, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
+  int rc = read_ctl(e);
+  if (rc) return rc;
+  *count = (long long)e.ctl_host->nan_count;
+  return IDFX_OK;
+}
+
+}  // extern "C"

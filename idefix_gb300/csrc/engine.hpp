@@ -1,0 +1,64 @@
+// Host side of one GPU block: device buffers, control block and the
+// TimeIntegrator::Cycle driver (timeIntegrator.cpp:246-414) behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "mhd_kernels.cuh"
+
+namespace idfx {
+
+struct Engine {
+  Geo g{};
+  Fields f{};
+  Ctl* ctl = nullptr;        // device control block
+  Ctl* ctl_host = nullptr;   // pinned mirror for reads
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int nstages = 2;
+  double wc[2] = {0, 0}, w0[2] = {0, 0};
+  int log_period = 0, check_nan_period = 0;
+  long long ncycles = 0;     // host mirror of the cycle counter
+  int seg[3] = {32, 32, 32}; // marching segment per direction
+  std::string err;
+  double* pool = nullptr;    // one allocation for every field
+  size_t pool_len = 0;
+  // optional per-kernel timing: CUDA events around every launch of a class
+  bool profile = false;
+  struct Mark {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> free_events;
+};
+
+// kernel classes reported by the per-kernel timing
+enum KernelClass {
+  kKFillFaces = 0,
+  kKStageBegin,
+  kKSweepX,
+  kKSweepY,
+  kKSweepZ,
+  kKCtCorner,
+  kKCtFaces,
+  kKStageEnd,
+  kKControl,
+  kKChecks,
+  kKNumClasses
+};
+
+cudaEvent_t take_event(Engine& e);
+void mark_begin(Engine& e, int cls);
+void mark_end(Engine& e);
+
+// launches the D flux sweeps of one stage (one function per Riemann solver,
+// each in its own translation unit)
+void launch_sweeps_hlld(Engine& e, int invdt, int fold_max);
+void launch_sweeps_hll(Engine& e, int invdt, int fold_max);
+void launch_sweeps_roe(Engine& e, int invdt, int fold_max);
+void launch_sweeps_tvdlf(Engine& e, int invdt, int fold_max);
+
+}  // namespace idfx

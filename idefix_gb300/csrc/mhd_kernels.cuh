@@ -1,0 +1,825 @@
+// Kernels of one Runge-Kutta stage of the ideal-MHD Godunov step on a
+// periodic Cartesian block, FP64, bit-identical to the reference.
+//
+// Device state keeps the reference layout (LayoutRight, ghost zones,
+// face arrays padded by one in every active dimension) so that the C-ABI
+// moves host arrays in and out unchanged:
+//   Vc[nvar][nt2][nt1][nt0]   Vs[D][ntv2][ntv1][ntv0]
+//
+// Stage = fill_faces -> stage_begin -> sweep x, y(, z) -> ct_corner ->
+// ct_faces -> stage_end.  Each face's Riemann problem is solved once and
+// each cell's reconstruction is evaluated once per direction; fluxes never
+// leave the chip (shared memory for x, registers for y/z).
+#pragma once
+#include <cstdint>
+
+#include "mhd_math.cuh"
+
+namespace idfx {
+
+enum EmfMode { kEmfContact = 0, kEmfArithmetic = 1, kEmfUct0 = 2, kEmfUctHll = 3, kEmfUctHlld = 4 };
+enum Status {
+  kOk = 0,
+  kErrConfig = 1,
+  kErrNan = 2,
+  kErrDivB = 3,
+  kErrDtSmall = 4,
+  kErrFirstDt = 5,
+  kErrCuda = 6,
+  kErrState = 7
+};
+
+// Geometry and scheme of one block (passed by value to every kernel).
+struct Geo {
+  int D, ng, order, solver, emf, nstages;
+  int n[3], nt[3], ntv[3], beg[3], end[3];
+  long long ncell, nface;
+  long long s[3];   // cell strides
+  long long fs[3];  // face strides
+  double dx[3];
+  double A[3];  // face areas (makeGeometry.cpp:146-147,178-179,201-202)
+  double gamma, gm1;
+  int ext;  // perpendicular extension of the flux sweeps for CT
+};
+
+// Device-resident time-integrator control block.
+struct Ctl {
+  double t, dt, t0, tstop;
+  double dtdV;        // dt / dV
+  double dtdx[3];     // dt / dx[d]
+  double cfl, cflmax, maxdivb;
+  unsigned long long invdt_max_bits;  // max over active cells of InvDt (stage 0)
+  unsigned long long divb_bits;       // max of the divB estimator
+  unsigned long long nan_count;
+  long long ncycles;
+  int done;    // 1: every kernel returns at entry
+  int status;  // Status
+};
+
+struct Fields {
+  double *Vc, *Uc, *Uc0, *Vs, *Vs0, *InvDt;
+  double *ezi, *ezj, *exj, *exk, *eyi, *eyk;
+  double *svx, *svy, *svz;
+  double *Ex1, *Ex2, *Ex3;
+  double *ex, *ey, *ez;
+  double *aL[3], *aR[3], *dL[3], *dR[3];
+};
+
+__device__ __forceinline__ long long cidx(const Geo& g, int k, int j, int i) {
+  return ((long long)k * g.nt[1] + j) * g.nt[0] + i;
+}
+__device__ __forceinline__ long long fidx(const Geo& g, int k, int j, int i) {
+  return ((long long)k * g.ntv[1] + j) * g.ntv[0] + i;
+}
+// periodic image of a ghost index (boundary.hpp:588-606); n active cells
+__device__ __forceinline__ int wrap(int i, int g, int n) { return g + (i + g * (n - 1)) % n; }
+
+// non-negative doubles order like their bit patterns
+__device__ __forceinline__ void atomic_max_pos(unsigned long long* p, double v) {
+  if (!(v >= 0.0)) return;  // NaN ignored, like fmin/fmax in the reference reduction
+  atomicMax(p, (unsigned long long)__double_as_longlong(v));
+}
+
+// ---------------------------------------------------------------------------
+// Ghost faces of Vs (Boundary::EnforcePeriodic on Vs, boundary.hpp:608-670),
+// plus the Runge-Kutta "begin" copy of the active faces at stage 0.
+// One thread per location of the padded face box of one component.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
+  if (ctl->done) return;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int comp = blockIdx.y;
+  if (tid >= g.nface) return;
+  int i = (int)(tid % g.ntv[0]);
+  long long r = tid / g.ntv[0];
+  int j = (int)(r % g.ntv[1]);
+  int k = (int)(r / g.ntv[1]);
+  const int idx3[3] = {i, j, k};
+  int src[3] = {i, j, k};
+  bool ghost = false;
+  for (int d = 0; d < D; d++) {
+    const int v = idx3[d];
+    const int hi = (d == comp) ? g.end[d] : g.end[d] - 1;  // last evolved face / cell
+    if (d != comp && v == g.nt[d]) return;                 // padding, never used
+    if (v < g.beg[d] || v > hi) {
+      ghost = true;
+      src[d] = wrap(v, g.ng, g.n[d]);
+    }
+  }
+  double* vs = f.Vs + (long long)comp * g.nface;
+  const long long fi = fidx(g, k, j, i);
+  if (ghost) {
+    vs[fi] = vs[fidx(g, src[2], src[1], src[0])];
+  } else if (save_begin) {
+    f.Vs0[(long long)comp * g.nface + fi] = vs[fi];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage begin: ghost cells of Vc (periodic image), cell-centred field from
+// the faces (ReconstructVcField, boundary.hpp:388-404), conservative state of
+// the active cells (ConvertPrimToCons), RK begin copy, and the cell-centred
+// EMF E = -v x B used by uct_contact / uct0 (calcCornerEmf.hpp:84-126).
+// ---------------------------------------------------------------------------
+enum { kSbCons = 1, kSbSaveBegin = 2, kSbCellEmf = 4 };
+
+template <int D>
+__global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
+  if (ctl->done) return;
+  using v = Var<D>;
+  constexpr int NV = v::NV;
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.ncell) return;
+  int i = (int)(c % g.nt[0]);
+  long long r = c / g.nt[0];
+  int j = (int)(r % g.nt[1]);
+  int k = (int)(r / g.nt[1]);
+  int src[3] = {i, j, k};
+  bool ghost = false;
+  const int idx3[3] = {i, j, k};
+  for (int d = 0; d < D; d++) {
+    if (idx3[d] < g.beg[d] || idx3[d] >= g.end[d]) {
+      ghost = true;
+      src[d] = wrap(idx3[d], g.ng, g.n[d]);
+    }
+  }
+  double V[NV];
+  const long long cs = cidx(g, src[2], src[1], src[0]);
+#pragma unroll
+  for (int n = 0; n < v::BX1; n++) V[n] = f.Vc[n * g.ncell + cs];
+  const long long fc = fidx(g, k, j, i);
+#pragma unroll
+  for (int d = 0; d < D; d++) {
+    const double* vs = f.Vs + d * g.nface;
+    V[v::BX1 + d] = 0.5 * (vs[fc] + vs[fc + g.fs[d]]);
+  }
+  if (ghost) {
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) f.Vc[n * g.ncell + c] = V[n];
+  }
+#pragma unroll
+  for (int d = 0; d < D; d++) f.Vc[(v::BX1 + d) * g.ncell + c] = V[v::BX1 + d];
+  if (!ghost && (flags & kSbCons)) {
+    double U[NV];
+    prim_to_cons<D>(g.gm1, U, V);
+#pragma unroll
+    for (int n = 0; n < NV; n++) f.Uc[n * g.ncell + c] = U[n];
+    if (flags & kSbSaveBegin) {
+#pragma unroll
+      for (int n = 0; n < NV; n++) f.Uc0[n * g.ncell + c] = U[n];
+    }
+  }
+  if (flags & kSbCellEmf) {
+    const double vx1 = V[v::MX1], vx2 = V[v::MX2];
+    const double Bx1 = V[v::BX1], Bx2 = V[v::BX2];
+    if constexpr (D == 3) {
+      const double vx3 = V[v::MX3], Bx3 = V[v::BX3];
+      f.Ex1[c] = (vx3 * Bx2 - vx2 * Bx3);
+      f.Ex2[c] = (vx1 * Bx3 - vx3 * Bx1);
+    }
+    f.Ex3[c] = (vx2 * Bx1 - vx1 * Bx2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// EMF side outputs of a face (storeFlux.hpp:14-208)
+// ---------------------------------------------------------------------------
+template <int D, int DIR>
+__device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long long c,
+                                          const RiemannOut<D>& r, const double* vL,
+                                          const double* vR) {
+  using d = Dir<D, DIR>;
+  using vv = Var<D>;
+  double st, sb;
+  double *Et, *Eb, *SV;
+  if constexpr (DIR == 0) {
+    st = -1.0; sb = +1.0; Et = f.ezi; Eb = f.eyi; SV = f.svx;
+  } else if constexpr (DIR == 1) {
+    st = +1.0; sb = -1.0; Et = f.ezj; Eb = f.exj; SV = f.svy;
+  } else {
+    st = -1.0; sb = +1.0; Et = f.eyk; Eb = f.exk; SV = f.svz;
+  }
+  if (g.emf == kEmfContact || g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
+    Et[c] = st * r.F[d::BXt];
+    if constexpr (D == 3) Eb[c] = sb * r.F[d::BXb];
+    if (g.emf == kEmfContact) {
+      double s = 0.5;
+      if (r.F[vv::RHO] > kEpsUctContact) s = 1.0;
+      if (r.F[vv::RHO] < -kEpsUctContact) s = 0.0;
+      SV[c] = s;
+    }
+    return;
+  }
+  double* aL = f.aL[DIR];
+  double* aR = f.aR[DIR];
+  double* dL = f.dL[DIR];
+  double* dR = f.dR[DIR];
+  const double sl = r.sl, sr = r.sr;
+  if (g.emf == kEmfUctHll) {
+    const double ar = fmax(0.0, sr);
+    const double al = fmin(0.0, sl);
+    const double scrh = 1.0 / (ar - al);
+    Et[c] = -st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh;
+    if constexpr (D == 3) Eb[c] = -sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh;
+    aL[c] = ar * scrh;
+    aR[c] = -al * scrh;
+    const double dr = -al * ar * scrh;
+    dR[c] = dr;
+    dL[c] = dr;
+    return;
+  }
+  // uct_hlld (K_StoreHLLD, energy branch)
+  const double* uL = r.uL;
+  const double* uR = r.uR;
+  const double ptL = vL[vv::PRS] + half_b2<D>(vL);
+  const double ptR = vR[vv::PRS] + half_b2<D>(vR);
+  int revert_to_hll = 0;
+  const double Bn = (sr * vR[d::BXn] - sl * vL[d::BXn]) / (sr - sl);
+  const double duL = sl - vL[d::Xn];
+  const double duR = sr - vR[d::Xn];
+  double scrh = 1.0 / (duR * uR[vv::RHO] - duL * uL[vv::RHO]);
+  const double Sc = (duR * uR[d::Xn] - duL * uL[d::Xn] - ptR + ptL) * scrh;
+  const double usLRHO = uL[vv::RHO] * duL / (sl - Sc);
+  const double usRRHO = uR[vv::RHO] * duR / (sr - Sc);
+  const double sqrL = sqrt(usLRHO);
+  const double sqrR = sqrt(usRRHO);
+  const double SaL = Sc - fabs(Bn) / sqrL;
+  const double SaR = Sc + fabs(Bn) / sqrR;
+  if ((SaL - sl) < 1e-4 * (Sc - sl)) revert_to_hll = 1;
+  if ((SaR - sr) > -1e-4 * (sr - Sc)) revert_to_hll = 1;
+  const double chiL = (vL[d::Xn] - Sc) * (sl - Sc) / (SaL + sl - 2.0 * Sc);
+  const double chiR = (vR[d::Xn] - Sc) * (sr - Sc) / (SaR + sr - 2.0 * Sc);
+  const double nuL = (SaL + sl) / (fabs(SaL) + fabs(sl));
+  const double nuR = (SaR + sr) / (fabs(SaR) + fabs(sr));
+  const double nuLR = (SaL + SaR) / (fabs(SaL) + fabs(SaR));
+  double a_l, a_r, d_l, d_r;
+  if (fabs(SaR - SaL) > 1.e-9 * fabs(sr - sl)) {
+    d_l = 0.5 * (chiL * nuL - chiL * nuLR) + 0.5 * (fabs(SaL) - nuLR * SaL);
+    d_r = 0.5 * (chiR * nuR - chiR * nuLR) + 0.5 * (fabs(SaR) - nuLR * SaR);
+    a_l = 0.5 * (1.0 + nuLR);
+    a_r = 0.5 * (1.0 - nuLR);
+  } else {
+    d_l = 0.5 * chiL * nuL + 0.5 * fabs(SaL);
+    d_r = 0.5 * chiR * nuR + 0.5 * fabs(SaR);
+    a_l = 0.5;
+    a_r = 0.5;
+  }
+  const double ar = fmax(0.0, sr);
+  const double al = fmin(0.0, sl);
+  scrh = 1.0 / (ar - al);
+  if (revert_to_hll) {
+    a_l = ar * scrh;
+    a_r = -al * scrh;
+    d_r = -al * ar * scrh;
+    d_l = d_r;
+  }
+  aL[c] = a_l;
+  aR[c] = a_r;
+  dL[c] = d_l;
+  dR[c] = d_r;
+  Et[c] = -st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh;
+  if constexpr (D == 3) Eb[c] = -sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh;
+}
+
+// ---------------------------------------------------------------------------
+// x sweep: one block = TX faces of one (j,k) row.  Phase 1 reconstructs the
+// TX+2 cells once into shared memory, phase 2 solves TX+1 Riemann problems,
+// phase 3 applies the flux difference (Fluid_CorrectFluxFunctor +
+// Fluid_CalcRHSFunctor, calcRightHandSide.hpp:84-195,333-550).
+// ---------------------------------------------------------------------------
+constexpr int kTX = 64;
+
+// invdt: 0 = no InvDt work, 1 = first contribution of a cycle (InvDt was
+// reset to 0), 2 = accumulate onto the stored InvDt.  last_dir: fold the
+// completed InvDt into the device maximum used for the next dt.
+template <int D, int ORDER, int SOLVER>
+__global__ void __launch_bounds__(kTX) k_sweep_x(Geo g, Fields f, const Ctl* ctl, int invdt,
+                                                 int last_dir) {
+  if (ctl->done) return;
+  using v = Var<D>;
+  using dd = Dir<D, 0>;
+  constexpr int NV = v::NV;
+  constexpr int H = Recon<ORDER>::H;
+  __shared__ double sL[NV][kTX + 2], sR[NV][kTX + 2];
+  __shared__ double sF[NV][kTX + 1];
+  __shared__ double sC[kTX + 1];
+  const int i0 = g.beg[0] + blockIdx.x * kTX;
+  const int j = g.beg[1] - g.ext + blockIdx.y;
+  const int k = (D == 3) ? g.beg[2] - g.ext + (int)blockIdx.z : 0;
+  const bool active_row = (j >= g.beg[1] && j < g.end[1]) && (D == 2 || (k >= g.beg[2] && k < g.end[2]));
+  const long long rowc = cidx(g, k, j, 0);
+  // phase 1: cells i0-1 .. min(i0+kTX, end0)
+  for (int t = threadIdx.x; t < kTX + 2; t += kTX) {
+    const int c = i0 - 1 + t;
+    if (c > g.end[0]) continue;
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      if (n == dd::BXn) continue;
+      const double* q = f.Vc + n * g.ncell + rowc + c;
+      double w[2 * H + 1];
+#pragma unroll
+      for (int m = 0; m <= 2 * H; m++) w[m] = q[m - H];
+      double vl, vr;
+      Recon<ORDER>::cell(w, g.dx[0], n == v::RHO || n == v::PRS, vl, vr);
+      sL[n][t] = vl;
+      sR[n][t] = vr;
+    }
+  }
+  __syncthreads();
+  // phase 2: faces i0 .. min(i0+kTX, end0)
+  for (int t = threadIdx.x; t < kTX + 1; t += kTX) {
+    const int fi = i0 + t;
+    if (fi > g.end[0]) continue;
+    double vL[NV], vR[NV];
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      if (n == dd::BXn) continue;
+      vL[n] = sR[n][t];
+      vR[n] = sL[n][t + 1];
+    }
+    const double bn = f.Vs[fidx(g, k, j, fi)];
+    vL[dd::BXn] = bn;
+    vR[dd::BXn] = bn;
+    RiemannOut<D> r;
+    riemann<D, 0, SOLVER>(g.gamma, vL, vR, r);
+    store_emf<D, 0>(g, f, rowc + fi, r, vL, vR);
+    if (active_row) {
+#pragma unroll
+      for (int n = 0; n < NV; n++) sF[n][t] = r.F[n] * g.A[0];
+      sC[t] = r.cmax;
+    }
+  }
+  if (!active_row) return;
+  __syncthreads();
+  // phase 3: cells i0 .. min(i0+kTX, end0)-1
+  const int c = i0 + threadIdx.x;
+  if (c >= g.end[0]) return;
+  const int t = threadIdx.x;
+  const long long ci = rowc + c;
+  const double dtdV = ctl->dtdV;
+#pragma unroll
+  for (int n = 0; n < v::BX1; n++) {
+    const double rhs = -dtdV * (sF[n][t + 1] - sF[n][t]);
+    f.Uc[n * g.ncell + ci] = f.Uc[n * g.ncell + ci] + rhs;
+  }
+  if (invdt) {
+    const double prev = (invdt == 1) ? 0.0 : f.InvDt[ci];
+    const double inv = prev + 0.5 * (sC[t + 1] + sC[t]) / (g.dx[0]);
+    f.InvDt[ci] = inv;
+    if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// y / z sweeps: each thread owns one column (perpendicular position) and
+// marches a segment of `seg` cells along DIR, keeping the reconstruction
+// stencil, the left face state and the previous face flux in registers.
+// ---------------------------------------------------------------------------
+constexpr int kTM = 64;
+
+template <int D, int DIR, int ORDER, int SOLVER>
+__global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl* ctl, int invdt,
+                                                     int last_dir, int seg) {
+  if (ctl->done) return;
+  using v = Var<D>;
+  using dd = Dir<D, DIR>;
+  constexpr int NV = v::NV;
+  constexpr int H = Recon<ORDER>::H;
+  constexpr int W = 2 * H + 1;
+  const int i = g.beg[0] - g.ext + blockIdx.x * kTM + threadIdx.x;
+  if (i >= g.end[0] + g.ext) return;
+  // the other perpendicular coordinate
+  const int p = (D == 3) ? ((DIR == 1 ? g.beg[2] : g.beg[1]) - g.ext + (int)blockIdx.z) : 0;
+  const int m0 = g.beg[DIR] + blockIdx.y * seg;
+  const int m1 = min(m0 + seg, g.end[DIR]);
+  const int j0 = (DIR == 1) ? m0 : p;
+  const int k0 = (DIR == 1) ? p : m0;
+  bool active_col = (i >= g.beg[0] && i < g.end[0]);
+  if constexpr (D == 3) {
+    const int pd = (DIR == 1) ? 2 : 1;
+    active_col = active_col && p >= g.beg[pd] && p < g.end[pd];
+  }
+  const long long sd = g.s[DIR];
+  const long long fsd = g.fs[DIR];
+  // address of the first face (cell m0) of this column
+  const long long c0 = cidx(g, (D == 3) ? k0 : 0, (DIR == 1 || D == 3) ? j0 : p, i);
+  const long long f0 = fidx(g, (D == 3) ? k0 : 0, (DIR == 1 || D == 3) ? j0 : p, i);
+  const double* vs = f.Vs + DIR * g.nface;
+  double w[NV][W];
+  double vrp[NV];       // right-face state of the previous cell
+  double Fp[v::BX1];    // flux x A of the previous face
+  double cp = 0.0;      // cmax of the previous face
+  // prime the window with cells m0-1-H .. m0-2+H
+#pragma unroll
+  for (int n = 0; n < NV; n++) {
+    if (n == dd::BXn) continue;
+#pragma unroll
+    for (int m = 0; m < W - 1; m++) w[n][m + 1] = f.Vc[n * g.ncell + c0 + (m - 1 - H) * sd];
+  }
+  const double dtdV = ctl->dtdV;
+  for (int c = m0 - 1; c <= m1; c++) {
+    const long long cc = c0 + (long long)(c - m0) * sd;
+    double vl[NV], vr[NV];
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      if (n == dd::BXn) continue;
+#pragma unroll
+      for (int m = 0; m < W - 1; m++) w[n][m] = w[n][m + 1];
+      w[n][W - 1] = f.Vc[n * g.ncell + cc + H * sd];
+      Recon<ORDER>::cell(w[n], g.dx[DIR], n == v::RHO || n == v::PRS, vl[n], vr[n]);
+    }
+    if (c >= m0) {
+      double vL[NV], vR[NV];
+#pragma unroll
+      for (int n = 0; n < NV; n++) {
+        if (n == dd::BXn) continue;
+        vL[n] = vrp[n];
+        vR[n] = vl[n];
+      }
+      const double bn = vs[f0 + (long long)(c - m0) * fsd];
+      vL[dd::BXn] = bn;
+      vR[dd::BXn] = bn;
+      RiemannOut<D> r;
+      riemann<D, DIR, SOLVER>(g.gamma, vL, vR, r);
+      store_emf<D, DIR>(g, f, cc, r, vL, vR);
+      if (active_col) {
+        double FA[v::BX1];
+#pragma unroll
+        for (int n = 0; n < v::BX1; n++) FA[n] = r.F[n] * g.A[DIR];
+        if (c > m0) {
+          const long long cu = cc - sd;  // cell c-1
+#pragma unroll
+          for (int n = 0; n < v::BX1; n++) {
+            const double rhs = -dtdV * (FA[n] - Fp[n]);
+            f.Uc[n * g.ncell + cu] = f.Uc[n * g.ncell + cu] + rhs;
+          }
+          if (invdt) {
+            const double inv = f.InvDt[cu] + 0.5 * (r.cmax + cp) / (g.dx[DIR]);
+            f.InvDt[cu] = inv;
+            if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
+          }
+        }
+#pragma unroll
+        for (int n = 0; n < v::BX1; n++) Fp[n] = FA[n];
+        cp = r.cmax;
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < NV; n++) vrp[n] = vr[n];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Corner EMFs (ConstrainedTransport::CalcCornerEMF, calcCornerEmf.hpp;
+// uct_hll / uct_hlld: calcRiemannEmf.hpp).  One thread per edge position
+// (k,j,i) in [beg, end]^D; writes ez (and ex, ey in 3-D).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double riemann_edge(int order, const double* q, long long fq, long long fs,
+                                               const double* e, long long c, long long s,
+                                               const double* AL, const double* AR, const double* DL,
+                                               const double* DR, long long sp, double& phi) {
+  const double aL = 0.5 * (AL[c - sp] + AL[c]);
+  const double aR = 0.5 * (AR[c - sp] + AR[c]);
+  const double dL = 0.5 * (DL[c - sp] + DL[c]);
+  const double dR = 0.5 * (DR[c - sp] + DR[c]);
+  double bL, bR, vLv, vRv, db, dv;
+  const long long fm = fq - fs, m = c - s;
+  if (order == 4) {
+    ppm_states(q[fm - 2 * fs], q[fm - fs], q[fm], q[fm + fs], q[fm + 2 * fs], db, bL);
+    ppm_states(q[fq - 2 * fs], q[fq - fs], q[fq], q[fq + fs], q[fq + 2 * fs], bR, db);
+    ppm_states(e[m - 2 * s], e[m - s], e[m], e[m + s], e[m + 2 * s], dv, vLv);
+    ppm_states(e[c - 2 * s], e[c - s], e[c], e[c + s], e[c + 2 * s], vRv, dv);
+  } else {
+    db = lim_mc(q[fm + fs] - q[fm], q[fm] - q[fm - fs]);
+    bL = q[fm] + 0.5 * db;
+    db = lim_mc(q[fq + fs] - q[fq], q[fq] - q[fq - fs]);
+    bR = q[fq] - 0.5 * db;
+    dv = lim_mc(e[m + s] - e[m], e[m] - e[m - s]);
+    vLv = e[m] + 0.5 * dv;
+    dv = lim_mc(e[c + s] - e[c], e[c] - e[c - s]);
+    vRv = e[c] - 0.5 * dv;
+  }
+  phi = dR * bR - dL * bL;
+  return aL * vLv * bL + aR * vRv * bR;
+}
+
+template <int D>
+__global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
+  if (ctl->done) return;
+  const int nx = g.n[0] + 1, ny = g.n[1] + 1;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)nx * ny * (D == 3 ? g.n[2] + 1 : 1);
+  if (tid >= tot) return;
+  const int i = g.beg[0] + (int)(tid % nx);
+  const long long r = tid / nx;
+  const int j = g.beg[1] + (int)(r % ny);
+  const int k = (D == 3) ? g.beg[2] + (int)(r / ny) : 0;
+  const long long c = cidx(g, k, j, i);
+  const long long si = 1, sj = g.s[1], sk = g.s[2];
+  const double* ezi = f.ezi;
+  const double* ezj = f.ezj;
+  if (g.emf == kEmfUctHll || g.emf == kEmfUctHlld) {
+    const long long fc = fidx(g, k, j, i);
+    const double* Vs1 = f.Vs;
+    const double* Vs2 = f.Vs + g.nface;
+    double phi, X, ezv;
+    X = riemann_edge(g.order, Vs2, fc, 1, ezj, c, si, f.aL[0], f.aR[0], f.dL[0], f.dR[0], sj, phi);
+    ezv = X + phi;
+    if constexpr (D == 3) {
+      const double* Vs3 = f.Vs + 2 * g.nface;
+      double eyv, exv;
+      X = riemann_edge(g.order, Vs3, fc, 1, f.eyk, c, si, f.aL[0], f.aR[0], f.dL[0], f.dR[0], sk, phi);
+      eyv = X - phi;
+      X = riemann_edge(g.order, Vs3, fc, g.fs[1], f.exk, c, sj, f.aL[1], f.aR[1], f.dL[1], f.dR[1], sk, phi);
+      exv = X + phi;
+      X = riemann_edge(g.order, Vs1, fc, g.fs[1], ezi, c, sj, f.aL[1], f.aR[1], f.dL[1], f.dR[1], si, phi);
+      ezv += X - phi;
+      X = riemann_edge(g.order, Vs1, fc, g.fs[2], f.eyi, c, sk, f.aL[2], f.aR[2], f.dL[2], f.dR[2], si, phi);
+      eyv += X + phi;
+      X = riemann_edge(g.order, Vs2, fc, g.fs[2], f.exj, c, sk, f.aL[2], f.aR[2], f.dL[2], f.dR[2], sj, phi);
+      exv += X - phi;
+      f.ex[c] = exv;
+      f.ey[c] = eyv;
+    } else {
+      X = riemann_edge(g.order, Vs1, fc, g.fs[1], ezi, c, sj, f.aL[1], f.aR[1], f.dL[1], f.dR[1], si, phi);
+      ezv += X - phi;
+    }
+    f.ez[c] = ezv;
+    return;
+  }
+  if (g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
+    const double w = 0.25;
+    if (g.emf == kEmfArithmetic) {
+      if constexpr (D == 3) {
+        f.ex[c] = w * (f.exj[c] + f.exj[c - sk] + f.exk[c] + f.exk[c - sj]);
+        f.ey[c] = w * (f.eyi[c] + f.eyi[c - sk] + f.eyk[c] + f.eyk[c - si]);
+      }
+      f.ez[c] = w * (ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
+    } else {
+      // CalcUCT0Average: face EMFs become 2 e - (cell EMF average), computed
+      // here for the four faces around the edge (calcCornerEmf.hpp:150-190)
+      auto mz_i = [&](long long q) { double a = ezi[q] * 2.0; return a - 0.5 * (f.Ex3[q - si] + f.Ex3[q]); };
+      auto mz_j = [&](long long q) { double a = ezj[q] * 2.0; return a - 0.5 * (f.Ex3[q - sj] + f.Ex3[q]); };
+      if constexpr (D == 3) {
+        auto mx_j = [&](long long q) { double a = f.exj[q] * 2.0; return a - 0.5 * (f.Ex1[q - sj] + f.Ex1[q]); };
+        auto mx_k = [&](long long q) { double a = f.exk[q] * 2.0; return a - 0.5 * (f.Ex1[q - sk] + f.Ex1[q]); };
+        auto my_i = [&](long long q) { double a = f.eyi[q] * 2.0; return a - 0.5 * (f.Ex2[q - si] + f.Ex2[q]); };
+        auto my_k = [&](long long q) { double a = f.eyk[q] * 2.0; return a - 0.5 * (f.Ex2[q - sk] + f.Ex2[q]); };
+        f.ex[c] = w * (mx_j(c) + mx_j(c - sk) + mx_k(c) + mx_k(c - sj));
+        f.ey[c] = w * (my_i(c) + my_i(c - sk) + my_k(c) + my_k(c - si));
+      }
+      f.ez[c] = w * (mz_i(c) + mz_i(c - sj) + mz_j(c) + mz_j(c - si));
+    }
+    return;
+  }
+  // uct_contact (calcCornerEmf.hpp:224-282)
+  const double* wsx = f.svx;
+  const double* wsy = f.svy;
+  const double* Ex3 = f.Ex3;
+  const double ez_l2 = (1 - wsx[c - sj]) * (ezj[c] - Ex3[c - sj]) + (wsx[c - sj]) * (ezj[c - si] - Ex3[c - sj - si]);
+  const double ez_r2 = (1 - wsx[c]) * (ezj[c] - Ex3[c]) + (wsx[c]) * (ezj[c - si] - Ex3[c - si]);
+  const double ez_l1 = (1 - wsy[c - si]) * (ezi[c] - Ex3[c - si]) + (wsy[c - si]) * (ezi[c - sj] - Ex3[c - sj - si]);
+  const double ez_r1 = (1 - wsy[c]) * (ezi[c] - Ex3[c]) + (wsy[c]) * (ezi[c - sj] - Ex3[c - sj]);
+  f.ez[c] = 0.25 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
+  if constexpr (D == 3) {
+    const double* wsz = f.svz;
+    const double* Ex1 = f.Ex1;
+    const double* Ex2 = f.Ex2;
+    const double *exj = f.exj, *exk = f.exk, *eyi = f.eyi, *eyk = f.eyk;
+    const double ex_l3 = (1 - wsy[c - sk]) * (exk[c] - Ex1[c - sk]) + (wsy[c - sk]) * (exk[c - sj] - Ex1[c - sk - sj]);
+    const double ex_r3 = (1 - wsy[c]) * (exk[c] - Ex1[c]) + (wsy[c]) * (exk[c - sj] - Ex1[c - sj]);
+    const double ex_l2 = (1 - wsz[c - sj]) * (exj[c] - Ex1[c - sj]) + (wsz[c - sj]) * (exj[c - sk] - Ex1[c - sk - sj]);
+    const double ex_r2 = (1 - wsz[c]) * (exj[c] - Ex1[c]) + (wsz[c]) * (exj[c - sk] - Ex1[c - sk]);
+    f.ex[c] = 0.25 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
+    const double ey_l3 = (1 - wsx[c - sk]) * (eyk[c] - Ex2[c - sk]) + (wsx[c - sk]) * (eyk[c - si] - Ex2[c - sk - si]);
+    const double ey_r3 = (1 - wsx[c]) * (eyk[c] - Ex2[c]) + (wsx[c]) * (eyk[c - si] - Ex2[c - si]);
+    const double ey_l1 = (1 - wsz[c - si]) * (eyi[c] - Ex2[c - si]) + (wsz[c - si]) * (eyi[c - sk] - Ex2[c - sk - si]);
+    const double ey_r1 = (1 - wsz[c]) * (eyi[c] - Ex2[c]) + (wsz[c]) * (eyi[c - sk] - Ex2[c - sk]);
+    f.ey[c] = 0.25 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Face-field update Vs += dt curl E (evolveMagField.hpp:53-132, Cartesian),
+// then the Runge-Kutta combination of the faces (AddAndStore).  Only faces
+// that the next boundary pass does not overwrite are touched.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
+  if (ctl->done) return;
+  const int nx = g.n[0] + 1, ny = g.n[1] + 1;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)nx * ny * (D == 3 ? g.n[2] + 1 : 1);
+  if (tid >= tot) return;
+  const int i = g.beg[0] + (int)(tid % nx);
+  const long long r = tid / nx;
+  const int j = g.beg[1] + (int)(r % ny);
+  const int k = (D == 3) ? g.beg[2] + (int)(r / ny) : 0;
+  const long long c = cidx(g, k, j, i);
+  const long long fc = fidx(g, k, j, i);
+  const long long si = 1, sj = g.s[1], sk = g.s[2];
+  const double* Ex1 = f.ex;
+  const double* Ex2 = f.ey;
+  const double* Ex3 = f.ez;
+  const double dtdx1 = ctl->dtdx[0], dtdx2 = ctl->dtdx[1], dtdx3 = ctl->dtdx[2];
+  const bool in_i = i < g.end[0], in_j = j < g.end[1], in_k = (D == 2) || k < g.end[2];
+  // BX1s: faces i in [beg, end], j, k active
+  if (in_j && in_k) {
+    double rhs;
+    if constexpr (D == 2) {
+      rhs = 0.0 - dtdx2 * (Ex3[c + sj] - Ex3[c]);
+    } else {
+      rhs = 0.0 - dtdx2 * (Ex3[c + sj] - Ex3[c]) + dtdx3 * (Ex2[c + sk] - Ex2[c]);
+    }
+    double* vs = f.Vs;
+    double b = vs[fc] + rhs;
+    if (combine) b = wc * b + w0 * f.Vs0[fc];
+    vs[fc] = b;
+  }
+  if (in_i && in_k) {
+    double rhs;
+    if constexpr (D == 2) {
+      rhs = dtdx1 * (Ex3[c + si] - Ex3[c]);
+    } else {
+      rhs = dtdx1 * (Ex3[c + si] - Ex3[c]) - dtdx3 * (Ex1[c + sk] - Ex1[c]);
+    }
+    double* vs = f.Vs + g.nface;
+    double b = vs[fc] + rhs;
+    if (combine) b = wc * b + w0 * f.Vs0[g.nface + fc];
+    vs[fc] = b;
+  }
+  if constexpr (D == 3) {
+    if (in_i && in_j) {
+      const double rhs = -dtdx1 * (Ex2[c + si] - Ex2[c]) + dtdx2 * (Ex1[c + sj] - Ex1[c]);
+      double* vs = f.Vs + 2 * g.nface;
+      double b = vs[fc] + rhs;
+      if (combine) b = wc * b + w0 * f.Vs0[2 * g.nface + fc];
+      vs[fc] = b;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Stage end over the active cells: RK combination of Uc (AddAndStore),
+// cell-centred field from the faces (ReconstructVcField on Uc), and
+// ConvertConsToPrim.  Writes Uc and Vc.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_stage_end(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
+  if (ctl->done) return;
+  using v = Var<D>;
+  constexpr int NV = v::NV;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)g.n[0] * g.n[1] * (D == 3 ? g.n[2] : 1);
+  if (tid >= tot) return;
+  const int i = g.beg[0] + (int)(tid % g.n[0]);
+  const long long r = tid / g.n[0];
+  const int j = g.beg[1] + (int)(r % g.n[1]);
+  const int k = (D == 3) ? g.beg[2] + (int)(r / g.n[1]) : 0;
+  const long long c = cidx(g, k, j, i);
+  const long long fc = fidx(g, k, j, i);
+  double U[NV], V[NV];
+#pragma unroll
+  for (int n = 0; n < v::BX1; n++) {
+    double u = f.Uc[n * g.ncell + c];
+    if (combine) u = wc * u + w0 * f.Uc0[n * g.ncell + c];
+    U[n] = u;
+  }
+#pragma unroll
+  for (int d = 0; d < D; d++) {
+    const double* vs = f.Vs + d * g.nface;
+    U[v::BX1 + d] = 0.5 * (vs[fc] + vs[fc + g.fs[d]]);
+  }
+  cons_to_prim<D>(g.gm1, V, U);
+#pragma unroll
+  for (int n = 0; n < NV; n++) {
+    f.Uc[n * g.ncell + c] = U[n];
+    f.Vc[n * g.ncell + c] = V[n];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics: divB estimator (checkDivB.hpp:14-68) and NaN count
+// (checkNan.hpp:17-45), as device reductions.
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void k_divb(Geo g, Fields f, Ctl* ctl) {
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)g.n[0] * g.n[1] * (D == 3 ? g.n[2] : 1);
+  if (tid >= tot) return;
+  const int i = g.beg[0] + (int)(tid % g.n[0]);
+  const long long r = tid / g.n[0];
+  const int j = g.beg[1] + (int)(r % g.n[1]);
+  const int k = (D == 3) ? g.beg[2] + (int)(r / g.n[1]) : 0;
+  const long long fc = fidx(g, k, j, i);
+  const double* B1s = f.Vs;
+  const double* B2s = f.Vs + g.nface;
+  const double A1 = g.A[0], A2 = g.A[1], A3 = g.A[2];
+  const double dB1 = (A1 * B1s[fc + 1] - A1 * B1s[fc]);
+  const double dB2 = (A2 * B2s[fc + g.fs[1]] - A2 * B2s[fc]);
+  const double d1 = 0.5 * (A1 + A1), d2 = 0.5 * (A2 + A2);
+  const double b1 = 0.5 * (B1s[fc + 1] + B1s[fc]);
+  const double b2 = 0.5 * (B2s[fc + g.fs[1]] + B2s[fc]);
+  double amplitude = 1e-40;
+  double val;
+  if constexpr (D == 2) {
+    amplitude += fabs(b1) * d1 + fabs(b2) * d2;
+    val = fabs(dB1 + dB2) / amplitude;
+  } else {
+    const double* B3s = f.Vs + 2 * g.nface;
+    const double dB3 = (A3 * B3s[fc + g.fs[2]] - A3 * B3s[fc]);
+    const double d3 = 0.5 * (A3 + A3);
+    const double b3 = 0.5 * (B3s[fc + g.fs[2]] + B3s[fc]);
+    amplitude += fabs(b1) * d1 + fabs(b2) * d2 + fabs(b3) * d3;
+    val = fabs(dB1 + dB2 + dB3) / amplitude;
+  }
+  atomic_max_pos(&ctl->divb_bits, val);
+}
+
+template <int D>
+__global__ void k_nan_count(Geo g, Fields f, Ctl* ctl) {
+  using v = Var<D>;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nx = g.n[0] + 1, ny = g.n[1] + 1;
+  const long long tot = (long long)nx * ny * (D == 3 ? g.n[2] + 1 : 1);
+  if (tid >= tot) return;
+  const int i = g.beg[0] + (int)(tid % nx);
+  const long long r = tid / nx;
+  const int j = g.beg[1] + (int)(r % ny);
+  const int k = (D == 3) ? g.beg[2] + (int)(r / ny) : 0;
+  unsigned long long n = 0;
+  const bool cell = i < g.end[0] && j < g.end[1] && (D == 2 || k < g.end[2]);
+  if (cell) {
+    const long long c = cidx(g, k, j, i);
+    for (int q = 0; q < v::NV; q++) n += isnan(f.Vc[q * g.ncell + c]) ? 1 : 0;
+  }
+  const long long fc = fidx(g, k, j, i);
+  for (int q = 0; q < D; q++) n += isnan(f.Vs[q * g.nface + fc]) ? 1 : 0;
+  if (n) atomicAdd(&ctl->nan_count, n);
+}
+
+// ---------------------------------------------------------------------------
+// Time-integrator control (timeIntegrator.cpp:246-414, main.cpp:190-225),
+// single thread.
+// ---------------------------------------------------------------------------
+static __global__ void k_cycle_begin(Geo g, Ctl* ctl, int use_tstop) {
+  if (ctl->done) return;
+  if (use_tstop) {
+    if (!(ctl->t < ctl->tstop)) {
+      ctl->done = 1;
+      return;
+    }
+    if (ctl->tstop - ctl->t < ctl->dt) ctl->dt = ctl->tstop - ctl->t;
+  }
+  const double dt = ctl->dt;
+  double dV = g.dx[0] * g.dx[1];
+  if (g.D == 3) dV = dV * g.dx[2];
+  ctl->dtdV = dt / dV;
+  for (int d = 0; d < 3; d++) ctl->dtdx[d] = dt / g.dx[d];
+  ctl->t0 = ctl->t;
+  ctl->invdt_max_bits = 0ull;
+}
+
+static __global__ void k_cycle_end(Ctl* ctl) {
+  if (ctl->done) return;
+  const double invmax = __longlong_as_double((long long)ctl->invdt_max_bits);
+  const double dtmin = 1.0 / invmax;  // = min over cells of 1/InvDt (division is monotone)
+  const double newdt = ctl->cfl * dtmin;
+  ctl->t = ctl->t0 + ctl->dt;
+  if (newdt > ctl->cflmax * ctl->dt) {
+    ctl->dt = ctl->cflmax * ctl->dt;
+  } else {
+    if (ctl->ncycles == 0 && newdt < 0.5 * ctl->dt) {
+      ctl->status = kErrFirstDt;
+      ctl->done = 1;
+      return;
+    }
+    ctl->dt = newdt;
+  }
+  if (ctl->dt < 1e-15) {
+    ctl->status = kErrDtSmall;
+    ctl->done = 1;
+    return;
+  }
+  ctl->ncycles++;
+}
+
+static __global__ void k_check_divb(Ctl* ctl) {
+  if (ctl->done) return;
+  const double v = __longlong_as_double((long long)ctl->divb_bits);
+  if (v > ctl->maxdivb) {
+    ctl->status = kErrDivB;
+    ctl->done = 1;
+  }
+}
+
+static __global__ void k_check_nan(Ctl* ctl) {
+  if (ctl->done) return;
+  if (ctl->nan_count > 0) {
+    ctl->status = kErrNan;
+    ctl->done = 1;
+  }
+}
+
+}  // namespace idfx

@@ -1,0 +1,144 @@
+/*
+ * idefix_gb300 — C ABI of the GB300 (sm_103a) ideal-MHD Godunov stage.
+ *
+ * Drop-in for the hot path of Idefix v2.2.02: one periodic Cartesian block
+ * (COMPONENTS == DIMENSIONS in {2, 3}), advanced by the reference's
+ * TimeIntegrator::Cycle semantics with PLM / LimO3 / PPM reconstruction,
+ * HLLD / HLL / Roe / TVDLF fluxes and constrained transport.  In FP64 mode
+ * the results are bit-identical to the reference built without FMA
+ * contraction (its GPU CI setting).
+ *
+ * Conventions
+ *  - Host arrays use the reference layout (LayoutRight, ghosts included):
+ *      Vc[nvar][nt2][nt1][nt0]        nt = n + 2*nghost (1 in unused dims)
+ *      Vs[dims][nt2+ko][nt1+jo][nt0+io]  (+1 in every active dimension)
+ *    variable order RHO, VX1..VXd, PRS, BX1..BXd   (src/idefix.hpp:74-108)
+ *  - Every function returns an idfx_status; idfx_gpu_last_error() returns
+ *    the message of the last failure.  Nothing traps on the device.
+ *  - A handle is used by one host thread at a time; work is ordered on the
+ *    handle's CUDA stream.  No device pointer crosses the ABI except in the
+ *    *_device entry points, which take pointers into this process's GPU
+ *    memory.
+ */
+#ifndef IDEFIX_GB300_H_
+#define IDEFIX_GB300_H_
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  IDFX_OK = 0,
+  IDFX_ERR_CONFIG = 1,      /* IDEFIX_ERROR on an invalid setup            */
+  IDFX_ERR_NAN = 2,         /* "Nan found after integration cycle"         */
+  IDFX_ERR_DIVB = 3,        /* "divB too large, check your calculation"    */
+  IDFX_ERR_DT_SMALL = 4,    /* "dt = ... is too small."                    */
+  IDFX_ERR_FIRST_DT = 5,    /* "Your guessed first_dt is too large."       */
+  IDFX_ERR_CUDA = 6,        /* CUDA runtime failure                         */
+  IDFX_ERR_STATE = 7        /* call out of order / null handle             */
+} idfx_status;
+
+/* reconstruction order: Idefix_RECONSTRUCTION (CMakeLists.txt:198-209) */
+enum { IDFX_ORDER1 = 1, IDFX_PLM = 2, IDFX_LIMO3 = 3, IDFX_PPM = 4 };
+/* [Hydro] solver (riemannSolver.hpp:27) */
+enum { IDFX_HLLD = 0, IDFX_HLL = 1, IDFX_ROE = 2, IDFX_TVDLF = 3 };
+/* [Hydro] emf (constrainedTransport.hpp:155-179) */
+enum {
+  IDFX_EMF_UCT_CONTACT = 0,
+  IDFX_EMF_ARITHMETIC = 1,
+  IDFX_EMF_UCT0 = 2,
+  IDFX_EMF_UCT_HLL = 3,
+  IDFX_EMF_UCT_HLLD = 4
+};
+/* arithmetic of the reconstruction and Riemann solve */
+enum { IDFX_FP64 = 0 };
+
+typedef struct {
+  int dims;                 /* 2 or 3 (DIMENSIONS, with COMPONENTS == DIMENSIONS) */
+  int n[3];                 /* active cells per direction, n[2] = 1 in 2-D        */
+  double xbeg[3], xend[3];  /* [Grid] X?-grid uniform patch bounds                */
+  int order;                /* IDFX_ORDER1 .. IDFX_PPM                            */
+  int solver;               /* IDFX_HLLD ..                                       */
+  int emf;                  /* IDFX_EMF_* (default uct_contact)                   */
+  int nstages;              /* [TimeIntegrator] nstages: 1, 2 or 3                */
+  double gamma;             /* [Hydro] gamma (default 5/3)                        */
+  double cfl;               /* [TimeIntegrator] CFL                               */
+  double cfl_max_var;       /* [TimeIntegrator] CFL_max_var (default 1.1)         */
+  double first_dt;          /* [TimeIntegrator] first_dt                          */
+  double maxdivb;           /* [TimeIntegrator] maxdivB (default 1e-6)            */
+  int log_period;           /* [Output] log: divB check period, 0 = off           */
+  int check_nan_period;     /* [TimeIntegrator] check_nan, 0 = off                */
+  int precision;            /* IDFX_FP64                                          */
+} idfx_gpu_config;
+
+typedef struct idfx_gpu idfx_gpu;
+
+/* Fills a config with the reference's defaults for the given grid. */
+void idfx_gpu_default_config(idfx_gpu_config* cfg, int dims, int nx, int ny, int nz);
+
+/* Replaces: Fluid<Phys>::Fluid + RiemannSolver + ConstrainedTransport +
+ * TimeIntegrator construction (fluid.hpp:263-755, timeIntegrator.cpp:22-86).
+ * stream: a cudaStream_t, or NULL for a stream owned by the handle. */
+int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out);
+int idfx_gpu_destroy(idfx_gpu* h);
+int idfx_gpu_last_error(const idfx_gpu* h, char* buf, size_t len);
+
+/* sizes of the host arrays (in doubles) */
+int idfx_gpu_sizes(const idfx_gpu* h, int* nvar, int* nghost, long long* vc_len, long long* vs_len);
+
+/* Replaces: DataBlockHost::SyncToDevice / SyncFromDevice of Vc, Vs, Uc
+ * (dataBlockHost.hpp:94-95).  Host pointers, reference layout. */
+int idfx_gpu_upload_prim(idfx_gpu* h, const double* Vc, const double* Vs);
+int idfx_gpu_download_prim(idfx_gpu* h, double* Vc, double* Vs);
+int idfx_gpu_download_cons(idfx_gpu* h, double* Uc);
+/* same, with device pointers of this process */
+int idfx_gpu_upload_prim_device(idfx_gpu* h, const double* Vc, const double* Vs);
+int idfx_gpu_download_prim_device(idfx_gpu* h, double* Vc, double* Vs);
+
+/* DataBlock::t, DataBlock::dt, TimeIntegrator::ncycles */
+int idfx_gpu_set_time(idfx_gpu* h, double t, double dt, long long ncycles);
+int idfx_gpu_get_time(idfx_gpu* h, double* t, double* dt, long long* ncycles);
+
+/* Replaces: TimeIntegrator::Cycle (timeIntegrator.cpp:246-414). Synchronous. */
+int idfx_gpu_cycle(idfx_gpu* h);
+/* Replaces: the main loop of main.cpp:190-225: cycles while t < tstop
+ * (tstop < 0: no time limit) and at most max_cycles cycles (< 0: no limit).
+ * Cycles are queued without host synchronisation between them. */
+int idfx_gpu_run(idfx_gpu* h, double tstop, long long max_cycles);
+
+/* Building blocks (each synchronous), same meaning as the reference methods */
+int idfx_gpu_set_boundaries(idfx_gpu* h);                   /* Boundary::SetBoundaries     */
+int idfx_gpu_prim_to_cons(idfx_gpu* h);                     /* Fluid::ConvertPrimToCons    */
+int idfx_gpu_cons_to_prim(idfx_gpu* h);                     /* Fluid::ConvertConsToPrim    */
+int idfx_gpu_reset_stage(idfx_gpu* h);                     /* Fluid::ResetStage (InvDt=0) */
+int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt);/* Fluid::EvolveStage          */
+int idfx_gpu_compute_timestep(idfx_gpu* h, double* dt);     /* DataBlock::ComputeTimestep  */
+int idfx_gpu_check_divb(idfx_gpu* h, double* divb);         /* Fluid::CheckDivB            */
+int idfx_gpu_check_nan(idfx_gpu* h, long long* count);      /* Fluid::CheckNan             */
+
+/* Per-kernel timing (no counterpart in the reference, which times regions
+ * through Kokkos-Tools, profiler.cpp:55-130): when enabled, every launch of
+ * the kernel classes below is bracketed by CUDA events on the handle's
+ * stream.  Enabling clears the record; read returns total ms and launch
+ * counts per class. */
+enum {
+  IDFX_K_FILL_FACES = 0,
+  IDFX_K_STAGE_BEGIN,
+  IDFX_K_SWEEP_X,
+  IDFX_K_SWEEP_Y,
+  IDFX_K_SWEEP_Z,
+  IDFX_K_CT_CORNER,
+  IDFX_K_CT_FACES,
+  IDFX_K_STAGE_END,
+  IDFX_K_CONTROL,
+  IDFX_K_CHECKS,
+  IDFX_K_NUM
+};
+int idfx_gpu_profile(idfx_gpu* h, int enable);
+int idfx_gpu_profile_read(idfx_gpu* h, double* ms, long long* launches, int nclasses);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IDEFIX_GB300_H_ */
