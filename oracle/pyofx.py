@@ -76,7 +76,8 @@ class Oracle:
 
     def __init__(self, dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm",
                  solver="hlld", emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.6,
-                 cfl_max_var=1.1, first_dt=1e-4, kind="port", threads=1):
+                 cfl_max_var=1.1, first_dt=1e-4, kind="port", threads=1, log_period=0,
+                 check_nan_period=0, maxdivb=1e-6):
         self.lib = load(kind)
         n = list(n) + [1] * (3 - len(n))
         self.dims, self.n = dims, n
@@ -92,6 +93,7 @@ class Oracle:
         self.nt = [n[d] + 2 * g if d < dims else 1 for d in range(3)]
         self.ntv = [self.nt[d] + (1 if d < dims else 0) for d in range(3)]
         self.lib.ofx_set_threads(self.h, threads)
+        self.lib.ofx_set_checks(self.h, log_period, check_nan_period, maxdivb)
 
     def __del__(self):
         if getattr(self, "h", None):
