@@ -68,6 +68,7 @@ EXPORTS = [
     "idfx_gpu_prim_to_cons", "idfx_gpu_cons_to_prim", "idfx_gpu_reset_stage",
     "idfx_gpu_evolve_stage", "idfx_gpu_compute_timestep", "idfx_gpu_check_divb",
     "idfx_gpu_check_nan", "idfx_gpu_profile", "idfx_gpu_profile_read",
+    "idfx_evolve_stage_noalloc",
 ]
 
 KERNEL_CLASSES = ["fill_faces", "stage_begin", "sweep_x", "sweep_y", "sweep_z", "ct_corner",
@@ -110,6 +111,8 @@ def load_library(path=LIB_PATH):
     lib.idfx_gpu_check_nan.argtypes = [P, ctypes.POINTER(LL)]
     lib.idfx_gpu_profile.argtypes = [P, I]
     lib.idfx_gpu_profile_read.argtypes = [P, dp, ctypes.POINTER(LL), I]
+    lib.idfx_evolve_stage_noalloc.argtypes = [ctypes.POINTER(Config), P, P, P, D, D, P,
+                                              ctypes.c_char_p, ctypes.c_size_t]
     for f in EXPORTS:
         if f != "idfx_gpu_default_config":
             getattr(lib, f).restype = I

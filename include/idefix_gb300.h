@@ -138,6 +138,23 @@ enum {
 int idfx_gpu_profile(idfx_gpu* h, int enable);
 int idfx_gpu_profile_read(idfx_gpu* h, double* ms, long long* launches, int nclasses);
 
+/* Allocation-free Fluid::EvolveStage — no counterpart in the reference.
+ * For callers that may not allocate GPU memory while they step (state held
+ * in their own pools or arenas, regions where cudaMalloc is forbidden):
+ * Vc (in), Uc and Vs (in/out) are device arrays of this process in the
+ * reference layout, as after Boundary::SetBoundaries and ConvertPrimToCons;
+ * the stage's other work arrays live in a static device array of
+ * IDFX_NOALLOC_SCRATCH_DOUBLES doubles (32 MiB, held by every GPU that
+ * loads the library until exit).  Blocks that do not fit are refused with
+ * IDFX_ERR_CONFIG and a message in err.  Asynchronous on `stream` (NULL =
+ * legacy default stream).  All calls share the scratch: calls whose GPU
+ * work overlaps race.  The first call on a device looks up the scratch
+ * address; make it before any stream capture.  Results equal
+ * idfx_gpu_reset_stage + idfx_gpu_evolve_stage on the same arrays. */
+#define IDFX_NOALLOC_SCRATCH_DOUBLES (4u * 1024u * 1024u)
+int idfx_evolve_stage_noalloc(const idfx_gpu_config* cfg, const double* Vc, double* Uc, double* Vs,
+                              double t, double dt, void* stream, char* err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,14 +26,14 @@ def _declared():
     names = set()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
         txt = open(h).read()
-        names |= set(re.findall(r"\b(idfx_gpu_\w+)\s*\(", txt))
+        names |= set(re.findall(r"\b(idfx_\w+)\s*\(", txt))
     return sorted(names)
 
 
 def test_every_declared_symbol_is_exported(lib):
     so = os.path.join(ROOT, "idefix_gb300", "libidefix_gb300.so")
     out = subprocess.run(["nm", "-D", "--defined-only", so], capture_output=True, text=True).stdout
-    exported = set(re.findall(r" T (idfx_gpu_\w+)", out))
+    exported = set(re.findall(r" T (idfx_\w+)", out))
     declared = _declared()
     assert len(declared) >= 20
     missing = [d for d in declared if d not in exported]
