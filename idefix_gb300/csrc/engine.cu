@@ -257,8 +257,10 @@ int choose_segments(Engine& e) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long want = (long long)sms * 512;
-  for (int d = 1; d < e.g.D; d++) {
-    const long long cols = (long long)(e.g.n[0] + 2 * e.g.ext) * (e.g.D == 3 ? e.g.n[3 - d] + 2 * e.g.ext : 1);
+  for (int d = 0; d < e.g.D; d++) {
+    // marching columns: the two other directions (with the CT extension)
+    const int a = (d == 0) ? 1 : 0, b = (d == 2) ? 1 : 2;
+    const long long cols = (long long)(e.g.n[a] + 2 * e.g.ext) * (e.g.D == 3 ? e.g.n[b] + 2 * e.g.ext : 1);
     int s = 64;
     while (s > 2 && cols * ((e.g.n[d] + s - 1) / s) < want) s /= 2;
     e.seg[d] = s;

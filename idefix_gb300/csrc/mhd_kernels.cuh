@@ -9,7 +9,7 @@
 // Stage = fill_faces -> stage_begin -> sweep x, y(, z) -> ct_corner ->
 // ct_faces -> stage_end.  Each face's Riemann problem is solved once and
 // each cell's reconstruction is evaluated once per direction; fluxes never
-// leave the chip (shared memory for x, registers for y/z).
+// leave the registers of the thread that marches the column.
 #pragma once
 #include <cstdint>
 
@@ -283,98 +283,17 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
 }
 
 // ---------------------------------------------------------------------------
-// x sweep: one block = TX faces of one (j,k) row.  Phase 1 reconstructs the
-// TX+2 cells once into shared memory, phase 2 solves TX+1 Riemann problems,
-// phase 3 applies the flux difference (Fluid_CorrectFluxFunctor +
-// Fluid_CalcRHSFunctor, calcRightHandSide.hpp:84-195,333-550).
-// ---------------------------------------------------------------------------
-constexpr int kTX = 64;
-
+// Flux sweeps (RiemannSolver::CalcFlux<DIR> + Fluid_CorrectFluxFunctor +
+// Fluid_CalcRHSFunctor, calcRightHandSide.hpp:84-195,333-550): each thread
+// owns one column (a line of cells along DIR) and marches a segment of `seg`
+// cells, keeping the reconstruction stencil, the left face state and the
+// previous face flux in registers.  Every cell is reconstructed once and
+// every face solved once (plus one face and two cells per segment).
+// Thread index -> coordinate A (j for the x sweep, i otherwise); blockIdx.z
+// -> coordinate B (k, or j for the z sweep); both include the CT extension.
 // invdt: 0 = no InvDt work, 1 = first contribution of a cycle (InvDt was
 // reset to 0), 2 = accumulate onto the stored InvDt.  last_dir: fold the
 // completed InvDt into the device maximum used for the next dt.
-template <int D, int ORDER, int SOLVER>
-__global__ void __launch_bounds__(kTX) k_sweep_x(Geo g, Fields f, const Ctl* ctl, int invdt,
-                                                 int last_dir) {
-  if (ctl->done) return;
-  using v = Var<D>;
-  using dd = Dir<D, 0>;
-  constexpr int NV = v::NV;
-  constexpr int H = Recon<ORDER>::H;
-  __shared__ double sL[NV][kTX + 2], sR[NV][kTX + 2];
-  __shared__ double sF[NV][kTX + 1];
-  __shared__ double sC[kTX + 1];
-  const int i0 = g.beg[0] + blockIdx.x * kTX;
-  const int j = g.beg[1] - g.ext + blockIdx.y;
-  const int k = (D == 3) ? g.beg[2] - g.ext + (int)blockIdx.z : 0;
-  const bool active_row = (j >= g.beg[1] && j < g.end[1]) && (D == 2 || (k >= g.beg[2] && k < g.end[2]));
-  const long long rowc = cidx(g, k, j, 0);
-  // phase 1: cells i0-1 .. min(i0+kTX, end0)
-  for (int t = threadIdx.x; t < kTX + 2; t += kTX) {
-    const int c = i0 - 1 + t;
-    if (c > g.end[0]) continue;
-#pragma unroll
-    for (int n = 0; n < NV; n++) {
-      if (n == dd::BXn) continue;
-      const double* q = f.Vc + n * g.ncell + rowc + c;
-      double w[2 * H + 1];
-#pragma unroll
-      for (int m = 0; m <= 2 * H; m++) w[m] = q[m - H];
-      double vl, vr;
-      Recon<ORDER>::cell(w, g.dx[0], n == v::RHO || n == v::PRS, vl, vr);
-      sL[n][t] = vl;
-      sR[n][t] = vr;
-    }
-  }
-  __syncthreads();
-  // phase 2: faces i0 .. min(i0+kTX, end0)
-  for (int t = threadIdx.x; t < kTX + 1; t += kTX) {
-    const int fi = i0 + t;
-    if (fi > g.end[0]) continue;
-    double vL[NV], vR[NV];
-#pragma unroll
-    for (int n = 0; n < NV; n++) {
-      if (n == dd::BXn) continue;
-      vL[n] = sR[n][t];
-      vR[n] = sL[n][t + 1];
-    }
-    const double bn = f.Vs[fidx(g, k, j, fi)];
-    vL[dd::BXn] = bn;
-    vR[dd::BXn] = bn;
-    RiemannOut<D> r;
-    riemann<D, 0, SOLVER>(g.gamma, vL, vR, r);
-    store_emf<D, 0>(g, f, rowc + fi, r, vL, vR);
-    if (active_row) {
-#pragma unroll
-      for (int n = 0; n < NV; n++) sF[n][t] = r.F[n] * g.A[0];
-      sC[t] = r.cmax;
-    }
-  }
-  if (!active_row) return;
-  __syncthreads();
-  // phase 3: cells i0 .. min(i0+kTX, end0)-1
-  const int c = i0 + threadIdx.x;
-  if (c >= g.end[0]) return;
-  const int t = threadIdx.x;
-  const long long ci = rowc + c;
-  const double dtdV = ctl->dtdV;
-#pragma unroll
-  for (int n = 0; n < v::BX1; n++) {
-    const double rhs = -dtdV * (sF[n][t + 1] - sF[n][t]);
-    f.Uc[n * g.ncell + ci] = f.Uc[n * g.ncell + ci] + rhs;
-  }
-  if (invdt) {
-    const double prev = (invdt == 1) ? 0.0 : f.InvDt[ci];
-    const double inv = prev + 0.5 * (sC[t + 1] + sC[t]) / (g.dx[0]);
-    f.InvDt[ci] = inv;
-    if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// y / z sweeps: each thread owns one column (perpendicular position) and
-// marches a segment of `seg` cells along DIR, keeping the reconstruction
-// stencil, the left face state and the previous face flux in registers.
 // ---------------------------------------------------------------------------
 constexpr int kTM = 64;
 
@@ -387,24 +306,23 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
   constexpr int NV = v::NV;
   constexpr int H = Recon<ORDER>::H;
   constexpr int W = 2 * H + 1;
-  const int i = g.beg[0] - g.ext + blockIdx.x * kTM + threadIdx.x;
-  if (i >= g.end[0] + g.ext) return;
-  // the other perpendicular coordinate
-  const int p = (D == 3) ? ((DIR == 1 ? g.beg[2] : g.beg[1]) - g.ext + (int)blockIdx.z) : 0;
+  constexpr int A = (DIR == 0) ? 1 : 0;
+  constexpr int B = (DIR == 2) ? 1 : 2;
+  const int ca = g.beg[A] - g.ext + blockIdx.x * kTM + threadIdx.x;
+  if (ca >= g.end[A] + g.ext) return;
+  const int cb = (D == 3) ? g.beg[B] - g.ext + (int)blockIdx.z : 0;
   const int m0 = g.beg[DIR] + blockIdx.y * seg;
   const int m1 = min(m0 + seg, g.end[DIR]);
-  const int j0 = (DIR == 1) ? m0 : p;
-  const int k0 = (DIR == 1) ? p : m0;
-  bool active_col = (i >= g.beg[0] && i < g.end[0]);
-  if constexpr (D == 3) {
-    const int pd = (DIR == 1) ? 2 : 1;
-    active_col = active_col && p >= g.beg[pd] && p < g.end[pd];
-  }
+  bool active_col = (ca >= g.beg[A] && ca < g.end[A]);
+  if constexpr (D == 3) active_col = active_col && cb >= g.beg[B] && cb < g.end[B];
+  int idx[3];
+  idx[DIR] = m0;
+  idx[A] = ca;
+  idx[B] = cb;
   const long long sd = g.s[DIR];
   const long long fsd = g.fs[DIR];
-  // address of the first face (cell m0) of this column
-  const long long c0 = cidx(g, (D == 3) ? k0 : 0, (DIR == 1 || D == 3) ? j0 : p, i);
-  const long long f0 = fidx(g, (D == 3) ? k0 : 0, (DIR == 1 || D == 3) ? j0 : p, i);
+  const long long c0 = cidx(g, idx[2], idx[1], idx[0]);  // cell m0 of this column
+  const long long f0 = fidx(g, idx[2], idx[1], idx[0]);
   const double* vs = f.Vs + DIR * g.nface;
   double w[NV][W];
   double vrp[NV];       // right-face state of the previous cell
@@ -455,7 +373,8 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
             f.Uc[n * g.ncell + cu] = f.Uc[n * g.ncell + cu] + rhs;
           }
           if (invdt) {
-            const double inv = f.InvDt[cu] + 0.5 * (r.cmax + cp) / (g.dx[DIR]);
+            const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
+            const double inv = prev + 0.5 * (r.cmax + cp) / (g.dx[DIR]);
             f.InvDt[cu] = inv;
             if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
           }

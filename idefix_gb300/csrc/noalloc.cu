@@ -219,8 +219,9 @@ extern "C" int idfx_evolve_stage_noalloc(const idfx_gpu_config* cfg, const doubl
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long want = (long long)sms * 512;
-  for (int d = 1; d < g.D; d++) {
-    const long long cols = (long long)(g.n[0] + 2 * g.ext) * (g.D == 3 ? g.n[3 - d] + 2 * g.ext : 1);
+  for (int d = 0; d < g.D; d++) {
+    const int a = (d == 0) ? 1 : 0, b = (d == 2) ? 1 : 2;
+    const long long cols = (long long)(g.n[a] + 2 * g.ext) * (g.D == 3 ? g.n[b] + 2 * g.ext : 1);
     int s = 64;
     while (s > 2 && cols * ((g.n[d] + s - 1) / s) < want) s /= 2;
     e.seg[d] = s;

@@ -5,33 +5,24 @@
 
 namespace idfx {
 
+template <int D, int DIR, int ORDER, int SOLVER>
+void launch_dir(Engine& e, int invdt, int last) {
+  const Geo& g = e.g;
+  constexpr int A = (DIR == 0) ? 1 : 0;
+  constexpr int B = (DIR == 2) ? 1 : 2;
+  const int nseg = (g.n[DIR] + e.seg[DIR] - 1) / e.seg[DIR];
+  dim3 grid((g.n[A] + 2 * g.ext + kTM - 1) / kTM, nseg, D == 3 ? g.n[B] + 2 * g.ext : 1);
+  mark_begin(e, kKSweepX + DIR);
+  k_sweep_march<D, DIR, ORDER, SOLVER><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt, last, e.seg[DIR]);
+  mark_end(e);
+}
+
+// invdt: 0 none, 1 first contribution of the cycle (InvDt reset), 2 accumulate
 template <int D, int ORDER, int SOLVER>
 void launch_sweeps_t(Engine& e, int invdt, int fold_max) {
-  const Geo& g = e.g;
-  // x: one block per kTX faces of each (j,k) row, rows include the CT extension
-  {
-    dim3 grid((g.n[0] + 1 + kTX - 1) / kTX, g.n[1] + 2 * g.ext, D == 3 ? g.n[2] + 2 * g.ext : 1);
-    mark_begin(e, kKSweepX);
-    k_sweep_x<D, ORDER, SOLVER><<<grid, kTX, 0, e.stream>>>(g, e.f, e.ctl, invdt, fold_max && D == 1);
-    mark_end(e);
-  }
-  // y
-  {
-    const int nseg = (g.n[1] + e.seg[1] - 1) / e.seg[1];
-    dim3 grid((g.n[0] + 2 * g.ext + kTM - 1) / kTM, nseg, D == 3 ? g.n[2] + 2 * g.ext : 1);
-    mark_begin(e, kKSweepY);
-    k_sweep_march<D, 1, ORDER, SOLVER><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt == 0 ? 0 : 2,
-                                                                   fold_max && D == 2, e.seg[1]);
-    mark_end(e);
-  }
-  if constexpr (D == 3) {
-    const int nseg = (g.n[2] + e.seg[2] - 1) / e.seg[2];
-    dim3 grid((g.n[0] + 2 * g.ext + kTM - 1) / kTM, nseg, g.n[1] + 2 * g.ext);
-    mark_begin(e, kKSweepZ);
-    k_sweep_march<D, 2, ORDER, SOLVER><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt == 0 ? 0 : 2,
-                                                                   fold_max, e.seg[2]);
-    mark_end(e);
-  }
+  launch_dir<D, 0, ORDER, SOLVER>(e, invdt, 0);
+  launch_dir<D, 1, ORDER, SOLVER>(e, invdt == 0 ? 0 : 2, fold_max && D == 2);
+  if constexpr (D == 3) launch_dir<D, 2, ORDER, SOLVER>(e, invdt == 0 ? 0 : 2, fold_max);
 }
 
 template <int SOLVER>
