@@ -31,6 +31,7 @@ LIB_PATH = os.path.join(HERE, "libidefix_gb300.so")
 ORDER = {"order1": 1, "plm": 2, "limo3": 3, "ppm": 4}
 SOLVER = {"hlld": 0, "hll": 1, "roe": 2, "tvdlf": 3}
 EMF = {"uct_contact": 0, "arithmetic": 1, "uct0": 2, "uct_hll": 3, "uct_hlld": 4}
+PRECISION = {"fp64": 0, "mixed": 1}
 
 OK, ERR_CONFIG, ERR_NAN, ERR_DIVB, ERR_DT_SMALL, ERR_FIRST_DT, ERR_CUDA, ERR_STATE = range(8)
 
@@ -130,13 +131,15 @@ class GpuBlock:
     Arguments mirror the reference's input file: [Grid] (dims, n, xbeg,
     xend), [Hydro] (solver, emf, gamma), [TimeIntegrator] (nstages, CFL,
     CFL_max_var, first_dt, maxdivB, check_nan), [Output] log, and the
-    build-time reconstruction order.
+    build-time reconstruction order.  precision: "fp64" (bit-identical to
+    the reference) or "mixed" (FP32 reconstruction and Riemann solve, FP64
+    conserved state, ConsToPrim and CT face update).
     """
 
     def __init__(self, dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm",
                  solver="hlld", emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.9,
                  cfl_max_var=1.1, first_dt=1.0e-10, maxdivb=1e-6, log_period=0,
-                 check_nan_period=0, stream=None):
+                 check_nan_period=0, precision="fp64", stream=None):
         self.lib = load_library()
         n = list(n) + [1] * (3 - len(n))
         cfg = Config()
@@ -146,6 +149,7 @@ class GpuBlock:
             cfg.xend[d] = float(xend[d]) if d < len(xend) else 1.0
         try:
             cfg.order, cfg.solver, cfg.emf = ORDER[order], SOLVER[solver], EMF[emf]
+            cfg.precision = PRECISION[precision]
         except KeyError as exc:
             raise IdefixError(f"unknown scheme option {exc}") from None
         cfg.nstages = nstages

@@ -305,7 +305,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   if (cfg->dims != 2 && cfg->dims != 3) return IDFX_ERR_CONFIG;
   if (cfg->order < 1 || cfg->order > 4 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
   if (cfg->emf < 0 || cfg->emf > 4 || cfg->nstages < 1 || cfg->nstages > 3) return IDFX_ERR_CONFIG;
-  if (cfg->precision != IDFX_FP64) return IDFX_ERR_CONFIG;
+  if (cfg->precision != IDFX_FP64 && cfg->precision != IDFX_MIXED) return IDFX_ERR_CONFIG;
   // constrainedTransport.hpp:256-261
   if (cfg->emf == IDFX_EMF_UCT_HLLD && (cfg->solver == IDFX_HLL || cfg->solver == IDFX_TVDLF))
     return IDFX_ERR_CONFIG;
@@ -354,6 +354,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   g.ext = 1;  // hlldMHD.hpp:30-49: uct_hll(d) with HLLD/HLL needs nghost cells
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
   e.nstages = cfg->nstages;
+  e.precision = cfg->precision;
   if (e.nstages == 2) {  // timeIntegrator.cpp:62-71
     e.wc[0] = 0.5;
     e.w0[0] = 0.5;

@@ -18,6 +18,7 @@ struct Engine {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int nstages = 2;
+  int precision = 0;         // 0: FP64 bit-exact, 1: mixed (FP32 recon + Riemann)
   double wc[2] = {0, 0}, w0[2] = {0, 0};
   int log_period = 0, check_nan_period = 0;
   long long ncycles = 0;     // host mirror of the cycle counter

@@ -185,28 +185,27 @@ __global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
 // ---------------------------------------------------------------------------
 // EMF side outputs of a face (storeFlux.hpp:14-208)
 // ---------------------------------------------------------------------------
-template <int D, int DIR>
+template <int D, int DIR, typename T>
 __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long long c,
-                                          const RiemannOut<D>& r, const double* vL,
-                                          const double* vR) {
+                                          const RiemannOut<D, T>& r, const T* vL, const T* vR) {
   using d = Dir<D, DIR>;
   using vv = Var<D>;
-  double st, sb;
+  T st, sb;
   double *Et, *Eb, *SV;
   if constexpr (DIR == 0) {
-    st = -1.0; sb = +1.0; Et = f.ezi; Eb = f.eyi; SV = f.svx;
+    st = T(-1); sb = T(+1); Et = f.ezi; Eb = f.eyi; SV = f.svx;
   } else if constexpr (DIR == 1) {
-    st = +1.0; sb = -1.0; Et = f.ezj; Eb = f.exj; SV = f.svy;
+    st = T(+1); sb = T(-1); Et = f.ezj; Eb = f.exj; SV = f.svy;
   } else {
-    st = -1.0; sb = +1.0; Et = f.eyk; Eb = f.exk; SV = f.svz;
+    st = T(-1); sb = T(+1); Et = f.eyk; Eb = f.exk; SV = f.svz;
   }
   if (g.emf == kEmfContact || g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
-    Et[c] = st * r.F[d::BXt];
-    if constexpr (D == 3) Eb[c] = sb * r.F[d::BXb];
+    Et[c] = (double)(st * r.F[d::BXt]);
+    if constexpr (D == 3) Eb[c] = (double)(sb * r.F[d::BXb]);
     if (g.emf == kEmfContact) {
       double s = 0.5;
-      if (r.F[vv::RHO] > kEpsUctContact) s = 1.0;
-      if (r.F[vv::RHO] < -kEpsUctContact) s = 0.0;
+      if (r.F[vv::RHO] > T(kEpsUctContact)) s = 1.0;
+      if (r.F[vv::RHO] < T(-kEpsUctContact)) s = 0.0;
       SV[c] = s;
     }
     return;
@@ -215,71 +214,71 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
   double* aR = f.aR[DIR];
   double* dL = f.dL[DIR];
   double* dR = f.dR[DIR];
-  const double sl = r.sl, sr = r.sr;
+  const T sl = r.sl, sr = r.sr;
   if (g.emf == kEmfUctHll) {
-    const double ar = fmax(0.0, sr);
-    const double al = fmin(0.0, sl);
-    const double scrh = 1.0 / (ar - al);
-    Et[c] = -st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh;
-    if constexpr (D == 3) Eb[c] = -sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh;
-    aL[c] = ar * scrh;
-    aR[c] = -al * scrh;
-    const double dr = -al * ar * scrh;
-    dR[c] = dr;
-    dL[c] = dr;
+    const T ar = fmax(T(0), sr);
+    const T al = fmin(T(0), sl);
+    const T scrh = dv(T(1), ar - al);
+    Et[c] = (double)(-st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh);
+    if constexpr (D == 3) Eb[c] = (double)(-sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh);
+    aL[c] = (double)(ar * scrh);
+    aR[c] = (double)(-al * scrh);
+    const T dr = -al * ar * scrh;
+    dR[c] = (double)dr;
+    dL[c] = (double)dr;
     return;
   }
   // uct_hlld (K_StoreHLLD, energy branch)
-  const double* uL = r.uL;
-  const double* uR = r.uR;
-  const double ptL = vL[vv::PRS] + half_b2<D>(vL);
-  const double ptR = vR[vv::PRS] + half_b2<D>(vR);
+  const T* uL = r.uL;
+  const T* uR = r.uR;
+  const T ptL = vL[vv::PRS] + half_b2<D>(vL);
+  const T ptR = vR[vv::PRS] + half_b2<D>(vR);
   int revert_to_hll = 0;
-  const double Bn = (sr * vR[d::BXn] - sl * vL[d::BXn]) / (sr - sl);
-  const double duL = sl - vL[d::Xn];
-  const double duR = sr - vR[d::Xn];
-  double scrh = 1.0 / (duR * uR[vv::RHO] - duL * uL[vv::RHO]);
-  const double Sc = (duR * uR[d::Xn] - duL * uL[d::Xn] - ptR + ptL) * scrh;
-  const double usLRHO = uL[vv::RHO] * duL / (sl - Sc);
-  const double usRRHO = uR[vv::RHO] * duR / (sr - Sc);
-  const double sqrL = sqrt(usLRHO);
-  const double sqrR = sqrt(usRRHO);
-  const double SaL = Sc - fabs(Bn) / sqrL;
-  const double SaR = Sc + fabs(Bn) / sqrR;
-  if ((SaL - sl) < 1e-4 * (Sc - sl)) revert_to_hll = 1;
-  if ((SaR - sr) > -1e-4 * (sr - Sc)) revert_to_hll = 1;
-  const double chiL = (vL[d::Xn] - Sc) * (sl - Sc) / (SaL + sl - 2.0 * Sc);
-  const double chiR = (vR[d::Xn] - Sc) * (sr - Sc) / (SaR + sr - 2.0 * Sc);
-  const double nuL = (SaL + sl) / (fabs(SaL) + fabs(sl));
-  const double nuR = (SaR + sr) / (fabs(SaR) + fabs(sr));
-  const double nuLR = (SaL + SaR) / (fabs(SaL) + fabs(SaR));
-  double a_l, a_r, d_l, d_r;
-  if (fabs(SaR - SaL) > 1.e-9 * fabs(sr - sl)) {
-    d_l = 0.5 * (chiL * nuL - chiL * nuLR) + 0.5 * (fabs(SaL) - nuLR * SaL);
-    d_r = 0.5 * (chiR * nuR - chiR * nuLR) + 0.5 * (fabs(SaR) - nuLR * SaR);
-    a_l = 0.5 * (1.0 + nuLR);
-    a_r = 0.5 * (1.0 - nuLR);
+  const T Bn = dv(sr * vR[d::BXn] - sl * vL[d::BXn], sr - sl);
+  const T duL = sl - vL[d::Xn];
+  const T duR = sr - vR[d::Xn];
+  T scrh = dv(T(1), duR * uR[vv::RHO] - duL * uL[vv::RHO]);
+  const T Sc = (duR * uR[d::Xn] - duL * uL[d::Xn] - ptR + ptL) * scrh;
+  const T usLRHO = dv(uL[vv::RHO] * duL, sl - Sc);
+  const T usRRHO = dv(uR[vv::RHO] * duR, sr - Sc);
+  const T sqrL = sqrt(usLRHO);
+  const T sqrR = sqrt(usRRHO);
+  const T SaL = Sc - dv(fabs(Bn), sqrL);
+  const T SaR = Sc + dv(fabs(Bn), sqrR);
+  if ((SaL - sl) < T(1e-4) * (Sc - sl)) revert_to_hll = 1;
+  if ((SaR - sr) > T(-1e-4) * (sr - Sc)) revert_to_hll = 1;
+  const T chiL = dv((vL[d::Xn] - Sc) * (sl - Sc), SaL + sl - T(2) * Sc);
+  const T chiR = dv((vR[d::Xn] - Sc) * (sr - Sc), SaR + sr - T(2) * Sc);
+  const T nuL = dv(SaL + sl, fabs(SaL) + fabs(sl));
+  const T nuR = dv(SaR + sr, fabs(SaR) + fabs(sr));
+  const T nuLR = dv(SaL + SaR, fabs(SaL) + fabs(SaR));
+  T a_l, a_r, d_l, d_r;
+  if (fabs(SaR - SaL) > T(1.e-9) * fabs(sr - sl)) {
+    d_l = T(0.5) * (chiL * nuL - chiL * nuLR) + T(0.5) * (fabs(SaL) - nuLR * SaL);
+    d_r = T(0.5) * (chiR * nuR - chiR * nuLR) + T(0.5) * (fabs(SaR) - nuLR * SaR);
+    a_l = T(0.5) * (T(1) + nuLR);
+    a_r = T(0.5) * (T(1) - nuLR);
   } else {
-    d_l = 0.5 * chiL * nuL + 0.5 * fabs(SaL);
-    d_r = 0.5 * chiR * nuR + 0.5 * fabs(SaR);
-    a_l = 0.5;
-    a_r = 0.5;
+    d_l = T(0.5) * chiL * nuL + T(0.5) * fabs(SaL);
+    d_r = T(0.5) * chiR * nuR + T(0.5) * fabs(SaR);
+    a_l = T(0.5);
+    a_r = T(0.5);
   }
-  const double ar = fmax(0.0, sr);
-  const double al = fmin(0.0, sl);
-  scrh = 1.0 / (ar - al);
+  const T ar = fmax(T(0), sr);
+  const T al = fmin(T(0), sl);
+  scrh = dv(T(1), ar - al);
   if (revert_to_hll) {
     a_l = ar * scrh;
     a_r = -al * scrh;
     d_r = -al * ar * scrh;
     d_l = d_r;
   }
-  aL[c] = a_l;
-  aR[c] = a_r;
-  dL[c] = d_l;
-  dR[c] = d_r;
-  Et[c] = -st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh;
-  if constexpr (D == 3) Eb[c] = -sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh;
+  aL[c] = (double)a_l;
+  aR[c] = (double)a_r;
+  dL[c] = (double)d_l;
+  dR[c] = (double)d_r;
+  Et[c] = (double)(-st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh);
+  if constexpr (D == 3) Eb[c] = (double)(-sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh);
 }
 
 // ---------------------------------------------------------------------------
@@ -297,7 +296,11 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
 // ---------------------------------------------------------------------------
 constexpr int kTM = 64;
 
-template <int D, int DIR, int ORDER, int SOLVER>
+// T: arithmetic of the reconstruction and the Riemann solve (double: the
+// bit-exact path; float: the mixed-precision path).  The state is read in
+// FP64 and converted once per cell; the flux difference, the conserved
+// update and InvDt are FP64 in both.
+template <int D, int DIR, int ORDER, int SOLVER, typename T>
 __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl* ctl, int invdt,
                                                      int last_dir, int seg) {
   if (ctl->done) return;
@@ -324,8 +327,10 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
   const long long c0 = cidx(g, idx[2], idx[1], idx[0]);  // cell m0 of this column
   const long long f0 = fidx(g, idx[2], idx[1], idx[0]);
   const double* vs = f.Vs + DIR * g.nface;
-  double w[NV][W];
-  double vrp[NV];       // right-face state of the previous cell
+  const T dxd = (T)g.dx[DIR];
+  const T gam = (T)g.gamma;
+  T w[NV][W];
+  T vrp[NV];            // right-face state of the previous cell
   double Fp[v::BX1];    // flux x A of the previous face
   double cp = 0.0;      // cmax of the previous face
   // prime the window with cells m0-1-H .. m0-2+H
@@ -333,38 +338,38 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
   for (int n = 0; n < NV; n++) {
     if (n == dd::BXn) continue;
 #pragma unroll
-    for (int m = 0; m < W - 1; m++) w[n][m + 1] = f.Vc[n * g.ncell + c0 + (m - 1 - H) * sd];
+    for (int m = 0; m < W - 1; m++) w[n][m + 1] = (T)f.Vc[n * g.ncell + c0 + (m - 1 - H) * sd];
   }
   const double dtdV = ctl->dtdV;
   for (int c = m0 - 1; c <= m1; c++) {
     const long long cc = c0 + (long long)(c - m0) * sd;
-    double vl[NV], vr[NV];
+    T vl[NV], vr[NV];
 #pragma unroll
     for (int n = 0; n < NV; n++) {
       if (n == dd::BXn) continue;
 #pragma unroll
       for (int m = 0; m < W - 1; m++) w[n][m] = w[n][m + 1];
-      w[n][W - 1] = f.Vc[n * g.ncell + cc + H * sd];
-      Recon<ORDER>::cell(w[n], g.dx[DIR], n == v::RHO || n == v::PRS, vl[n], vr[n]);
+      w[n][W - 1] = (T)f.Vc[n * g.ncell + cc + H * sd];
+      Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n]);
     }
     if (c >= m0) {
-      double vL[NV], vR[NV];
+      T vL[NV], vR[NV];
 #pragma unroll
       for (int n = 0; n < NV; n++) {
         if (n == dd::BXn) continue;
         vL[n] = vrp[n];
         vR[n] = vl[n];
       }
-      const double bn = vs[f0 + (long long)(c - m0) * fsd];
+      const T bn = (T)vs[f0 + (long long)(c - m0) * fsd];
       vL[dd::BXn] = bn;
       vR[dd::BXn] = bn;
-      RiemannOut<D> r;
-      riemann<D, DIR, SOLVER>(g.gamma, vL, vR, r);
+      RiemannOut<D, T> r;
+      riemann<D, DIR, SOLVER>(gam, vL, vR, r);
       store_emf<D, DIR>(g, f, cc, r, vL, vR);
       if (active_col) {
         double FA[v::BX1];
 #pragma unroll
-        for (int n = 0; n < v::BX1; n++) FA[n] = r.F[n] * g.A[DIR];
+        for (int n = 0; n < v::BX1; n++) FA[n] = (double)r.F[n] * g.A[DIR];
         if (c > m0) {
           const long long cu = cc - sd;  // cell c-1
 #pragma unroll
@@ -374,14 +379,14 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
           }
           if (invdt) {
             const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
-            const double inv = prev + 0.5 * (r.cmax + cp) / (g.dx[DIR]);
+            const double inv = prev + 0.5 * ((double)r.cmax + cp) / (g.dx[DIR]);
             f.InvDt[cu] = inv;
             if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
           }
         }
 #pragma unroll
         for (int n = 0; n < v::BX1; n++) Fp[n] = FA[n];
-        cp = r.cmax;
+        cp = (double)r.cmax;
       }
     }
 #pragma unroll

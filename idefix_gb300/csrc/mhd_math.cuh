@@ -1,8 +1,14 @@
 // Device arithmetic of the ideal-MHD stage: cons/prim, physical flux, slope
 // limiters, face reconstruction and the HLLD / HLL / Roe / TVDLF Riemann
-// solvers.  FP64, compiled with --fmad=false: every expression keeps the
-// operation order of the reference so that results are bit-identical to it
-// (the reference's GPU CI also disables contraction, pytools/idfx_test.py:121).
+// solvers, templated on the arithmetic type T.
+//
+// T = double is the parity path: compiled with --fmad=false, every
+// expression keeps the operation order of the reference so that results are
+// bit-identical to it (the reference's GPU CI also disables contraction,
+// pytools/idfx_test.py:121).  Literals are written T(x), which is the same
+// double for T = double.  T = float is the mixed-precision path (FP32
+// reconstruction and Riemann solve; the callers keep the conserved state,
+// cons->prim and the CT face update in FP64).
 //
 // D is the number of dimensions (= components, 2 or 3).  Variable order
 // follows src/idefix.hpp:74-108: RHO, MX1..MXD, ENG(=PRS), BX1..BXD.
@@ -34,10 +40,16 @@ struct Dir {
 constexpr double kSmallPressureFix = 1.0e-5;  // fluid_defs.hpp:23
 constexpr double kEpsUctContact = 1.0e-6;     // fluid_defs.hpp:24
 
-// sum of squares of the first D entries starting at a, in reference order
-template <int D>
-__device__ __forceinline__ double sumsq(double a, double b, double c) {
-  double s = a * a + b * b;
+// division: IEEE correctly rounded in both precisions
+template <typename T>
+__device__ __forceinline__ T dv(T a, T b) {
+  return a / b;
+}
+
+// sum of squares of the first D entries, in reference order
+template <int D, typename T>
+__device__ __forceinline__ T sumsq(T a, T b, T c) {
+  T s = a * a + b * b;
   if constexpr (D == 3) s = s + c * c;
   return s;
 }
@@ -46,8 +58,8 @@ __device__ __forceinline__ double sumsq(double a, double b, double c) {
 // cons <-> prim (convertConsToPrim.hpp:15-100; eos_adiabatic.hpp:38-45)
 // gm1 = gamma - 1.0, evaluated once on the host
 // ---------------------------------------------------------------------------
-template <int D>
-__device__ __forceinline__ void prim_to_cons(double gm1, double* U, const double* V) {
+template <int D, typename T>
+__device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V) {
   using v = Var<D>;
   U[v::RHO] = V[v::RHO];
   U[v::MX1] = V[v::MX1] * V[v::RHO];
@@ -56,67 +68,69 @@ __device__ __forceinline__ void prim_to_cons(double gm1, double* U, const double
   U[v::BX1] = V[v::BX1];
   U[v::BX2] = V[v::BX2];
   if constexpr (D == 3) U[v::BX3] = V[v::BX3];
-  double kin, mag;
+  const T z = T(0);
+  T kin, mag;
   if constexpr (D == 3) {
     kin = sumsq<3>(V[v::MX1], V[v::MX2], V[v::MX3]);
     mag = sumsq<3>(U[v::BX1], U[v::BX2], U[v::BX3]);
   } else {
-    kin = sumsq<2>(V[v::MX1], V[v::MX2], 0.0);
-    mag = sumsq<2>(U[v::BX1], U[v::BX2], 0.0);
+    kin = sumsq<2>(V[v::MX1], V[v::MX2], z);
+    mag = sumsq<2>(U[v::BX1], U[v::BX2], z);
   }
-  U[v::ENG] = V[v::PRS] / gm1 + 0.5 * V[v::RHO] * kin + 0.5 * mag;
+  U[v::ENG] = dv(V[v::PRS], gm1) + T(0.5) * V[v::RHO] * kin + T(0.5) * mag;
 }
 
-template <int D>
-__device__ __forceinline__ void cons_to_prim(double gm1, double* V, const double* U) {
+template <int D, typename T>
+__device__ __forceinline__ void cons_to_prim(T gm1, T* V, const T* U) {
   using v = Var<D>;
   V[v::RHO] = U[v::RHO];
-  V[v::MX1] = U[v::MX1] / U[v::RHO];
-  V[v::MX2] = U[v::MX2] / U[v::RHO];
-  if constexpr (D == 3) V[v::MX3] = U[v::MX3] / U[v::RHO];
+  V[v::MX1] = dv(U[v::MX1], U[v::RHO]);
+  V[v::MX2] = dv(U[v::MX2], U[v::RHO]);
+  if constexpr (D == 3) V[v::MX3] = dv(U[v::MX3], U[v::RHO]);
   V[v::BX1] = U[v::BX1];
   V[v::BX2] = U[v::BX2];
   if constexpr (D == 3) V[v::BX3] = U[v::BX3];
-  double m2, b2;
+  const T z = T(0);
+  T m2, b2;
   if constexpr (D == 3) {
     m2 = sumsq<3>(U[v::MX1], U[v::MX2], U[v::MX3]);
     b2 = sumsq<3>(U[v::BX1], U[v::BX2], U[v::BX3]);
   } else {
-    m2 = sumsq<2>(U[v::MX1], U[v::MX2], 0.0);
-    b2 = sumsq<2>(U[v::BX1], U[v::BX2], 0.0);
+    m2 = sumsq<2>(U[v::MX1], U[v::MX2], z);
+    b2 = sumsq<2>(U[v::BX1], U[v::BX2], z);
   }
-  double kin = 0.5 / U[v::RHO] * m2;
-  double mag = 0.5 * b2;
+  const T kin = dv(T(0.5), U[v::RHO]) * m2;
+  const T mag = T(0.5) * b2;
   V[v::PRS] = (U[v::ENG] - kin - mag) * gm1;
   // floor; the reference's energy repair only touches a discarded local copy
-  if (V[v::PRS] <= 0.0) V[v::PRS] = kSmallPressureFix;
+  if (V[v::PRS] <= T(0)) V[v::PRS] = T(kSmallPressureFix);
 }
 
 // physical MHD flux along DIR (flux.hpp:28-95); U is read before F is written
-template <int D, int DIR>
-__device__ __forceinline__ void phys_flux(double* F, const double* V, const double* U) {
+template <int D, int DIR, typename T>
+__device__ __forceinline__ void phys_flux(T* F, const T* V, const T* U) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
-  const double uXn = U[d::Xn], uE = U[v::ENG];
-  const double u1 = U[v::MX1], u2 = U[v::MX2];
-  double u3 = 0.0;
+  const T uXn = U[d::Xn], uE = U[v::ENG];
+  const T u1 = U[v::MX1], u2 = U[v::MX2];
+  T u3 = T(0);
   if constexpr (D == 3) u3 = U[v::MX3];
   F[v::RHO] = uXn;
   F[v::MX1] = u1 * V[d::Xn] - V[d::BXn] * V[v::BX1];
   F[v::MX2] = u2 * V[d::Xn] - V[d::BXn] * V[v::BX2];
   if constexpr (D == 3) F[v::MX3] = u3 * V[d::Xn] - V[d::BXn] * V[v::BX3];
-  F[d::BXn] = 0.0;
+  F[d::BXn] = T(0);
   F[d::BXt] = V[d::Xn] * V[d::BXt] - V[d::BXn] * V[d::Xt];
   if constexpr (D == 3) F[d::BXb] = V[d::Xn] * V[d::BXb] - V[d::BXn] * V[d::Xb];
-  double Bmag2, vB;
+  T Bmag2, vB;
   if constexpr (D == 3) {
     Bmag2 = sumsq<3>(V[v::BX1], V[v::BX2], V[v::BX3]);
     vB = V[v::MX1] * V[v::BX1] + V[v::MX2] * V[v::BX2] + V[v::MX3] * V[v::BX3];
   } else {
-    Bmag2 = sumsq<2>(V[v::BX1], V[v::BX2], 0.0);
+    Bmag2 = sumsq<2>(V[v::BX1], V[v::BX2], T(0));
     vB = V[v::MX1] * V[v::BX1] + V[v::MX2] * V[v::BX2];
   }
-  const double ptot = V[v::PRS] + 0.5 * Bmag2;
+  const T ptot = V[v::PRS] + T(0.5) * Bmag2;
   F[v::ENG] = (uE + ptot) * V[d::Xn] - V[d::BXn] * (vB);
   F[d::Xn] += ptot;
 }
@@ -126,86 +140,97 @@ __device__ __forceinline__ void phys_flux(double* F, const double* V, const doub
 // ---------------------------------------------------------------------------
 // The reference MinModLim shadows its result variable and always returns 0
 // (slopeLimiter.hpp:16-23); every "revert to minmod" path therefore adds 0.
-__device__ __forceinline__ double lim_minmod(double, double) { return 0.0; }
-
-__device__ __forceinline__ double lim_vanleer(double dvp, double dvm) {  // :54-57
-  return (dvp * dvm > 0.0 ? 2.0 * dvp * dvm / (dvp + dvm) : 0.0);
+template <typename T>
+__device__ __forceinline__ T lim_minmod(T, T) {
+  return T(0);
 }
 
-__device__ __forceinline__ double lim_mc(double dvp, double dvm) {  // :68-76
-  double dq = 0;
-  if (dvp * dvm > 0.0) {
-    double dqc = 0.5 * (dvp + dvm);
-    double d2q = 2.0 * (fabs(dvp) < fabs(dvm) ? dvp : dvm);
+template <typename T>
+__device__ __forceinline__ T lim_vanleer(T dvp, T dvm) {  // :54-57
+  return (dvp * dvm > T(0) ? dv(T(2) * dvp * dvm, dvp + dvm) : T(0));
+}
+
+template <typename T>
+__device__ __forceinline__ T lim_mc(T dvp, T dvm) {  // :68-76
+  T dq = T(0);
+  if (dvp * dvm > T(0)) {
+    T dqc = T(0.5) * (dvp + dvm);
+    T d2q = T(2) * (fabs(dvp) < fabs(dvm) ? dvp : dvm);
     dq = fabs(d2q) < fabs(dqc) ? d2q : dqc;
   }
   return dq;
 }
 
-__device__ __forceinline__ double lim_limo3(double dvp, double dvm, double dx) {  // :25-52
-  const double r = 0.1, eps = 1.e-12;
-  double th = dvm / (dvp + 1.e-16);
-  double q = (2.0 + th) / 3.0;
-  double a = fmin(1.5, 2.0 * th);
+template <typename T>
+__device__ __forceinline__ T lim_limo3(T dvp, T dvm, T dx) {  // :25-52
+  const T r = T(0.1), eps = T(1.e-12);
+  T th = dv(dvm, dvp + T(1.e-16));
+  T q = dv(T(2) + th, T(3));
+  T a = fmin(T(1.5), T(2) * th);
   a = fmin(q, a);
-  double b = fmax(-0.5 * th, a);
-  double c = fmin(q, b);
-  double psi = fmax(0.0, c);
-  double eta = r * dx;
-  eta = (dvm * dvm + dvp * dvp) / (eta * eta);
-  double lim;
-  if (eta <= 1.0 - eps) {
+  T b = fmax(T(-0.5) * th, a);
+  T c = fmin(q, b);
+  T psi = fmax(T(0), c);
+  T eta = r * dx;
+  eta = dv(dvm * dvm + dvp * dvp, eta * eta);
+  T lim;
+  if (eta <= T(1) - eps) {
     lim = q;
-  } else if (eta >= 1.0 + eps) {
+  } else if (eta >= T(1) + eps) {
     lim = psi;
   } else {
-    psi = (1.0 - (eta - 1.0) / eps) * q + (1.0 + (eta - 1.0) / eps) * psi;
-    lim = 0.5 * psi;
+    psi = (T(1) - dv(eta - T(1), eps)) * q + (T(1) + dv(eta - T(1), eps)) * psi;
+    lim = T(0.5) * psi;
   }
   return lim;
 }
 
-__device__ __forceinline__ int sgn(double v) { return (0.0 < v) - (v < 0.0); }
+template <typename T>
+__device__ __forceinline__ int sgn(T v) {
+  return (T(0) < v) - (v < T(0));
+}
 
-__device__ __forceinline__ void ppm_limit_face(double vm1, double v0, double vp1, double vp2,
-                                               double& vph) {  // :121-140
-  if ((vp1 - vph) * (vph - v0) < 0.0) {
-    const double deltaL = (vm1 - 2 * v0 + vp1);
-    const double deltaC = 3 * (v0 - 2 * vph + vp1);
-    const double deltaR = (v0 - 2 * vp1 + vp2);
-    double delta = 0.0;
+template <typename T>
+__device__ __forceinline__ void ppm_limit_face(T vm1, T v0, T vp1, T vp2, T& vph) {  // :121-140
+  if ((vp1 - vph) * (vph - v0) < T(0)) {
+    const T deltaL = (vm1 - 2 * v0 + vp1);
+    const T deltaC = 3 * (v0 - 2 * vph + vp1);
+    const T deltaR = (v0 - 2 * vp1 + vp2);
+    T delta = T(0);
     if (sgn(deltaL) == sgn(deltaC) && sgn(deltaR) == sgn(deltaC)) {
-      const double C = 1.25;
+      const T C = T(1.25);
       delta = C * fmin(fabs(deltaL), fabs(deltaR));
       delta = sgn(deltaC) * fmin(delta, fabs(deltaC));
     }
-    vph = 0.5 * (v0 + vp1) - delta / 6.0;
+    vph = T(0.5) * (v0 + vp1) - dv(delta, T(6));
   }
 }
 
-__device__ __forceinline__ void ppm_states(double vm2, double vm1, double v0, double vp1, double vp2,
-                                           double& vl, double& vr) {  // :142-191
+template <typename T>
+__device__ __forceinline__ void ppm_states(T vm2, T vm1, T v0, T vp1, T vp2, T& vl,
+                                           T& vr) {  // :142-191
   const int n = 2;
-  vr = 7.0 / 12.0 * (v0 + vp1) - 1.0 / 12.0 * (vm1 + vp2);
-  vl = 7.0 / 12.0 * (vm1 + v0) - 1.0 / 12.0 * (vm2 + vp1);
+  const T c7 = T(7.0 / 12.0), c1 = T(1.0 / 12.0);
+  vr = c7 * (v0 + vp1) - c1 * (vm1 + vp2);
+  vl = c7 * (vm1 + v0) - c1 * (vm2 + vp1);
   ppm_limit_face(vm2, vm1, v0, vp1, vl);
   ppm_limit_face(vm1, v0, vp1, vp2, vr);
-  double d2qf = 6.0 * (vl + vr - 2.0 * v0);
-  double d2qc0 = vm1 + vp1 - 2.0 * v0;
-  double d2qcp1 = v0 + vp2 - 2.0 * vp1;
-  double d2qcm1 = vm2 + v0 - 2.0 * vm1;
-  double d2q = 0.0;
+  T d2qf = T(6) * (vl + vr - T(2) * v0);
+  T d2qc0 = vm1 + vp1 - T(2) * v0;
+  T d2qcp1 = v0 + vp2 - T(2) * vp1;
+  T d2qcm1 = vm2 + v0 - T(2) * vm1;
+  T d2q = T(0);
   if (sgn(d2qf) == sgn(d2qc0) && sgn(d2qf) == sgn(d2qcp1) && sgn(d2qf) == sgn(d2qcm1)) {
-    const double C = 1.25;
+    const T C = T(1.25);
     d2q = fmin(fabs(d2qc0), fabs(d2qcp1));
     d2q = C * fmin(fabs(d2qcm1), d2q);
     d2q = sgn(d2qf) * fmin(fabs(d2qf), d2q);
   }
-  double qmax = fmax(fmax(fabs(vm1), fabs(v0)), fabs(vp1));
-  double rho = 0.0;
-  if (fabs(d2qf) > 1e-12 * qmax) rho = d2q / d2qf;
-  if (((vr - v0) * (v0 - vl) <= 0) || (vm1 - v0) * (v0 - vp1) <= 0) {
-    if (rho <= (1.0 - 1e-12)) {
+  T qmax = fmax(fmax(fabs(vm1), fabs(v0)), fabs(vp1));
+  T rho = T(0);
+  if (fabs(d2qf) > T(1e-12) * qmax) rho = dv(d2q, d2qf);
+  if (((vr - v0) * (v0 - vl) <= T(0)) || (vm1 - v0) * (v0 - vp1) <= T(0)) {
+    if (rho <= (T(1) - T(1e-12))) {
       vl = v0 - rho * (v0 - vl);
       vr = v0 + rho * (vr - v0);
     }
@@ -225,41 +250,41 @@ __device__ __forceinline__ void ppm_states(double vm2, double vm1, double v0, do
 template <int ORDER>
 struct Recon {
   static constexpr int H = (ORDER == 1 ? 0 : (ORDER == 4 ? 2 : 1));
-  __device__ __forceinline__ static void cell(const double* w, double dx, bool pos, double& vl,
-                                              double& vr) {
+  template <typename T>
+  __device__ __forceinline__ static void cell(const T* w, T dx, bool pos, T& vl, T& vr) {
     if constexpr (ORDER == 1) {
       vl = w[0];
       vr = w[0];
     } else if constexpr (ORDER == 2) {
-      const double dvm = w[1] - w[0];
-      const double dvp = w[2] - w[1];
-      const double dv = lim_vanleer(dvp, dvm);
-      vr = w[1] + 0.5 * dv;
-      vl = w[1] - 0.5 * dv;
+      const T dvm = w[1] - w[0];
+      const T dvp = w[2] - w[1];
+      const T d = lim_vanleer(dvp, dvm);
+      vr = w[1] + T(0.5) * d;
+      vl = w[1] - T(0.5) * d;
     } else if constexpr (ORDER == 3) {
-      const double dm = w[1] - w[0];
-      const double dp = w[2] - w[1];
-      double dv = dp * lim_limo3(dp, dm, dx);
-      vr = w[1] + 0.5 * dv;
-      if (pos && vr <= 0.0) {
-        dv = lim_minmod(dp, dm);
-        vr = w[1] + 0.5 * dv;
+      const T dm = w[1] - w[0];
+      const T dp = w[2] - w[1];
+      T d = dp * lim_limo3(dp, dm, dx);
+      vr = w[1] + T(0.5) * d;
+      if (pos && vr <= T(0)) {
+        d = lim_minmod(dp, dm);
+        vr = w[1] + T(0.5) * d;
       }
-      dv = dm * lim_limo3(dm, dp, dx);
-      vl = w[1] - 0.5 * dv;
-      if (pos && vl <= 0.0) {
-        dv = lim_minmod(dp, dm);
-        vl = w[1] - 0.5 * dv;
+      d = dm * lim_limo3(dm, dp, dx);
+      vl = w[1] - T(0.5) * d;
+      if (pos && vl <= T(0)) {
+        d = lim_minmod(dp, dm);
+        vl = w[1] - T(0.5) * d;
       }
     } else {
       ppm_states(w[0], w[1], w[2], w[3], w[4], vl, vr);
-      if (pos && vr <= 0.0) {
-        double dv = lim_vanleer(w[3] - w[2], w[2] - w[1]);
-        vr = w[2] + 0.5 * dv;
+      if (pos && vr <= T(0)) {
+        T d = lim_vanleer(w[3] - w[2], w[2] - w[1]);
+        vr = w[2] + T(0.5) * d;
       }
-      if (pos && vl <= 0.0) {
-        double dv = lim_vanleer(w[3] - w[2], w[2] - w[1]);
-        vl = w[2] - 0.5 * dv;
+      if (pos && vl <= T(0)) {
+        T d = lim_vanleer(w[3] - w[2], w[2] - w[1]);
+        vl = w[2] - T(0.5) * d;
       }
     }
   }
@@ -271,102 +296,101 @@ struct Recon {
 // ---------------------------------------------------------------------------
 enum Solver { kHLLD = 0, kHLL = 1, kROE = 2, kTVDLF = 3 };
 
-template <int D>
+template <int D, typename T>
 struct RiemannOut {
-  double F[Var<D>::NV];
-  double uL[Var<D>::NV], uR[Var<D>::NV];
-  double cmax, sl, sr;
+  T F[Var<D>::NV];
+  T uL[Var<D>::NV], uR[Var<D>::NV];
+  T cmax, sl, sr;
 };
 
 // fast magnetosonic speed of one face state (hlldMHD.hpp:205-238)
-template <int D, int DIR>
-__device__ __forceinline__ double fast_speed(double gamma, const double* v) {
+template <int D, int DIR, typename T>
+__device__ __forceinline__ T fast_speed(T gamma, const T* v) {
   using vv = Var<D>;
   using d = Dir<D, DIR>;
-  const double gpr = gamma * v[vv::PRS];
-  const double b1 = v[d::BXn];
-  const double b2 = v[d::BXt];
-  double b3 = 0.0;
+  const T gpr = gamma * v[vv::PRS];
+  const T b1 = v[d::BXn];
+  const T b2 = v[d::BXt];
+  T b3 = T(0);
   if constexpr (D == 3) b3 = v[d::BXb];
-  const double Btmag2 = b2 * b2 + b3 * b3;
-  const double Bmag2 = b1 * b1 + Btmag2;
-  double c = gpr - Bmag2;
-  c = gpr + Bmag2 + sqrt(c * c + 4.0 * gpr * Btmag2);
-  c = sqrt(0.5 * c / v[vv::RHO]);
+  const T Btmag2 = b2 * b2 + b3 * b3;
+  const T Bmag2 = b1 * b1 + Btmag2;
+  T c = gpr - Bmag2;
+  c = gpr + Bmag2 + sqrt(c * c + T(4) * gpr * Btmag2);
+  c = sqrt(dv(T(0.5) * c, v[vv::RHO]));
   return c;
 }
 
-template <int D>
-__device__ __forceinline__ double half_b2(const double* v) {
+template <int D, typename T>
+__device__ __forceinline__ T half_b2(const T* v) {
   using vv = Var<D>;
-  if constexpr (D == 3) return 0.5 * (sumsq<3>(v[vv::BX1], v[vv::BX2], v[vv::BX3]));
-  return 0.5 * (sumsq<2>(v[vv::BX1], v[vv::BX2], 0.0));
+  if constexpr (D == 3) return T(0.5) * (sumsq<3>(v[vv::BX1], v[vv::BX2], v[vv::BX3]));
+  return T(0.5) * (sumsq<2>(v[vv::BX1], v[vv::BX2], T(0)));
 }
 
 // HLLD (Miyoshi & Kusano 2005) with the reference's HLLC fall-back near
 // degeneracy (hlldMHD.hpp:147-457, energy equation branch)
-template <int D, int DIR>
-__device__ __forceinline__ void riemann_hlld(double gamma, const double* vL, const double* vR,
-                                             RiemannOut<D>& r) {
+template <int D, int DIR, typename T>
+__device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
   constexpr int RHO = v::RHO, ENG = v::ENG, Xn = d::Xn, Xt = d::Xt, Xb = d::Xb;
   constexpr int BXn = d::BXn, BXt = d::BXt, BXb = d::BXb;
-  double* uL = r.uL;
-  double* uR = r.uR;
-  double fluxL[NV], fluxR[NV];
-  const double cL = fast_speed<D, DIR>(gamma, vL);
-  const double cR = fast_speed<D, DIR>(gamma, vR);
-  const double cminL = vL[Xn] - cL, cmaxL = vL[Xn] + cL;
-  const double cminR = vR[Xn] - cR, cmaxR = vR[Xn] + cR;
-  const double sl = fmin(cminL, cminR);
-  const double sr = fmax(cmaxL, cmaxR);
+  T* uL = r.uL;
+  T* uR = r.uR;
+  T fluxL[NV], fluxR[NV];
+  const T cL = fast_speed<D, DIR>(gamma, vL);
+  const T cR = fast_speed<D, DIR>(gamma, vR);
+  const T cminL = vL[Xn] - cL, cmaxL = vL[Xn] + cL;
+  const T cminR = vR[Xn] - cR, cmaxR = vR[Xn] + cR;
+  const T sl = fmin(cminL, cminR);
+  const T sr = fmax(cmaxL, cmaxR);
   r.sl = sl;
   r.sr = sr;
   r.cmax = fmax(fabs(sl), fabs(sr));
-  const double gm1 = gamma - 1.0;
+  const T gm1 = gamma - T(1);
   prim_to_cons<D>(gm1, uL, vL);
   prim_to_cons<D>(gm1, uR, vR);
   phys_flux<D, DIR>(fluxL, vL, uL);
   phys_flux<D, DIR>(fluxR, vR, uR);
-  const double ptL = vL[v::PRS] + half_b2<D>(vL);
-  const double ptR = vR[v::PRS] + half_b2<D>(vR);
-  double* F = r.F;
-  if (sl > 0) {
+  const T ptL = vL[v::PRS] + half_b2<D>(vL);
+  const T ptR = vR[v::PRS] + half_b2<D>(vR);
+  T* F = r.F;
+  if (sl > T(0)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxL[n];
     return;
   }
-  if (sr < 0) {
+  if (sr < T(0)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxR[n];
     return;
   }
-  double usL[NV], usR[NV];
-  double scrh, scrhL, scrhR;
-  double vsL = 0, vsR = 0, wsL = 0, wsR = 0;
+  T usL[NV], usR[NV];
+  T scrh, scrhL, scrhR;
+  T vsL = T(0), vsR = T(0), wsL = T(0), wsR = T(0);
   int revert_to_hllc = 0;
-  scrh = 1.0 / (sr - sl);
-  const double Bx = (sr * vR[BXn] - sl * vL[BXn]) * scrh;
-  const double sBx = (Bx > 0.0 ? 1.0 : -1.0);
-  const double duL = sl - vL[Xn];
-  const double duR = sr - vR[Xn];
-  scrh = 1.0 / (duR * uR[RHO] - duL * uL[RHO]);
-  const double SM = (duR * uR[Xn] - duL * uL[Xn] - ptR + ptL) * scrh;
-  double pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR + vL[RHO] * vR[RHO] * duR * duL * (vR[Xn] - vL[Xn]);
+  scrh = dv(T(1), sr - sl);
+  const T Bx = (sr * vR[BXn] - sl * vL[BXn]) * scrh;
+  const T sBx = (Bx > T(0) ? T(1) : T(-1));
+  const T duL = sl - vL[Xn];
+  const T duR = sr - vR[Xn];
+  scrh = dv(T(1), duR * uR[RHO] - duL * uL[RHO]);
+  const T SM = (duR * uR[Xn] - duL * uL[Xn] - ptR + ptL) * scrh;
+  T pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR + vL[RHO] * vR[RHO] * duR * duL * (vR[Xn] - vL[Xn]);
   pts *= scrh;
-  usL[RHO] = uL[RHO] * duL / (sl - SM);
-  usR[RHO] = uR[RHO] * duR / (sr - SM);
-  const double sqrL = sqrt(usL[RHO]);
-  const double sqrR = sqrt(usR[RHO]);
-  double S1L = SM - fabs(Bx) / sqrL;
-  double S1R = SM + fabs(Bx) / sqrR;
-  if ((S1L - sl) < 1.e-4 * (SM - sl)) revert_to_hllc = 1;
-  if ((S1R - sr) > -1.e-4 * (sr - SM)) revert_to_hllc = 1;
+  usL[RHO] = dv(uL[RHO] * duL, sl - SM);
+  usR[RHO] = dv(uR[RHO] * duR, sr - SM);
+  const T sqrL = sqrt(usL[RHO]);
+  const T sqrR = sqrt(usR[RHO]);
+  T S1L = SM - dv(fabs(Bx), sqrL);
+  T S1R = SM + dv(fabs(Bx), sqrR);
+  if ((S1L - sl) < T(1.e-4) * (SM - sl)) revert_to_hllc = 1;
+  if ((S1R - sr) > T(-1.e-4) * (sr - SM)) revert_to_hllc = 1;
   if (revert_to_hllc) {
-    scrh = 1.0 / (sr - sl);
-    double Uhll[NV];
+    scrh = dv(T(1), sr - sl);
+    T Uhll[NV];
 #pragma unroll
     for (int n = 0; n < NV; n++) {
       Uhll[n] = sr * uR[n] - sl * uL[n] + fluxL[n] - fluxR[n];
@@ -377,8 +401,8 @@ __device__ __forceinline__ void riemann_hlld(double gamma, const double* vL, con
     if constexpr (D == 3) usL[BXb] = usR[BXb] = Uhll[BXb];
     S1L = S1R = SM;
   } else {
-    scrhL = (uL[RHO] * duL * duL - Bx * Bx) / (uL[RHO] * duL * (sl - SM) - Bx * Bx);
-    scrhR = (uR[RHO] * duR * duR - Bx * Bx) / (uR[RHO] * duR * (sr - SM) - Bx * Bx);
+    scrhL = dv(uL[RHO] * duL * duL - Bx * Bx, uL[RHO] * duL * (sl - SM) - Bx * Bx);
+    scrhR = dv(uR[RHO] * duR * duR - Bx * Bx, uR[RHO] * duR * (sr - SM) - Bx * Bx);
     usL[BXn] = Bx;
     usL[BXt] = uL[BXt] * scrhL;
     if constexpr (D == 3) usL[BXb] = uL[BXb] * scrhL;
@@ -386,8 +410,8 @@ __device__ __forceinline__ void riemann_hlld(double gamma, const double* vL, con
     usR[BXt] = uR[BXt] * scrhR;
     if constexpr (D == 3) usR[BXb] = uR[BXb] * scrhR;
   }
-  scrhL = Bx / (uL[RHO] * duL);
-  scrhR = Bx / (uR[RHO] * duR);
+  scrhL = dv(Bx, uL[RHO] * duL);
+  scrhR = dv(Bx, uR[RHO] * duR);
   vsL = vL[Xt] - scrhL * (usL[BXt] - uL[BXt]);
   vsR = vR[Xt] - scrhR * (usR[BXt] - uR[BXt]);
   if constexpr (D == 3) {
@@ -403,42 +427,42 @@ __device__ __forceinline__ void riemann_hlld(double gamma, const double* vL, con
     usR[Xb] = usR[RHO] * wsR;
   }
   {
-    double a = vL[Xn] * Bx + vL[Xt] * uL[BXt];
+    T a = vL[Xn] * Bx + vL[Xt] * uL[BXt];
     if constexpr (D == 3) a = a + vL[Xb] * uL[BXb];
-    double b = SM * Bx + vsL * usL[BXt];
+    T b = SM * Bx + vsL * usL[BXt];
     if constexpr (D == 3) b = b + wsL * usL[BXb];
     scrhL = a;
     scrhL -= b;
   }
   usL[ENG] = duL * uL[ENG] - ptL * vL[Xn] + pts * SM + Bx * scrhL;
-  usL[ENG] /= sl - SM;
+  usL[ENG] = dv(usL[ENG], sl - SM);
   {
-    double a = vR[Xn] * Bx + vR[Xt] * uR[BXt];
+    T a = vR[Xn] * Bx + vR[Xt] * uR[BXt];
     if constexpr (D == 3) a = a + vR[Xb] * uR[BXb];
-    double b = SM * Bx + vsR * usR[BXt];
+    T b = SM * Bx + vsR * usR[BXt];
     if constexpr (D == 3) b = b + wsR * usR[BXb];
     scrhR = a;
     scrhR -= b;
   }
   usR[ENG] = duR * uR[ENG] - ptR * vR[Xn] + pts * SM + Bx * scrhR;
-  usR[ENG] /= sr - SM;
+  usR[ENG] = dv(usR[ENG], sr - SM);
 
-  if (S1L >= 0.0) {
+  if (S1L >= T(0)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxL[n] + sl * (usL[n] - uL[n]);
-  } else if (S1R <= 0.0) {
+  } else if (S1R <= T(0)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxR[n] + sr * (usR[n] - uR[n]);
   } else {
-    double vss = 0, wss = 0;
-    double ussl[NV], ussr[NV];
+    T vss = T(0), wss = T(0);
+    T ussl[NV], ussr[NV];
     ussl[RHO] = usL[RHO];
     ussr[RHO] = usR[RHO];
     vss = sqrL * vsL + sqrR * vsR + (usR[BXt] - usL[BXt]) * sBx;
-    vss /= sqrL + sqrR;
+    vss = dv(vss, sqrL + sqrR);
     if constexpr (D == 3) {
       wss = sqrL * wsL + sqrR * wsR + (usR[BXb] - usL[BXb]) * sBx;
-      wss /= sqrL + sqrR;
+      wss = dv(wss, sqrL + sqrR);
     }
     ussl[Xn] = ussl[RHO] * SM;
     ussr[Xn] = ussr[RHO] * SM;
@@ -450,17 +474,17 @@ __device__ __forceinline__ void riemann_hlld(double gamma, const double* vL, con
     }
     ussl[BXn] = ussr[BXn] = Bx;
     ussl[BXt] = sqrL * usR[BXt] + sqrR * usL[BXt] + sqrL * sqrR * (vsR - vsL) * sBx;
-    ussl[BXt] /= sqrL + sqrR;
+    ussl[BXt] = dv(ussl[BXt], sqrL + sqrR);
     ussr[BXt] = ussl[BXt];
     if constexpr (D == 3) {
       ussl[BXb] = sqrL * usR[BXb] + sqrR * usL[BXb] + sqrL * sqrR * (wsR - wsL) * sBx;
-      ussl[BXb] /= sqrL + sqrR;
+      ussl[BXb] = dv(ussl[BXb], sqrL + sqrR);
       ussr[BXb] = ussl[BXb];
     }
     {
-      double a = SM * Bx + vsL * usL[BXt];
+      T a = SM * Bx + vsL * usL[BXt];
       if constexpr (D == 3) a = a + wsL * usL[BXb];
-      double b = SM * Bx + vss * ussl[BXt];
+      T b = SM * Bx + vss * ussl[BXt];
       if constexpr (D == 3) b = b + wss * ussl[BXb];
       scrhL = a;
       scrhL -= b;
@@ -473,7 +497,7 @@ __device__ __forceinline__ void riemann_hlld(double gamma, const double* vL, con
     }
     ussl[ENG] = usL[ENG] - sqrL * scrhL * sBx;
     ussr[ENG] = usR[ENG] + sqrR * scrhR * sBx;
-    if (SM >= 0.0) {
+    if (SM >= T(0)) {
 #pragma unroll
       for (int n = 0; n < NV; n++) F[n] = fluxL[n] + S1L * (ussl[n] - usL[n]) + sl * (usL[n] - uL[n]);
     } else {
@@ -484,46 +508,45 @@ __device__ __forceinline__ void riemann_hlld(double gamma, const double* vL, con
 }
 
 // HLL (hllMHD.hpp:154-453; the Hall whistler term is not part of ideal MHD)
-template <int D, int DIR>
-__device__ __forceinline__ void riemann_hll(double gamma, const double* vL, const double* vR,
-                                            RiemannOut<D>& r) {
+template <int D, int DIR, typename T>
+__device__ __forceinline__ void riemann_hll(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
-  double* uL = r.uL;
-  double* uR = r.uR;
-  double fluxL[NV], fluxR[NV];
-  const double cL = fast_speed<D, DIR>(gamma, vL);
-  const double cR = fast_speed<D, DIR>(gamma, vR);
-  const double cminL = vL[d::Xn] - cL, cmaxL = vL[d::Xn] + cL;
-  const double cminR = vR[d::Xn] - cR, cmaxR = vR[d::Xn] + cR;
-  const double sl = fmin(cminL, cminR);
-  const double sr = fmax(cmaxL, cmaxR);
+  T* uL = r.uL;
+  T* uR = r.uR;
+  T fluxL[NV], fluxR[NV];
+  const T cL = fast_speed<D, DIR>(gamma, vL);
+  const T cR = fast_speed<D, DIR>(gamma, vR);
+  const T cminL = vL[d::Xn] - cL, cmaxL = vL[d::Xn] + cL;
+  const T cminR = vR[d::Xn] - cR, cmaxR = vR[d::Xn] + cR;
+  const T sl = fmin(cminL, cminR);
+  const T sr = fmax(cmaxL, cmaxR);
   r.sl = sl;
   r.sr = sr;
   r.cmax = fmax(fabs(sl), fabs(sr));
-  const double gm1 = gamma - 1.0;
+  const T gm1 = gamma - T(1);
   prim_to_cons<D>(gm1, uL, vL);
   prim_to_cons<D>(gm1, uR, vR);
   phys_flux<D, DIR>(fluxL, vL, uL);
   phys_flux<D, DIR>(fluxR, vR, uR);
-  double* F = r.F;
-  if (sl > 0) {
+  T* F = r.F;
+  if (sl > T(0)) {
 #pragma unroll
     for (int n = 0; n <= D; n++) F[n] = fluxL[n];
-  } else if (sr < 0) {
+  } else if (sr < T(0)) {
 #pragma unroll
     for (int n = 0; n <= D; n++) F[n] = fluxR[n];
   } else {
 #pragma unroll
     for (int n = 0; n <= D; n++)
-      F[n] = (sl * sr * uR[n] - sl * sr * uL[n] + sr * fluxL[n] - sl * fluxR[n]) / (sr - sl);
+      F[n] = dv(sl * sr * uR[n] - sl * sr * uL[n] + sr * fluxL[n] - sl * fluxR[n], sr - sl);
   }
-  if (sl > 0) {
+  if (sl > T(0)) {
 #pragma unroll
     for (int n = v::BX1; n < v::BX1 + D; n++) F[n] = fluxL[n];
     F[v::ENG] = fluxL[v::ENG];
-  } else if (sr < 0) {
+  } else if (sr < T(0)) {
 #pragma unroll
     for (int n = v::BX1; n < v::BX1 + D; n++) F[n] = fluxR[n];
     F[v::ENG] = fluxR[v::ENG];
@@ -531,48 +554,46 @@ __device__ __forceinline__ void riemann_hll(double gamma, const double* vL, cons
 #pragma unroll
     for (int n = v::BX1; n < v::BX1 + D; n++) {
       F[n] = sl * sr * uR[n] - sl * sr * uL[n] + sr * fluxL[n] - sl * fluxR[n];
-      F[n] *= (1.0 / (sr - sl));
+      F[n] *= dv(T(1), sr - sl);
     }
     F[v::ENG] = sl * sr * uR[v::ENG] - sl * sr * uL[v::ENG] + sr * fluxL[v::ENG] - sl * fluxR[v::ENG];
-    F[v::ENG] *= (1.0 / (sr - sl));
+    F[v::ENG] *= dv(T(1), sr - sl);
   }
 }
 
 // TVDLF / Rusanov (tvdlfMHD.hpp:140-232)
-template <int D, int DIR>
-__device__ __forceinline__ void riemann_tvdlf(double gamma, const double* vL, const double* vR,
-                                              RiemannOut<D>& r) {
+template <int D, int DIR, typename T>
+__device__ __forceinline__ void riemann_tvdlf(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
-  double vv[NV];
+  T vv[NV];
 #pragma unroll
-  for (int n = 0; n < NV; n++) vv[n] = 0.5 * (vL[n] + vR[n]);
-  const double gpr = gamma * vv[v::PRS];
-  double Bt2 = 0.0 + vv[d::BXt] * vv[d::BXt];
+  for (int n = 0; n < NV; n++) vv[n] = T(0.5) * (vL[n] + vR[n]);
+  const T gpr = gamma * vv[v::PRS];
+  T Bt2 = T(0) + vv[d::BXt] * vv[d::BXt];
   if constexpr (D == 3) Bt2 = Bt2 + vv[d::BXb] * vv[d::BXb];
-  const double B2 = Bt2 + vv[d::BXn] * vv[d::BXn];
-  double cRL = gpr - B2;
-  cRL = cRL + B2 + sqrt(cRL * cRL + 4.0 * gpr * Bt2);
-  cRL = sqrt(0.5 * cRL / vv[v::RHO]);
-  const double cmax = fmax(fabs(vv[d::Xn] + cRL), fabs(vv[d::Xn] - cRL));
+  const T B2 = Bt2 + vv[d::BXn] * vv[d::BXn];
+  T cRL = gpr - B2;
+  cRL = cRL + B2 + sqrt(cRL * cRL + T(4) * gpr * Bt2);
+  cRL = sqrt(dv(T(0.5) * cRL, vv[v::RHO]));
+  const T cmax = fmax(fabs(vv[d::Xn] + cRL), fabs(vv[d::Xn] - cRL));
   r.sl = -cmax;
   r.sr = cmax;
   r.cmax = cmax;
-  double fluxL[NV], fluxR[NV];
-  const double gm1 = gamma - 1.0;
+  T fluxL[NV], fluxR[NV];
+  const T gm1 = gamma - T(1);
   prim_to_cons<D>(gm1, r.uL, vL);
   prim_to_cons<D>(gm1, r.uR, vR);
   phys_flux<D, DIR>(fluxL, vL, r.uL);
   phys_flux<D, DIR>(fluxR, vR, r.uR);
 #pragma unroll
-  for (int n = 0; n < NV; n++) r.F[n] = 0.5 * (fluxL[n] + fluxR[n] + cmax * (r.uL[n] - r.uR[n]));
+  for (int n = 0; n < NV; n++) r.F[n] = T(0.5) * (fluxL[n] + fluxR[n] + cmax * (r.uL[n] - r.uR[n]));
 }
 
 // Roe with the entropy fix (roeMHD.hpp:175-650, energy equation branch)
-template <int D, int DIR>
-__device__ __forceinline__ void riemann_roe(double gamma, const double* vL, const double* vR,
-                                            RiemannOut<D>& r) {
+template <int D, int DIR, typename T>
+__device__ __forceinline__ void riemann_roe(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
@@ -580,14 +601,14 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
   constexpr int BXn = d::BXn, BXt = d::BXt, BXb = d::BXb;
   constexpr int KFASTM = 0, KFASTP = 1, KDIVB = 2, KENTRP = 3, KSLOWM = 4, KSLOWP = 5, KALFVM = 6,
                 KALFVP = 7;
-  const double delta = 1.e-6;
-  double dV[NV], dU[NV], fluxL[NV], fluxR[NV];
-  double Rc[NV][NV];
-  double* uL = r.uL;
-  double* uR = r.uR;
+  const T delta = T(1.e-6);
+  T dV[NV], dU[NV], fluxL[NV], fluxR[NV];
+  T Rc[NV][NV];
+  T* uL = r.uL;
+  T* uR = r.uR;
 #pragma unroll
   for (int n = 0; n < NV; n++) dV[n] = vR[n] - vL[n];
-  const double gm1 = gamma - 1.0;
+  const T gm1 = gamma - T(1);
   prim_to_cons<D>(gm1, uL, vL);
   prim_to_cons<D>(gm1, uR, vR);
 #pragma unroll
@@ -597,32 +618,32 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
 #pragma unroll
   for (int a = 0; a < NV; a++)
 #pragma unroll
-    for (int b = 0; b < NV; b++) Rc[a][b] = 0;
-  const double sqr_rho_L = sqrt(vL[RHO]);
-  const double sqr_rho_R = sqrt(vR[RHO]);
-  const double sl = sqr_rho_L / (sqr_rho_L + sqr_rho_R);
-  const double sr = sqr_rho_R / (sqr_rho_L + sqr_rho_R);
-  const double rho = sr * vL[RHO] + sl * vR[RHO];
-  const double sqrt_rho = sqrt(rho);
-  double w = 0, Bz = 0, bz = 0;
-  const double u = sl * vL[Xn] + sr * vR[Xn];
-  const double vv = sl * vL[Xt] + sr * vR[Xt];
+    for (int b = 0; b < NV; b++) Rc[a][b] = T(0);
+  const T sqr_rho_L = sqrt(vL[RHO]);
+  const T sqr_rho_R = sqrt(vR[RHO]);
+  const T sl = dv(sqr_rho_L, sqr_rho_L + sqr_rho_R);
+  const T sr = dv(sqr_rho_R, sqr_rho_L + sqr_rho_R);
+  const T rho = sr * vL[RHO] + sl * vR[RHO];
+  const T sqrt_rho = sqrt(rho);
+  T w = T(0), Bz = T(0), bz = T(0);
+  const T u = sl * vL[Xn] + sr * vR[Xn];
+  const T vv = sl * vL[Xt] + sr * vR[Xt];
   if constexpr (D == 3) w = sl * vL[Xb] + sr * vR[Xb];
-  const double Bx = sr * vL[BXn] + sl * vR[BXn];
-  const double By = sr * vL[BXt] + sl * vR[BXt];
+  const T Bx = sr * vL[BXn] + sl * vR[BXn];
+  const T By = sr * vL[BXt] + sl * vR[BXt];
   if constexpr (D == 3) Bz = sr * vL[BXb] + sl * vR[BXb];
-  const double sBx = (Bx >= 0.0 ? 1.0 : -1.0);
-  const double bx = Bx / sqrt_rho;
-  const double by = By / sqrt_rho;
-  if constexpr (D == 3) bz = Bz / sqrt_rho;
-  double bt2 = 0.0 + by * by;
+  const T sBx = (Bx >= T(0) ? T(1) : T(-1));
+  const T bx = dv(Bx, sqrt_rho);
+  const T by = dv(By, sqrt_rho);
+  if constexpr (D == 3) bz = dv(Bz, sqrt_rho);
+  T bt2 = T(0) + by * by;
   if constexpr (D == 3) bt2 = bt2 + bz * bz;
-  const double b2 = bx * bx + bt2;
-  const double Btmag = sqrt(bt2 * rho);
-  double X = dV[BXn] * dV[BXn] + dV[BXt] * dV[BXt];
+  const T b2 = bx * bx + bt2;
+  const T Btmag = sqrt(bt2 * rho);
+  T X = dV[BXn] * dV[BXn] + dV[BXt] * dV[BXt];
   if constexpr (D == 3) X = X + dV[BXb] * dV[BXb];
-  X /= (sqr_rho_L + sqr_rho_R) * (sqr_rho_L + sqr_rho_R) * 2.0;
-  double Bmag2L, Bmag2R, vdm, BdB, vel2;
+  X = dv(X, (sqr_rho_L + sqr_rho_R) * (sqr_rho_L + sqr_rho_R) * T(2));
+  T Bmag2L, Bmag2R, vdm, BdB, vel2;
   if constexpr (D == 3) {
     Bmag2L = sumsq<3>(vL[v::BX1], vL[v::BX2], vL[v::BX3]);
     Bmag2R = sumsq<3>(vR[v::BX1], vR[v::BX2], vR[v::BX3]);
@@ -630,69 +651,70 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
     BdB = Bx * dU[BXn] + By * dU[BXt] + Bz * dU[BXb];
     vel2 = u * u + vv * vv + w * w;
   } else {
-    Bmag2L = sumsq<2>(vL[v::BX1], vL[v::BX2], 0.0);
-    Bmag2R = sumsq<2>(vR[v::BX1], vR[v::BX2], 0.0);
+    Bmag2L = sumsq<2>(vL[v::BX1], vL[v::BX2], T(0));
+    Bmag2R = sumsq<2>(vR[v::BX1], vR[v::BX2], T(0));
     vdm = u * dU[Xn] + vv * dU[Xt];
     BdB = Bx * dU[BXn] + By * dU[BXt];
     vel2 = u * u + vv * vv;
   }
-  const double pL = vL[PRS] + 0.5 * Bmag2L;
-  const double pR = vR[PRS] + 0.5 * Bmag2R;
-  dV[PRS] = (gamma - 1.0) * ((0.5 * vel2 - X) * dV[RHO] - vdm + dU[ENG] - BdB);
-  const double HL = (uL[ENG] + pL) / vL[RHO];
-  const double HR = (uR[ENG] + pR) / vR[RHO];
-  const double H = sl * HL + sr * HR;
-  const double Hgas = H - b2;
-  const double a2 = (2.0 - gamma) * X + (gamma - 1.0) * (Hgas - 0.5 * vel2);
-  double scrh = a2 - b2;
-  const double ca2 = bx * bx;
-  scrh = scrh * scrh + 4.0 * bt2 * a2;
+  const T pL = vL[PRS] + T(0.5) * Bmag2L;
+  const T pR = vR[PRS] + T(0.5) * Bmag2R;
+  dV[PRS] = (gamma - T(1)) * ((T(0.5) * vel2 - X) * dV[RHO] - vdm + dU[ENG] - BdB);
+  const T HL = dv(uL[ENG] + pL, vL[RHO]);
+  const T HR = dv(uR[ENG] + pR, vR[RHO]);
+  const T H = sl * HL + sr * HR;
+  const T Hgas = H - b2;
+  const T a2 = (T(2) - gamma) * X + (gamma - T(1)) * (Hgas - T(0.5) * vel2);
+  T scrh = a2 - b2;
+  const T ca2 = bx * bx;
+  scrh = scrh * scrh + T(4) * bt2 * a2;
   scrh = sqrt(scrh);
-  const double cf2 = 0.5 * (a2 + b2 + scrh);
-  const double cs2 = a2 * ca2 / cf2;
-  const double cf = sqrt(cf2);
-  const double cs = sqrt(cs2);
-  const double ca = sqrt(ca2);
-  const double a = sqrt(a2);
-  double alpha_f, alpha_s;
+  const T cf2 = T(0.5) * (a2 + b2 + scrh);
+  const T cs2 = dv(a2 * ca2, cf2);
+  const T cf = sqrt(cf2);
+  const T cs = sqrt(cs2);
+  const T ca = sqrt(ca2);
+  const T a = sqrt(a2);
+  T alpha_f, alpha_s;
   if (cf == cs) {
-    alpha_f = 1.0;
-    alpha_s = 0.0;
+    alpha_f = T(1);
+    alpha_s = T(0);
   } else if (a <= cs) {
-    alpha_f = 0.0;
-    alpha_s = 1.0;
+    alpha_f = T(0);
+    alpha_s = T(1);
   } else if (cf <= a) {
-    alpha_f = 1.0;
-    alpha_s = 0.0;
+    alpha_f = T(1);
+    alpha_s = T(0);
   } else {
-    scrh = 1.0 / (cf2 - cs2);
+    scrh = dv(T(1), cf2 - cs2);
     alpha_f = (a2 - cs2) * scrh;
     alpha_s = (cf2 - a2) * scrh;
-    alpha_f = fmax(0.0, alpha_f);
-    alpha_s = fmax(0.0, alpha_s);
+    alpha_f = fmax(T(0), alpha_f);
+    alpha_s = fmax(T(0), alpha_s);
     alpha_f = sqrt(alpha_f);
     alpha_s = sqrt(alpha_s);
   }
-  double beta_y, beta_z = 0;
+  T beta_y, beta_z = T(0);
   if constexpr (D == 2) {
-    beta_y = (Btmag > 1.e-9) ? ((By) >= 0.0 ? (1.0) : (-1.0)) : 1.0;
+    beta_y = (Btmag > T(1.e-9)) ? ((By) >= T(0) ? T(1) : T(-1)) : T(1);
   } else {
-    if (Btmag > 1.e-9) {
-      beta_y = By / Btmag;
-      beta_z = Bz / Btmag;
+    if (Btmag > T(1.e-9)) {
+      beta_y = dv(By, Btmag);
+      beta_z = dv(Bz, Btmag);
     } else {
-      beta_z = beta_y = 1.0;
+      beta_z = beta_y = T(1);
     }
   }
-  double lambda[NV], alambda[NV], eta[NV];
-  double beta_dv = 0.0 + beta_y * dV[Xt];
-  double beta_dB = 0.0 + beta_y * dV[BXt];
-  double beta_v = 0.0 + beta_y * vv;
+  T lambda[NV], alambda[NV], eta[NV];
+  T beta_dv = T(0) + beta_y * dV[Xt];
+  T beta_dB = T(0) + beta_y * dV[BXt];
+  T beta_v = T(0) + beta_y * vv;
   if constexpr (D == 3) {
     beta_dv = beta_dv + beta_z * dV[Xb];
     beta_dB = beta_dB + beta_z * dV[BXb];
     beta_v = beta_v + beta_z * w;
   }
+  const T half_a2 = dv(T(0.5), a2);
   int kk = KFASTM;
   lambda[kk] = u - cf;
   scrh = alpha_s * cs * sBx;
@@ -700,12 +722,12 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
   Rc[Xn][kk] = alpha_f * lambda[kk];
   Rc[Xt][kk] = alpha_f * vv + scrh * beta_y;
   if constexpr (D == 3) Rc[Xb][kk] = alpha_f * w + scrh * beta_z;
-  Rc[BXt][kk] = alpha_s * a * beta_y / sqrt_rho;
-  if constexpr (D == 3) Rc[BXb][kk] = alpha_s * a * beta_z / sqrt_rho;
-  Rc[ENG][kk] = alpha_f * (Hgas - u * cf) + scrh * beta_v + alpha_s * a * Btmag / sqrt_rho;
+  Rc[BXt][kk] = dv(alpha_s * a * beta_y, sqrt_rho);
+  if constexpr (D == 3) Rc[BXb][kk] = dv(alpha_s * a * beta_z, sqrt_rho);
+  Rc[ENG][kk] = alpha_f * (Hgas - u * cf) + scrh * beta_v + dv(alpha_s * a * Btmag, sqrt_rho);
   eta[kk] = alpha_f * (X * dV[RHO] + dV[PRS]);
   eta[kk] += rho * scrh * beta_dv - rho * alpha_f * cf * dV[Xn] + sqrt_rho * alpha_s * a * beta_dB;
-  eta[kk] *= 0.5 / a2;
+  eta[kk] *= half_a2;
 
   kk = KFASTP;
   lambda[kk] = u + cf;
@@ -715,23 +737,23 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
   if constexpr (D == 3) Rc[Xb][kk] = alpha_f * w - scrh * beta_z;
   Rc[BXt][kk] = Rc[BXt][KFASTM];
   if constexpr (D == 3) Rc[BXb][kk] = Rc[BXb][KFASTM];
-  Rc[ENG][kk] = alpha_f * (Hgas + u * cf) - scrh * beta_v + alpha_s * a * Btmag / sqrt_rho;
+  Rc[ENG][kk] = alpha_f * (Hgas + u * cf) - scrh * beta_v + dv(alpha_s * a * Btmag, sqrt_rho);
   eta[kk] = alpha_f * (X * dV[RHO] + dV[PRS]) - rho * scrh * beta_dv + rho * alpha_f * cf * dV[Xn] +
             sqrt_rho * alpha_s * a * beta_dB;
-  eta[kk] *= 0.5 / a2;
+  eta[kk] *= half_a2;
 
   kk = KENTRP;
   lambda[kk] = u;
-  Rc[RHO][kk] = 1.0;
+  Rc[RHO][kk] = T(1);
   Rc[Xn][kk] = u;
   Rc[Xt][kk] = vv;
   if constexpr (D == 3) Rc[Xb][kk] = w;
-  Rc[ENG][kk] = 0.5 * vel2 + (gamma - 2.0) / (gamma - 1.0) * X;
-  eta[kk] = ((a2 - X) * dV[RHO] - dV[PRS]) / a2;
+  Rc[ENG][kk] = T(0.5) * vel2 + dv(gamma - T(2), gamma - T(1)) * X;
+  eta[kk] = dv((a2 - X) * dV[RHO] - dV[PRS], a2);
 
   kk = KDIVB;
   lambda[kk] = u;
-  eta[kk] = 0.0;
+  eta[kk] = T(0);
 
   scrh = alpha_f * cf * sBx;
   kk = KSLOWM;
@@ -740,12 +762,12 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
   Rc[Xn][kk] = alpha_s * lambda[kk];
   Rc[Xt][kk] = alpha_s * vv - scrh * beta_y;
   if constexpr (D == 3) Rc[Xb][kk] = alpha_s * w - scrh * beta_z;
-  Rc[BXt][kk] = -alpha_f * a * beta_y / sqrt_rho;
-  if constexpr (D == 3) Rc[BXb][kk] = -alpha_f * a * beta_z / sqrt_rho;
-  Rc[ENG][kk] = alpha_s * (Hgas - u * cs) - scrh * beta_v - alpha_f * a * Btmag / sqrt_rho;
+  Rc[BXt][kk] = dv(-alpha_f * a * beta_y, sqrt_rho);
+  if constexpr (D == 3) Rc[BXb][kk] = dv(-alpha_f * a * beta_z, sqrt_rho);
+  Rc[ENG][kk] = alpha_s * (Hgas - u * cs) - scrh * beta_v - dv(alpha_f * a * Btmag, sqrt_rho);
   eta[kk] = alpha_s * (X * dV[RHO] + dV[PRS]) - rho * scrh * beta_dv - rho * alpha_s * cs * dV[Xn] -
             sqrt_rho * alpha_f * a * beta_dB;
-  eta[kk] *= 0.5 / a2;
+  eta[kk] *= half_a2;
 
   kk = KSLOWP;
   lambda[kk] = u + cs;
@@ -755,10 +777,10 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
   if constexpr (D == 3) Rc[Xb][kk] = alpha_s * w + scrh * beta_z;
   Rc[BXt][kk] = Rc[BXt][KSLOWM];
   if constexpr (D == 3) Rc[BXb][kk] = Rc[BXb][KSLOWM];
-  Rc[ENG][kk] = alpha_s * (Hgas + u * cs) + scrh * beta_v - alpha_f * a * Btmag / sqrt_rho;
+  Rc[ENG][kk] = alpha_s * (Hgas + u * cs) + scrh * beta_v - dv(alpha_f * a * Btmag, sqrt_rho);
   eta[kk] = alpha_s * (X * dV[RHO] + dV[PRS]) + rho * scrh * beta_dv + rho * alpha_s * cs * dV[Xn] -
             sqrt_rho * alpha_f * a * beta_dB;
-  eta[kk] *= 0.5 / a2;
+  eta[kk] *= half_a2;
 
   if constexpr (D == 3) {
     kk = KALFVM;
@@ -768,8 +790,8 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
     Rc[BXt][kk] = -sBx * sqrt_rho * beta_z;
     Rc[BXb][kk] = sBx * sqrt_rho * beta_y;
     Rc[ENG][kk] = -rho * (vv * beta_z - w * beta_y);
-    eta[kk] = +beta_y * dV[Xb] - beta_z * dV[Xt] + sBx / sqrt_rho * (beta_y * dV[BXb] - beta_z * dV[BXt]);
-    eta[kk] *= 0.5;
+    eta[kk] = +beta_y * dV[Xb] - beta_z * dV[Xt] + dv(sBx, sqrt_rho) * (beta_y * dV[BXb] - beta_z * dV[BXt]);
+    eta[kk] *= T(0.5);
     kk = KALFVP;
     lambda[kk] = u + ca;
     Rc[Xt][kk] = -Rc[Xt][KALFVM];
@@ -777,30 +799,30 @@ __device__ __forceinline__ void riemann_roe(double gamma, const double* vL, cons
     Rc[BXt][kk] = Rc[BXt][KALFVM];
     Rc[BXb][kk] = Rc[BXb][KALFVM];
     Rc[ENG][kk] = -Rc[ENG][KALFVM];
-    eta[kk] = -beta_y * dV[Xb] + beta_z * dV[Xt] + sBx / sqrt_rho * (beta_y * dV[BXb] - beta_z * dV[BXt]);
-    eta[kk] *= 0.5;
+    eta[kk] = -beta_y * dV[Xb] + beta_z * dV[Xt] + dv(sBx, sqrt_rho) * (beta_y * dV[BXb] - beta_z * dV[BXt]);
+    eta[kk] *= T(0.5);
   }
   r.cmax = fabs(u) + cf;
   r.sl = lambda[KFASTM];
   r.sr = lambda[KFASTP];
 #pragma unroll
   for (int n = 0; n < NV; n++) alambda[n] = fabs(lambda[n]);
-  if (alambda[KFASTM] < 0.5 * delta) alambda[KFASTM] = lambda[KFASTM] * lambda[KFASTM] / delta + 0.25 * delta;
-  if (alambda[KFASTP] < 0.5 * delta) alambda[KFASTP] = lambda[KFASTP] * lambda[KFASTP] / delta + 0.25 * delta;
-  if (alambda[KSLOWM] < 0.5 * delta) alambda[KSLOWM] = lambda[KSLOWM] * lambda[KSLOWM] / delta + 0.25 * delta;
-  if (alambda[KSLOWP] < 0.5 * delta) alambda[KSLOWP] = lambda[KSLOWP] * lambda[KSLOWP] / delta + 0.25 * delta;
+  const T hd = T(0.5) * delta, qd = T(0.25) * delta;
+  if (alambda[KFASTM] < hd) alambda[KFASTM] = dv(lambda[KFASTM] * lambda[KFASTM], delta) + qd;
+  if (alambda[KFASTP] < hd) alambda[KFASTP] = dv(lambda[KFASTP] * lambda[KFASTP], delta) + qd;
+  if (alambda[KSLOWM] < hd) alambda[KSLOWM] = dv(lambda[KSLOWM] * lambda[KSLOWM], delta) + qd;
+  if (alambda[KSLOWP] < hd) alambda[KSLOWP] = dv(lambda[KSLOWP] * lambda[KSLOWP], delta) + qd;
 #pragma unroll
   for (int n1 = 0; n1 < NV; n1++) {
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
     for (int n2 = 0; n2 < NV; n2++) s += alambda[n2] * eta[n2] * Rc[n1][n2];
-    r.F[n1] = 0.5 * (fluxL[n1] + fluxR[n1] - s);
+    r.F[n1] = T(0.5) * (fluxL[n1] + fluxR[n1] - s);
   }
 }
 
-template <int D, int DIR, int SOLVER>
-__device__ __forceinline__ void riemann(double gamma, const double* vL, const double* vR,
-                                        RiemannOut<D>& r) {
+template <int D, int DIR, int SOLVER, typename T>
+__device__ __forceinline__ void riemann(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   if constexpr (SOLVER == kHLLD) riemann_hlld<D, DIR>(gamma, vL, vR, r);
   if constexpr (SOLVER == kHLL) riemann_hll<D, DIR>(gamma, vL, vR, r);
   if constexpr (SOLVER == kROE) riemann_roe<D, DIR>(gamma, vL, vR, r);

@@ -161,6 +161,36 @@ def turbulence_3d(n=256, seed=1, nghost=2, gamma=5.0 / 3.0, mach=1.0, b0=0.1, be
     return Vc, Vs
 
 
+def low_beta_3d(n=384, seed=1, nghost=2, gamma=5.0 / 3.0, beta=1e-3, mach=0.3, drho=0.1,
+                kmin=1, kmax=4):
+    """Low-beta precision workload: rho = 1 + drho G (G a seeded Gaussian
+    field, k^-2 on kmin <= |k| <= kmax, unit rms), uniform Bz = 1, pressure
+    from beta (p = beta B^2 / 2), velocity a Gaussian field of the same
+    spectrum at rms Mach ``mach`` (sound speed of the mean state)."""
+    dims = 3
+    nvar, nt, ntv = grid_shapes(dims, (n, n, n), nghost)
+    rng = np.random.default_rng(seed)
+    shape = (n, n, n)
+    G = _gaussian_field(rng, shape, kmin, kmax)
+    rho = 1.0 + drho * G
+    p0 = beta * 0.5
+    cs = math.sqrt(gamma * p0 / 1.0)
+    v = [_gaussian_field(rng, shape, kmin, kmax) for _ in range(3)]
+    vrms = math.sqrt(sum(np.mean(c**2) for c in v))
+    v = [c * (mach * cs / vrms) for c in v]
+    Vc = np.zeros((nvar, nt[2], nt[1], nt[0]))
+    g = nghost
+    act = (slice(g, g + n),) * 3
+    Vc[0][act] = rho
+    Vc[1][act], Vc[2][act], Vc[3][act] = v
+    Vc[4][act] = p0
+    for q in range(5):
+        _fill_periodic_cells(Vc[q], dims, g)
+    zero = np.zeros(shape)
+    Vs = _faces_to_Vs((zero, zero, zero + 1.0), g, ntv)
+    return Vc, Vs
+
+
 def uniform_random_3d(n=16, seed=0, nghost=2, gamma=5.0 / 3.0):
     """small seeded 3-D state for parity tests (turbulence spectrum, kmax=4)"""
     return turbulence_3d(n=n, seed=seed, nghost=nghost, gamma=gamma, kmax=min(4, n // 2))

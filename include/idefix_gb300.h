@@ -51,8 +51,11 @@ enum {
   IDFX_EMF_UCT_HLL = 3,
   IDFX_EMF_UCT_HLLD = 4
 };
-/* arithmetic of the reconstruction and Riemann solve */
-enum { IDFX_FP64 = 0 };
+/* arithmetic of the reconstruction and Riemann solve: IDFX_FP64 is the
+ * bit-exact path; IDFX_MIXED runs reconstruction and Riemann solver in FP32
+ * while the conserved-state accumulation across stages, ConsToPrim and the
+ * CT face-field update stay FP64 */
+enum { IDFX_FP64 = 0, IDFX_MIXED = 1 };
 
 typedef struct {
   int dims;                 /* 2 or 3 (DIMENSIONS, with COMPONENTS == DIMENSIONS) */
@@ -69,7 +72,7 @@ typedef struct {
   double maxdivb;           /* [TimeIntegrator] maxdivB (default 1e-6)            */
   int log_period;           /* [Output] log: divB check period, 0 = off           */
   int check_nan_period;     /* [TimeIntegrator] check_nan, 0 = off                */
-  int precision;            /* IDFX_FP64                                          */
+  int precision;            /* IDFX_FP64 or IDFX_MIXED                            */
 } idfx_gpu_config;
 
 typedef struct idfx_gpu idfx_gpu;

@@ -1,0 +1,68 @@
+"""Mixed-precision path (FP32 reconstruction + Riemann solve, FP64 conserved
+state, ConsToPrim and CT face update) against the bit-exact FP64 path.
+
+The precision workload of the north-star (low beta = 1e-3, HLLD + LimO3 +
+CT) at reduced size: per-variable L1-relative and Linf errors of the mixed
+run against the FP64 run, and div B, which the FP64 face update keeps at
+round-off whatever the precision of the EMFs.
+"""
+import numpy as np
+import pytest
+
+import idefix_gb300 as ig
+from idefix_gb300 import ic
+from mhd_state import extract
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(precision, Vc, Vs, n, cycles, **kw):
+    blk = ig.GpuBlock(3, n, precision=precision, **kw)
+    blk.upload(Vc, Vs)
+    blk.run(max_cycles=cycles)
+    out = extract(3, n, blk.ng, *blk.download())
+    divb = blk.check_divb()
+    tm = blk.get_time()
+    blk.close()
+    return out, divb, tm
+
+
+def _errors(a, b):
+    vc_a, vc_b = a[0], b[0]
+    rows = {}
+    for q, name in enumerate(["RHO", "VX1", "VX2", "VX3", "PRS"]):
+        d = np.abs(vc_a[q] - vc_b[q])
+        rows[name] = (float(d.sum() / np.abs(vc_b[q]).sum()), float(d.max()))
+    for c in range(3):
+        d = np.abs(a[1][c] - b[1][c])
+        rows[f"BX{c + 1}s"] = (float(d.sum() / max(np.abs(b[1][c]).sum(), 1e-300)), float(d.max()))
+    return rows
+
+
+def test_mixed_low_beta_limo3_against_fp64():
+    n = (64, 64, 64)
+    Vc, Vs = ic.low_beta_3d(64, seed=3)
+    kw = dict(order="limo3", solver="hlld", emf="uct_contact", cfl=0.6, first_dt=1e-4)
+    fp64, divb64, t64 = _run("fp64", Vc, Vs, n, 40, **kw)
+    mixed, divbm, tm = _run("mixed", Vc, Vs, n, 40, **kw)
+    err = _errors(mixed, fp64)
+    # the FP32 arithmetic is really used ...
+    assert not np.array_equal(mixed[0], fp64[0])
+    # ... and stays close to FP64 on the state (relative L1 per variable)
+    assert err["RHO"][0] < 1e-5, err
+    assert err["PRS"][0] < 1e-3, err
+    assert err["BX1s"][0] < 1e-3 and err["BX3s"][0] < 1e-6, err
+    assert divbm < 1e-10 and divb64 < 1e-10, (divbm, divb64)
+    assert abs(tm[0] - t64[0]) < 1e-6 * t64[0]
+
+
+@pytest.mark.parametrize("solver,order", [("hlld", "plm"), ("roe", "ppm"), ("hll", "order1")])
+def test_mixed_turbulence_matches_fp64_closely(solver, order):
+    n = (48, 48, 48)
+    Vc, Vs = ic.turbulence_3d(48, seed=9)
+    kw = dict(order=order, solver=solver, emf="uct_contact", cfl=0.6, first_dt=1e-4)
+    fp64, _, _ = _run("fp64", Vc, Vs, n, 20, **kw)
+    mixed, divbm, _ = _run("mixed", Vc, Vs, n, 20, **kw)
+    err = _errors(mixed, fp64)
+    assert err["RHO"][0] < 1e-5 and err["PRS"][0] < 1e-5, err
+    assert divbm < 1e-10
