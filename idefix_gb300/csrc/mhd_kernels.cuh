@@ -86,10 +86,10 @@ __device__ __forceinline__ void atomic_max_pos(unsigned long long* p, double v) 
 // One thread per location of the padded face box of one component.
 // ---------------------------------------------------------------------------
 template <int D>
-__global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
+__device__ __forceinline__ void d_fill_faces(const Geo& g, const Fields& f, const Ctl* ctl, int save_begin, dim3 bid) {
   if (ctl->done) return;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int comp = blockIdx.y;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
+  const int comp = bid.y;
   if (tid >= g.nface) return;
   int i = (int)(tid % g.ntv[0]);
   long long r = tid / g.ntv[0];
@@ -116,6 +116,11 @@ __global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
   }
 }
 
+template <int D>
+__global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
+  d_fill_faces<D>(g, f, ctl, save_begin, blockIdx);
+}
+
 // ---------------------------------------------------------------------------
 // Stage begin: ghost cells of Vc (periodic image), cell-centred field from
 // the faces (ReconstructVcField, boundary.hpp:388-404), conservative state of
@@ -125,11 +130,11 @@ __global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
 enum { kSbCons = 1, kSbSaveBegin = 2, kSbCellEmf = 4 };
 
 template <int D>
-__global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
+__device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, const Ctl* ctl, int flags, dim3 bid) {
   if (ctl->done) return;
   using v = Var<D>;
   constexpr int NV = v::NV;
-  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long c = (long long)bid.x * blockDim.x + threadIdx.x;
   if (c >= g.ncell) return;
   int i = (int)(c % g.nt[0]);
   long long r = c / g.nt[0];
@@ -180,6 +185,11 @@ __global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
     }
     f.Ex3[c] = (vx2 * Bx1 - vx1 * Bx2);
   }
+}
+
+template <int D>
+__global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
+  d_stage_begin<D>(g, f, ctl, flags, blockIdx);
 }
 
 // ---------------------------------------------------------------------------
@@ -301,8 +311,8 @@ constexpr int kTM = 64;
 // FP64 and converted once per cell; the flux difference, the conserved
 // update and InvDt are FP64 in both.
 template <int D, int DIR, int ORDER, int SOLVER, typename T>
-__global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl* ctl, int invdt,
-                                                     int last_dir, int seg) {
+__device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, const Ctl* ctl, int invdt,
+                                              int last_dir, int seg, dim3 bid) {
   if (ctl->done) return;
   using v = Var<D>;
   using dd = Dir<D, DIR>;
@@ -311,10 +321,18 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
   constexpr int W = 2 * H + 1;
   constexpr int A = (DIR == 0) ? 1 : 0;
   constexpr int B = (DIR == 2) ? 1 : 2;
-  const int ca = g.beg[A] - g.ext + blockIdx.x * kTM + threadIdx.x;
-  if (ca >= g.end[A] + g.ext) return;
-  const int cb = (D == 3) ? g.beg[B] - g.ext + (int)blockIdx.z : 0;
-  const int m0 = g.beg[DIR] + blockIdx.y * seg;
+  // FP32 sweeps are load-latency bound: issue the next step's loads before
+  // the current step's arithmetic.  FP64 sweeps are FP64-issue bound and
+  // keep their registers for the arithmetic.
+  constexpr bool PF = (sizeof(T) == 4);
+  // flattened column index over the (A, B) plane, CT extension included
+  const int nA = g.n[A] + 2 * g.ext;
+  const int nB = (D == 3) ? g.n[B] + 2 * g.ext : 1;
+  const long long col = (long long)bid.x * kTM + threadIdx.x;
+  if (col >= (long long)nA * nB) return;
+  const int ca = g.beg[A] - g.ext + (int)(col % nA);
+  const int cb = (D == 3) ? g.beg[B] - g.ext + (int)(col / nA) : 0;
+  const int m0 = g.beg[DIR] + bid.y * seg;
   const int m1 = min(m0 + seg, g.end[DIR]);
   bool active_col = (ca >= g.beg[A] && ca < g.end[A]);
   if constexpr (D == 3) active_col = active_col && cb >= g.beg[B] && cb < g.end[B];
@@ -333,23 +351,50 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
   T vrp[NV];            // right-face state of the previous cell
   double Fp[v::BX1];    // flux x A of the previous face
   double cp = 0.0;      // cmax of the previous face
+  double nx[NV];        // prefetched stencil value of the next step
+  double nbn = 0.0;     // prefetched normal face field of the next face
+  double nU[v::BX1];    // prefetched conserved state of the next cell to update
+  double nI = 0.0;      // prefetched InvDt of that cell
   // prime the window with cells m0-1-H .. m0-2+H
 #pragma unroll
   for (int n = 0; n < NV; n++) {
     if (n == dd::BXn) continue;
 #pragma unroll
     for (int m = 0; m < W - 1; m++) w[n][m + 1] = (T)f.Vc[n * g.ncell + c0 + (m - 1 - H) * sd];
+    if constexpr (PF) nx[n] = f.Vc[n * g.ncell + c0 + (H - 1) * sd];
   }
+  if constexpr (PF) nbn = vs[f0];
   const double dtdV = ctl->dtdV;
   for (int c = m0 - 1; c <= m1; c++) {
     const long long cc = c0 + (long long)(c - m0) * sd;
+    const bool more = c < m1;
+    double curU[v::BX1];
+    double curI = 0.0;
+    if constexpr (PF) {
+      // conserved state (and InvDt) of cell c-1, loaded one step ago
+      if (active_col && c > m0) {
+#pragma unroll
+        for (int n = 0; n < v::BX1; n++) curU[n] = nU[n];
+        curI = nI;
+      }
+      if (active_col && c >= m0 && more) {
+#pragma unroll
+        for (int n = 0; n < v::BX1; n++) nU[n] = f.Uc[n * g.ncell + cc];
+        if (invdt == 2) nI = f.InvDt[cc];
+      }
+    }
     T vl[NV], vr[NV];
 #pragma unroll
     for (int n = 0; n < NV; n++) {
       if (n == dd::BXn) continue;
 #pragma unroll
       for (int m = 0; m < W - 1; m++) w[n][m] = w[n][m + 1];
-      w[n][W - 1] = (T)f.Vc[n * g.ncell + cc + H * sd];
+      if constexpr (PF) {
+        w[n][W - 1] = (T)nx[n];
+        if (more) nx[n] = f.Vc[n * g.ncell + cc + (H + 1) * sd];
+      } else {
+        w[n][W - 1] = (T)f.Vc[n * g.ncell + cc + H * sd];
+      }
       Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n]);
     }
     if (c >= m0) {
@@ -360,7 +405,13 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
         vL[n] = vrp[n];
         vR[n] = vl[n];
       }
-      const T bn = (T)vs[f0 + (long long)(c - m0) * fsd];
+      T bn;
+      if constexpr (PF) {
+        bn = (T)nbn;
+        if (more) nbn = vs[f0 + (long long)(c + 1 - m0) * fsd];
+      } else {
+        bn = (T)vs[f0 + (long long)(c - m0) * fsd];
+      }
       vL[dd::BXn] = bn;
       vR[dd::BXn] = bn;
       RiemannOut<D, T> r;
@@ -375,10 +426,11 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
 #pragma unroll
           for (int n = 0; n < v::BX1; n++) {
             const double rhs = -dtdV * (FA[n] - Fp[n]);
-            f.Uc[n * g.ncell + cu] = f.Uc[n * g.ncell + cu] + rhs;
+            const double u = PF ? curU[n] : f.Uc[n * g.ncell + cu];
+            f.Uc[n * g.ncell + cu] = u + rhs;
           }
           if (invdt) {
-            const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
+            const double prev = (invdt == 1) ? 0.0 : (PF ? curI : f.InvDt[cu]);
             const double inv = prev + 0.5 * ((double)r.cmax + cp) / (g.dx[DIR]);
             f.InvDt[cu] = inv;
             if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
@@ -392,6 +444,11 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
 #pragma unroll
     for (int n = 0; n < NV; n++) vrp[n] = vr[n];
   }
+}
+
+template <int D, int DIR, int ORDER, int SOLVER, typename T>
+__global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl* ctl, int invdt, int last_dir, int seg) {
+  d_sweep_march<D, DIR, ORDER, SOLVER, T>(g, f, ctl, invdt, last_dir, seg, blockIdx);
 }
 
 // ---------------------------------------------------------------------------
@@ -429,10 +486,10 @@ __device__ __forceinline__ double riemann_edge(int order, const double* q, long 
 }
 
 template <int D>
-__global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
+__device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const Ctl* ctl, dim3 bid) {
   if (ctl->done) return;
   const int nx = g.n[0] + 1, ny = g.n[1] + 1;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)nx * ny * (D == 3 ? g.n[2] + 1 : 1);
   if (tid >= tot) return;
   const int i = g.beg[0] + (int)(tid % nx);
@@ -524,16 +581,21 @@ __global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
   }
 }
 
+template <int D>
+__global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
+  d_ct_corner<D>(g, f, ctl, blockIdx);
+}
+
 // ---------------------------------------------------------------------------
 // Face-field update Vs += dt curl E (evolveMagField.hpp:53-132, Cartesian),
 // then the Runge-Kutta combination of the faces (AddAndStore).  Only faces
 // that the next boundary pass does not overwrite are touched.
 // ---------------------------------------------------------------------------
 template <int D>
-__global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
+__device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc, double w0, dim3 bid) {
   if (ctl->done) return;
   const int nx = g.n[0] + 1, ny = g.n[1] + 1;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)nx * ny * (D == 3 ? g.n[2] + 1 : 1);
   if (tid >= tot) return;
   const int i = g.beg[0] + (int)(tid % nx);
@@ -584,17 +646,22 @@ __global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double 
   }
 }
 
+template <int D>
+__global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
+  d_ct_faces<D>(g, f, ctl, combine, wc, w0, blockIdx);
+}
+
 // ---------------------------------------------------------------------------
 // Stage end over the active cells: RK combination of Uc (AddAndStore),
 // cell-centred field from the faces (ReconstructVcField on Uc), and
 // ConvertConsToPrim.  Writes Uc and Vc.
 // ---------------------------------------------------------------------------
 template <int D>
-__global__ void k_stage_end(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
+__device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc, double w0, dim3 bid) {
   if (ctl->done) return;
   using v = Var<D>;
   constexpr int NV = v::NV;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)g.n[0] * g.n[1] * (D == 3 ? g.n[2] : 1);
   if (tid >= tot) return;
   const int i = g.beg[0] + (int)(tid % g.n[0]);
@@ -623,13 +690,18 @@ __global__ void k_stage_end(Geo g, Fields f, const Ctl* ctl, int combine, double
   }
 }
 
+template <int D>
+__global__ void k_stage_end(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
+  d_stage_end<D>(g, f, ctl, combine, wc, w0, blockIdx);
+}
+
 // ---------------------------------------------------------------------------
 // Diagnostics: divB estimator (checkDivB.hpp:14-68) and NaN count
 // (checkNan.hpp:17-45), as device reductions.
 // ---------------------------------------------------------------------------
 template <int D>
-__global__ void k_divb(Geo g, Fields f, Ctl* ctl) {
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void d_divb(const Geo& g, const Fields& f, Ctl* ctl, dim3 bid) {
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)g.n[0] * g.n[1] * (D == 3 ? g.n[2] : 1);
   if (tid >= tot) return;
   const int i = g.beg[0] + (int)(tid % g.n[0]);
@@ -662,9 +734,14 @@ __global__ void k_divb(Geo g, Fields f, Ctl* ctl) {
 }
 
 template <int D>
-__global__ void k_nan_count(Geo g, Fields f, Ctl* ctl) {
+__global__ void k_divb(Geo g, Fields f, Ctl* ctl) {
+  d_divb<D>(g, f, ctl, blockIdx);
+}
+
+template <int D>
+__device__ __forceinline__ void d_nan_count(const Geo& g, const Fields& f, Ctl* ctl, dim3 bid) {
   using v = Var<D>;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
   const int nx = g.n[0] + 1, ny = g.n[1] + 1;
   const long long tot = (long long)nx * ny * (D == 3 ? g.n[2] + 1 : 1);
   if (tid >= tot) return;
@@ -683,11 +760,16 @@ __global__ void k_nan_count(Geo g, Fields f, Ctl* ctl) {
   if (n) atomicAdd(&ctl->nan_count, n);
 }
 
+template <int D>
+__global__ void k_nan_count(Geo g, Fields f, Ctl* ctl) {
+  d_nan_count<D>(g, f, ctl, blockIdx);
+}
+
 // ---------------------------------------------------------------------------
 // Time-integrator control (timeIntegrator.cpp:246-414, main.cpp:190-225),
 // single thread.
 // ---------------------------------------------------------------------------
-static __global__ void k_cycle_begin(Geo g, Ctl* ctl, int use_tstop) {
+__device__ __forceinline__ void d_cycle_begin(const Geo& g, Ctl* ctl, int use_tstop) {
   if (ctl->done) return;
   if (use_tstop) {
     if (!(ctl->t < ctl->tstop)) {
@@ -705,7 +787,7 @@ static __global__ void k_cycle_begin(Geo g, Ctl* ctl, int use_tstop) {
   ctl->invdt_max_bits = 0ull;
 }
 
-static __global__ void k_cycle_end(Ctl* ctl) {
+__device__ __forceinline__ void d_cycle_end(Ctl* ctl) {
   if (ctl->done) return;
   const double invmax = __longlong_as_double((long long)ctl->invdt_max_bits);
   const double dtmin = 1.0 / invmax;  // = min over cells of 1/InvDt (division is monotone)
@@ -729,7 +811,7 @@ static __global__ void k_cycle_end(Ctl* ctl) {
   ctl->ncycles++;
 }
 
-static __global__ void k_check_divb(Ctl* ctl) {
+__device__ __forceinline__ void d_check_divb(Ctl* ctl) {
   if (ctl->done) return;
   const double v = __longlong_as_double((long long)ctl->divb_bits);
   if (v > ctl->maxdivb) {
@@ -738,12 +820,17 @@ static __global__ void k_check_divb(Ctl* ctl) {
   }
 }
 
-static __global__ void k_check_nan(Ctl* ctl) {
+__device__ __forceinline__ void d_check_nan(Ctl* ctl) {
   if (ctl->done) return;
   if (ctl->nan_count > 0) {
     ctl->status = kErrNan;
     ctl->done = 1;
   }
 }
+
+static __global__ void k_cycle_begin(Geo g, Ctl* ctl, int use_tstop) { d_cycle_begin(g, ctl, use_tstop); }
+static __global__ void k_cycle_end(Ctl* ctl) { d_cycle_end(ctl); }
+static __global__ void k_check_divb(Ctl* ctl) { d_check_divb(ctl); }
+static __global__ void k_check_nan(Ctl* ctl) { d_check_nan(ctl); }
 
 }  // namespace idfx

@@ -11,7 +11,8 @@ void launch_dir(Engine& e, int invdt, int last) {
   constexpr int A = (DIR == 0) ? 1 : 0;
   constexpr int B = (DIR == 2) ? 1 : 2;
   const int nseg = (g.n[DIR] + e.seg[DIR] - 1) / e.seg[DIR];
-  dim3 grid((g.n[A] + 2 * g.ext + kTM - 1) / kTM, nseg, D == 3 ? g.n[B] + 2 * g.ext : 1);
+  const long long cols = (long long)(g.n[A] + 2 * g.ext) * (D == 3 ? g.n[B] + 2 * g.ext : 1);
+  dim3 grid((unsigned)((cols + kTM - 1) / kTM), nseg, 1);
   mark_begin(e, kKSweepX + DIR);
   k_sweep_march<D, DIR, ORDER, SOLVER, T><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt, last, e.seg[DIR]);
   mark_end(e);
