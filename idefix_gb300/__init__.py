@@ -28,7 +28,7 @@ __all__ = ["GpuBlock", "Fluid", "TimeIntegrator", "IdefixError", "load_library",
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libidefix_gb300.so")
 
-ORDER = {"order1": 1, "plm": 2, "limo3": 3, "ppm": 4}
+ORDER = {"order1": 1, "plm": 2, "limo3": 3, "ppm": 4, "learned": 5}
 SOLVER = {"hlld": 0, "hll": 1, "roe": 2, "tvdlf": 3}
 EMF = {"uct_contact": 0, "arithmetic": 1, "uct0": 2, "uct_hll": 3, "uct_hlld": 4}
 PRECISION = {"fp64": 0, "mixed": 1}
@@ -70,10 +70,18 @@ EXPORTS = [
     "idfx_gpu_evolve_stage", "idfx_gpu_compute_timestep", "idfx_gpu_check_divb",
     "idfx_gpu_check_nan", "idfx_gpu_profile", "idfx_gpu_profile_read",
     "idfx_evolve_stage_noalloc",
+    "idfx_ens_create", "idfx_ens_destroy", "idfx_ens_last_error", "idfx_ens_sizes",
+    "idfx_ens_upload_prim", "idfx_ens_download_prim", "idfx_ens_get_time", "idfx_ens_run",
+    "idfx_ens_autotune", "idfx_ens_get_segments", "idfx_ens_set_schedule",
+    "idfx_ens_download_prim_device",
+    "idfx_gpu_set_learned", "idfx_gpu_learned_states", "idfx_gpu_learned_stats", "idfx_mlp_create", "idfx_mlp_destroy",
+    "idfx_mlp_set_params", "idfx_mlp_get_params", "idfx_mlp_set_dataset_device", "idfx_mlp_train",
+    "idfx_mlp_eval", "idfx_mlp_feature_range", "idfx_mlp_batch_device", "idfx_mlp_grad_device",
+    "idfx_mlp_forward_device", "idfx_learn_coarsen_device",
 ]
 
 KERNEL_CLASSES = ["fill_faces", "stage_begin", "sweep_x", "sweep_y", "sweep_z", "ct_corner",
-                  "ct_faces", "stage_end", "control", "checks"]
+                  "ct_faces", "stage_end", "control", "checks", "learned_recon"]
 
 _lib = None
 
@@ -114,11 +122,64 @@ def load_library(path=LIB_PATH):
     lib.idfx_gpu_profile_read.argtypes = [P, dp, ctypes.POINTER(LL), I]
     lib.idfx_evolve_stage_noalloc.argtypes = [ctypes.POINTER(Config), P, P, P, D, D, P,
                                               ctypes.c_char_p, ctypes.c_size_t]
+    lib.idfx_ens_create.argtypes = [I, ctypes.POINTER(Config), P, ctypes.POINTER(P)]
+    lib.idfx_ens_destroy.argtypes = [P]
+    lib.idfx_ens_last_error.argtypes = [P, ctypes.c_char_p, ctypes.c_size_t]
+    lib.idfx_ens_sizes.argtypes = [P, I, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(LL),
+                                   ctypes.POINTER(LL)]
+    lib.idfx_ens_upload_prim.argtypes = [P, I, P, P]
+    lib.idfx_ens_download_prim.argtypes = [P, I, P, P]
+    lib.idfx_ens_get_time.argtypes = [P, I, dp, dp, ctypes.POINTER(LL), ctypes.POINTER(I)]
+    lib.idfx_ens_run.argtypes = [P, D, LL, I]
+    lib.idfx_ens_autotune.argtypes = [P, I]
+    lib.idfx_ens_get_segments.argtypes = [P, I, ctypes.POINTER(I)]
+    lib.idfx_ens_set_schedule.argtypes = [P, I]
+    lib.idfx_ens_download_prim_device.argtypes = [P, I, P, P]
+    fp = ctypes.POINTER(ctypes.c_float)
+    U64 = ctypes.c_ulonglong
+    lib.idfx_gpu_set_learned.argtypes = [P, fp, fp, fp]
+    lib.idfx_gpu_learned_states.argtypes = [P, P]
+    lib.idfx_gpu_learned_stats.argtypes = [P, ctypes.POINTER(LL), ctypes.POINTER(LL)]
+    lib.idfx_mlp_create.argtypes = [I, P, ctypes.POINTER(P)]
+    lib.idfx_mlp_destroy.argtypes = [P]
+    lib.idfx_mlp_set_params.argtypes = [P, fp]
+    lib.idfx_mlp_get_params.argtypes = [P, fp]
+    lib.idfx_mlp_set_dataset_device.argtypes = [P, P, P, I, I, D]
+    lib.idfx_mlp_train.argtypes = [P, I, I, ctypes.c_float, ctypes.c_float, U64, fp]
+    lib.idfx_mlp_eval.argtypes = [P, I, U64, dp, dp]
+    lib.idfx_mlp_feature_range.argtypes = [P, fp, fp]
+    lib.idfx_mlp_batch_device.argtypes = [P, I, U64, LL, P, P]
+    lib.idfx_mlp_grad_device.argtypes = [P, P, P, I, fp, dp]
+    lib.idfx_mlp_forward_device.argtypes = [P, P, I, P]
+    lib.idfx_learn_coarsen_device.argtypes = [P, P, I, I, I, D, P, P, P, P]
     for f in EXPORTS:
         if f != "idfx_gpu_default_config":
             getattr(lib, f).restype = I
     _lib = lib
     return lib
+
+
+def make_config(dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm", solver="hlld",
+                emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.9, cfl_max_var=1.1,
+                first_dt=1.0e-10, maxdivb=1e-6, log_period=0, check_nan_period=0, precision="fp64"):
+    """idfx_gpu_config from the input-file style arguments of GpuBlock."""
+    lib = load_library()
+    n = list(n) + [1] * (3 - len(n))
+    cfg = Config()
+    lib.idfx_gpu_default_config(ctypes.byref(cfg), dims, n[0], n[1], n[2])
+    for d in range(3):
+        cfg.xbeg[d] = float(xbeg[d]) if d < len(xbeg) else 0.0
+        cfg.xend[d] = float(xend[d]) if d < len(xend) else 1.0
+    try:
+        cfg.order, cfg.solver, cfg.emf = ORDER[order], SOLVER[solver], EMF[emf]
+        cfg.precision = PRECISION[precision]
+    except KeyError as exc:
+        raise IdefixError(f"unknown scheme option {exc}") from None
+    cfg.nstages = nstages
+    cfg.gamma, cfg.cfl, cfg.cfl_max_var = gamma, cfl, cfl_max_var
+    cfg.first_dt, cfg.maxdivb = first_dt, maxdivb
+    cfg.log_period, cfg.check_nan_period = log_period, check_nan_period
+    return cfg
 
 
 def _as_ptr(a):
@@ -142,20 +203,8 @@ class GpuBlock:
                  check_nan_period=0, precision="fp64", stream=None):
         self.lib = load_library()
         n = list(n) + [1] * (3 - len(n))
-        cfg = Config()
-        self.lib.idfx_gpu_default_config(ctypes.byref(cfg), dims, n[0], n[1], n[2])
-        for d in range(3):
-            cfg.xbeg[d] = float(xbeg[d]) if d < len(xbeg) else 0.0
-            cfg.xend[d] = float(xend[d]) if d < len(xend) else 1.0
-        try:
-            cfg.order, cfg.solver, cfg.emf = ORDER[order], SOLVER[solver], EMF[emf]
-            cfg.precision = PRECISION[precision]
-        except KeyError as exc:
-            raise IdefixError(f"unknown scheme option {exc}") from None
-        cfg.nstages = nstages
-        cfg.gamma, cfg.cfl, cfg.cfl_max_var = gamma, cfl, cfl_max_var
-        cfg.first_dt, cfg.maxdivb = first_dt, maxdivb
-        cfg.log_period, cfg.check_nan_period = log_period, check_nan_period
+        cfg = make_config(dims, n, xbeg, xend, order, solver, emf, nstages, gamma, cfl, cfl_max_var,
+                          first_dt, maxdivb, log_period, check_nan_period, precision)
         h = ctypes.c_void_p()
         rc = self.lib.idfx_gpu_create(ctypes.byref(cfg), ctypes.c_void_p(stream), ctypes.byref(h))
         if rc != OK:
@@ -268,6 +317,34 @@ class GpuBlock:
 
 
     # -- per-kernel timing --------------------------------------------------
+    def set_learned(self, params, fmin=None, fmax=None):
+        """Load the learned-reconstruction network (order "learned")."""
+        fp = ctypes.POINTER(ctypes.c_float)
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != 46352:
+            raise IdefixError("the network has 46352 parameters")
+        lo = hi = None
+        if fmin is not None:
+            lo = np.ascontiguousarray(fmin, dtype=np.float32)
+            hi = np.ascontiguousarray(fmax, dtype=np.float32)
+        self._check(self.lib.idfx_gpu_set_learned(
+            self.h, p.ctypes.data_as(fp), None if lo is None else lo.ctypes.data_as(fp),
+            None if hi is None else hi.ctypes.data_as(fp)))
+        self._learned_keep = (p, lo, hi)
+
+    def learned_states(self):
+        """face states of the learned reconstruction on the current state:
+        [3 directions, 16 (minus 0-7, plus 8-15), nz, ny, nx] (ghosted)"""
+        ls = np.zeros((3, 16) + self.vc_shape[1:])
+        self._check(self.lib.idfx_gpu_learned_states(self.h, _as_ptr(ls)))
+        return ls
+
+    def learned_stats(self):
+        """(cells evaluated, cells that fell back to plain PLM)"""
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        self._check(self.lib.idfx_gpu_learned_stats(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def profile(self, enable=True):
         self._check(self.lib.idfx_gpu_profile(self.h, 1 if enable else 0))
 
@@ -315,3 +392,98 @@ class TimeIntegrator:
 
     def GetNCycles(self):
         return self.block.get_time()[2]
+
+
+class Ensemble:
+    """Independent periodic blocks of uneven sizes advanced together.
+
+    boxes: list of dicts of GpuBlock keyword arguments (dims, n, xbeg, xend,
+    gamma, cfl, first_dt, ...); the scheme keywords (dims, order, solver, emf,
+    nstages, precision, log_period, check_nan_period) must agree.  Each box
+    evolves exactly as a GpuBlock with the same arguments, with its own
+    CFL time step.
+    """
+
+    def __init__(self, boxes, stream=None):
+        self.lib = load_library()
+        nbox = len(boxes)
+        if nbox < 1:
+            raise IdefixError("an ensemble needs at least one box")
+        cfgs = (Config * nbox)()
+        for b, kw in enumerate(boxes):
+            cfgs[b] = make_config(**kw)
+        h = ctypes.c_void_p()
+        rc = self.lib.idfx_ens_create(nbox, cfgs, ctypes.c_void_p(stream), ctypes.byref(h))
+        if rc != OK:
+            raise IdefixError(f"idfx_ens_create failed with status {rc}")
+        self.h = h
+        self.nbox = nbox
+        self.shapes = []
+        for b, kw in enumerate(boxes):
+            dims = kw["dims"]
+            n = list(kw["n"]) + [1] * (3 - len(kw["n"]))
+            nvar, ng = ctypes.c_int(), ctypes.c_int()
+            self.lib.idfx_ens_sizes(self.h, b, ctypes.byref(nvar), ctypes.byref(ng), None, None)
+            nt = [n[d] + 2 * ng.value if d < dims else 1 for d in range(3)]
+            ntv = [nt[d] + (1 if d < dims else 0) for d in range(3)]
+            self.shapes.append(((nvar.value, nt[2], nt[1], nt[0]), (dims, ntv[2], ntv[1], ntv[0])))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.idfx_ens_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc == OK:
+            return
+        buf = ctypes.create_string_buffer(512)
+        self.lib.idfx_ens_last_error(self.h, buf, 512)
+        msg = buf.value.decode(errors="replace")
+        if rc in (ERR_NAN, ERR_DIVB, ERR_DT_SMALL):
+            raise RuntimeError(msg)
+        raise IdefixError(f"status {rc}: {msg}")
+
+    def upload(self, box, Vc, Vs):
+        Vc = np.ascontiguousarray(Vc, dtype=np.float64)
+        Vs = np.ascontiguousarray(Vs, dtype=np.float64)
+        if (Vc.shape, Vs.shape) != self.shapes[box]:
+            raise IdefixError(f"box {box}: state shapes {Vc.shape}/{Vs.shape} != {self.shapes[box]}")
+        self._check(self.lib.idfx_ens_upload_prim(self.h, box, _as_ptr(Vc), _as_ptr(Vs)))
+
+    def download(self, box):
+        Vc = np.empty(self.shapes[box][0])
+        Vs = np.empty(self.shapes[box][1])
+        self._check(self.lib.idfx_ens_download_prim(self.h, box, _as_ptr(Vc), _as_ptr(Vs)))
+        return Vc, Vs
+
+    def download_device(self, box, vc_ptr, vs_ptr):
+        """copy one box's Vc / Vs into device arrays of this process"""
+        self._check(self.lib.idfx_ens_download_prim_device(self.h, box, ctypes.c_void_p(vc_ptr),
+                                                           ctypes.c_void_p(vs_ptr)))
+
+    def get_time(self, box):
+        """(t, dt, ncycles, status) of one box."""
+        t, dt = ctypes.c_double(), ctypes.c_double()
+        nc, st = ctypes.c_longlong(), ctypes.c_int()
+        self._check(self.lib.idfx_ens_get_time(self.h, box, ctypes.byref(t), ctypes.byref(dt),
+                                               ctypes.byref(nc), ctypes.byref(st)))
+        return t.value, dt.value, nc.value, st.value
+
+    def run(self, tstop=-1.0, max_cycles=-1, graph=True):
+        self._check(self.lib.idfx_ens_run(self.h, float(tstop), int(max_cycles), 1 if graph else 0))
+
+    def autotune(self, reps=3):
+        self._check(self.lib.idfx_ens_autotune(self.h, int(reps)))
+
+    def segments(self, box):
+        seg = (ctypes.c_int * 3)()
+        self._check(self.lib.idfx_ens_get_segments(self.h, box, seg))
+        return list(seg)
+
+    def set_schedule(self, schedule):
+        """Block order of the batched launches: "largest_first" or "box_order"."""
+        code = {"largest_first": 0, "box_order": 1}[schedule]
+        self._check(self.lib.idfx_ens_set_schedule(self.h, code))

@@ -17,10 +17,6 @@
 
 using namespace idfx;
 
-struct idfx_gpu {
-  Engine e;
-};
-
 namespace idfx {
 
 cudaEvent_t take_event(Engine& e) {
@@ -217,6 +213,7 @@ void queue_cycle(Engine& e, int use_tstop) {
     const int save = (e.nstages > 1 && stage == 0);
     launch_fill_faces(e, save);
     launch_stage_begin(e, kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
+    if (g.order == IDFX_LEARNED) launch_learned_recon(e);
     launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
     const int combine = stage > 0;
     const double wc = combine ? e.wc[stage - 1] : 1.0, w0 = combine ? e.w0[stage - 1] : 0.0;
@@ -303,7 +300,11 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   if (!cfg || !out) return IDFX_ERR_STATE;
   *out = nullptr;
   if (cfg->dims != 2 && cfg->dims != 3) return IDFX_ERR_CONFIG;
-  if (cfg->order < 1 || cfg->order > 4 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
+  if (cfg->order < 1 || cfg->order > 5 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
+  // the learned reconstruction: 3-D, HLLD, FP64 arithmetic around the network
+  if (cfg->order == IDFX_LEARNED &&
+      (cfg->dims != 3 || cfg->solver != IDFX_HLLD || cfg->precision != IDFX_FP64))
+    return IDFX_ERR_CONFIG;
   if (cfg->emf < 0 || cfg->emf > 4 || cfg->nstages < 1 || cfg->nstages > 3) return IDFX_ERR_CONFIG;
   if (cfg->precision != IDFX_FP64 && cfg->precision != IDFX_MIXED) return IDFX_ERR_CONFIG;
   // constrainedTransport.hpp:256-261
@@ -374,7 +375,8 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   const bool hll_emf = (g.emf == kEmfUctHll || g.emf == kEmfUctHlld);
   size_t len = 3 * NV * nc + 2 * g.D * nf + nc  // Vc, Uc, Uc0, Vs, Vs0, InvDt
                + 6 * nc + 3 * nc + 3 * nc + 3 * nc  // face EMFs, sv, cell EMFs, corner EMFs
-               + (hll_emf ? 12 * nc : 0);
+               + (hll_emf ? 12 * nc : 0)
+               + (g.order == IDFX_LEARNED ? 48 * nc : 0);  // learned face states
   int rc = IDFX_OK;
   if (stream) {
     e.stream = (cudaStream_t)stream;
@@ -411,6 +413,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
     f.dL[d] = hll_emf ? take(nc) : nullptr;
     f.dR[d] = hll_emf ? take(nc) : nullptr;
   }
+  f.ls = (g.order == IDFX_LEARNED) ? take(48 * nc) : nullptr;
   Ctl c{};
   c.t = 0.0;
   c.dt = cfg->first_dt;
@@ -471,6 +474,7 @@ int idfx_gpu_destroy(idfx_gpu* h) {
     cudaEventDestroy(m.b);
   }
   for (auto ev : e.free_events) cudaEventDestroy(ev);
+  free_learned(e);
   if (e.pool) cudaFree(e.pool);
   if (e.ctl) cudaFree(e.ctl);
   if (e.ctl_host) cudaFreeHost(e.ctl_host);
@@ -562,6 +566,8 @@ int idfx_gpu_get_time(idfx_gpu* h, double* t, double* dt, long long* ncycles) {
 // run cycles; the device flags `done` when t reaches tstop or on error
 static int run_cycles(idfx_gpu* h, double tstop, long long max_cycles) {
   Engine& e = h->e;
+  if (e.g.order == IDFX_LEARNED && !e.learned)
+    return fail(e, IDFX_ERR_STATE, "the learned reconstruction needs idfx_gpu_set_learned first");
   int rc = read_ctl(e);
   if (rc) return rc;
   e.ctl_host->tstop = tstop;
@@ -648,7 +654,10 @@ int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt) {
   if (!h) return IDFX_ERR_STATE;
   Engine& e = h->e;
   clear_done(e);
+  if (e.g.order == IDFX_LEARNED && !e.learned)
+    return fail(e, IDFX_ERR_STATE, "the learned reconstruction needs idfx_gpu_set_learned first");
   k_set_stage_dt<<<1, 1, 0, e.stream>>>(e.g, e.ctl, dt);
+  if (e.g.order == IDFX_LEARNED) launch_learned_recon(e);
   if (e.g.emf == kEmfContact || e.g.emf == kEmfUct0)
     IDFX_DISPATCH_D(k_cell_emf_all, nblocks(e.g.ncell), kThreads, e.g, e.f);
   launch_sweeps(e, 2, 0);

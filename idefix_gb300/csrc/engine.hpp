@@ -34,6 +34,7 @@ struct Engine {
   };
   std::vector<Mark> marks;
   std::vector<cudaEvent_t> free_events;
+  void* learned = nullptr;   // network of the learned reconstruction (ORDER 5)
 };
 
 // kernel classes reported by the per-kernel timing
@@ -48,12 +49,17 @@ enum KernelClass {
   kKStageEnd,
   kKControl,
   kKChecks,
+  kKLearned,
   kKNumClasses
 };
 
 cudaEvent_t take_event(Engine& e);
 void mark_begin(Engine& e, int cls);
 void mark_end(Engine& e);
+
+// fused learned reconstruction of one stage (ORDER 5) and its release
+void launch_learned_recon(Engine& e);
+void free_learned(Engine& e);
 
 // launches the D flux sweeps of one stage (one function per Riemann solver,
 // each in its own translation unit)
@@ -63,3 +69,7 @@ void launch_sweeps_roe(Engine& e, int invdt, int fold_max);
 void launch_sweeps_tvdlf(Engine& e, int invdt, int fold_max);
 
 }  // namespace idfx
+
+struct idfx_gpu {
+  idfx::Engine e;
+};

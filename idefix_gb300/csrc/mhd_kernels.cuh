@@ -63,6 +63,7 @@ struct Fields {
   double *Ex1, *Ex2, *Ex3;
   double *ex, *ey, *ez;
   double *aL[3], *aR[3], *dL[3], *dR[3];
+  double* ls;  // learned face states [3][16][ncell] (ORDER 5)
 };
 
 __device__ __forceinline__ long long cidx(const Geo& g, int k, int j, int i) {
@@ -395,7 +396,12 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
       } else {
         w[n][W - 1] = (T)f.Vc[n * g.ncell + cc + H * sd];
       }
-      Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n]);
+      if constexpr (ORDER == 5) {  // states of the fused learned reconstruction
+        vl[n] = (T)f.ls[((long long)DIR * 16 + n) * g.ncell + cc];
+        vr[n] = (T)f.ls[((long long)DIR * 16 + 8 + n) * g.ncell + cc];
+      } else {
+        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n]);
+      }
     }
     if (c >= m0) {
       T vL[NV], vR[NV];

@@ -247,9 +247,11 @@ __device__ __forceinline__ void ppm_states(T vm2, T vm1, T v0, T vp1, T vp2, T& 
 // the reference evaluates the same limiter twice per cell (once for each
 // face); here it is evaluated once and shared, with identical arithmetic.
 // pos = true for RHO and PRS (positivity fallbacks of ORDER 3 and 4).
+// ORDER 5 (learned) reads its states from the fused learned reconstruction;
+// its stencil half-width is PLM's.
 template <int ORDER>
 struct Recon {
-  static constexpr int H = (ORDER == 1 ? 0 : (ORDER == 4 ? 2 : 1));
+  static constexpr int H = (ORDER == 1 ? 0 : (ORDER == 4 ? 2 : 1));  // ORDER 5: 1
   template <typename T>
   __device__ __forceinline__ static void cell(const T* w, T dx, bool pos, T& vl, T& vr) {
     if constexpr (ORDER == 1) {

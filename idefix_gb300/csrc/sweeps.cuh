@@ -2,6 +2,7 @@
 // dimensionality and reconstruction order.
 #pragma once
 #include "engine.hpp"
+#include "ensemble.hpp"
 
 namespace idfx {
 
@@ -44,6 +45,43 @@ void launch_sweeps_solver(Engine& e, int invdt, int fold_max) {
   IDFX_CASE(2, 1) IDFX_CASE(2, 2) IDFX_CASE(2, 3) IDFX_CASE(2, 4)
   IDFX_CASE(3, 1) IDFX_CASE(3, 2) IDFX_CASE(3, 3) IDFX_CASE(3, 4)
 #undef IDFX_CASE
+  if constexpr (SOLVER == kHLLD)  // learned reconstruction: 3-D, HLLD, FP64
+    if (D == 3 && O == 5) launch_sweeps_tt<3, 5, SOLVER, double>(e, invdt, fold_max);
+}
+
+// ---------------------------------------------------------------------------
+// ensemble: one launch covers the sweep blocks of every box
+// ---------------------------------------------------------------------------
+template <int D, int DIR, int ORDER, int SOLVER, typename T>
+__global__ void __launch_bounds__(kTM) ke_sweep_march(const EnsBox* boxes, const int4* items, int invdt,
+                                                      int last) {
+  const int4 it = items[blockIdx.x];
+  const EnsBox& B = boxes[it.x];
+  d_sweep_march<D, DIR, ORDER, SOLVER, T>(B.g, B.f, B.ctl, invdt, last, B.seg[DIR], dim3(it.y, it.z, it.w));
+}
+
+template <int D, int ORDER, int SOLVER, typename T>
+void launch_ens_dir(EnsEngine& e, int dir, const EnsTable& t, int invdt, int last) {
+  if (t.n == 0) return;
+  if (dir == 0) ke_sweep_march<D, 0, ORDER, SOLVER, T><<<t.n, kTM, 0, e.stream>>>(e.d_boxes, t.items, invdt, last);
+  if (dir == 1) ke_sweep_march<D, 1, ORDER, SOLVER, T><<<t.n, kTM, 0, e.stream>>>(e.d_boxes, t.items, invdt, last);
+  if constexpr (D == 3)
+    if (dir == 2) ke_sweep_march<D, 2, ORDER, SOLVER, T><<<t.n, kTM, 0, e.stream>>>(e.d_boxes, t.items, invdt, last);
+}
+
+template <int SOLVER>
+void launch_ens_sweep_solver(EnsEngine& e, int dir, const EnsTable& t, int invdt, int last) {
+  const int D = e.D, O = e.order;
+  const bool mixed = e.precision == 1;
+#define IDFX_ECASE(DD, OO)                                                            \
+  if (D == DD && O == OO) {                                                           \
+    if (mixed) launch_ens_dir<DD, OO, SOLVER, float>(e, dir, t, invdt, last);         \
+    else launch_ens_dir<DD, OO, SOLVER, double>(e, dir, t, invdt, last);              \
+    return;                                                                           \
+  }
+  IDFX_ECASE(2, 1) IDFX_ECASE(2, 2) IDFX_ECASE(2, 3) IDFX_ECASE(2, 4)
+  IDFX_ECASE(3, 1) IDFX_ECASE(3, 2) IDFX_ECASE(3, 3) IDFX_ECASE(3, 4)
+#undef IDFX_ECASE
 }
 
 }  // namespace idfx

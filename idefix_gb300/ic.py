@@ -65,6 +65,37 @@ def orszag_tang_2d(n=256, nghost=2, gamma=5.0 / 3.0):
     return Vc, Vs
 
 
+def orszag_tang_like_2d(n, mach=1.0, beta=10.0 / 3.0, nghost=2, gamma=5.0 / 3.0):
+    """Orszag-Tang vortex with a chosen sonic Mach number and plasma beta.
+
+    rho and p are the vortex's (sound speed sqrt(gamma p / rho) = 1 at
+    gamma = 5/3); the velocity amplitude is mach times the sound speed and
+    the field amplitude B0 = sqrt(2 p / beta) (beta = p / (B0^2 / 2)).
+    mach = 1, beta = 10/3 is the standard vortex.
+    """
+    Vc, Vs = orszag_tang_2d(n, nghost)
+    p = 5.0 / (12.0 * math.pi)
+    cs = math.sqrt(gamma * p / (25.0 / (36.0 * math.pi)))
+    Vc[1:3] *= mach * cs
+    b_scale = math.sqrt(2.0 * p / beta) * math.sqrt(4.0 * math.pi)
+    Vs *= b_scale
+    return Vc, Vs
+
+
+ENSEMBLE_SIZES = (64, 96, 128, 192, 256, 384, 512)
+
+
+def ensemble_boxes(nbox=512, seed=0, sizes=ENSEMBLE_SIZES):
+    """Seeded ensemble of Orszag-Tang-like boxes: size uniform over `sizes`
+    (square boxes), sonic Mach uniform in [0.5, 2], beta log-uniform in
+    [0.1, 10].  Returns a list of (n, mach, beta)."""
+    rng = np.random.default_rng(seed)
+    n = rng.choice(np.asarray(sizes), size=nbox)
+    mach = rng.uniform(0.5, 2.0, size=nbox)
+    beta = 10.0 ** rng.uniform(-1.0, 1.0, size=nbox)
+    return [(int(n[b]), float(mach[b]), float(beta[b])) for b in range(nbox)]
+
+
 def _gaussian_field(rng, shape, kmin, kmax, slope=-2.0):
     """Real Gaussian random field with power ~ k^slope on kmin <= |k| <= kmax
     (integer wavenumbers of a periodic box), unit rms."""

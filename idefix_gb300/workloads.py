@@ -1,0 +1,226 @@
+"""Workloads measured beyond the single-block throughput run.
+
+learned: 3-D decaying turbulence (the throughput run's initial state);
+training snapshots from an ensemble of seeded fine runs coarsened by r,
+the correction network trained on them with the library's BF16 kernels,
+then on held-out seeds the coarse learned run, the coarse plain run and a
+plain run at twice the coarse resolution are compared with the coarsened
+fine FP64 run at the same end time (L1 error and wall time).
+
+ensemble: 512 Orszag-Tang-like 2-D boxes of sizes drawn from
+{64..512}^2 (sonic Mach U[0.5, 2], beta log-U[0.1, 10], seeded), HLLD + PLM
++ CT (uct_contact), RK2, CFL 0.6, FP64, a fixed number of cycles with each
+box's own CFL time step; every box is then compared with the same box run
+alone through GpuBlock (exact equality expected), and the two wall times
+are reported.
+"""
+import json
+import sys
+import time
+
+import numpy as np
+
+import idefix_gb300 as ig
+from idefix_gb300 import ic
+
+
+def ensemble_case(nbox=512, seed=0, sizes=ic.ENSEMBLE_SIZES, cfl=0.6, first_dt=1e-4):
+    """Per-box (config dict, mach, beta) of the seeded ensemble."""
+    out = []
+    for n, mach, beta in ic.ensemble_boxes(nbox, seed, sizes):
+        cfg = dict(dims=2, n=(n, n), order="plm", solver="hlld", emf="uct_contact", nstages=2,
+                   cfl=cfl, first_dt=first_dt)
+        out.append((cfg, mach, beta))
+    return out
+
+
+def run_ensemble(nbox=512, seed=0, cycles=500, sizes=ic.ENSEMBLE_SIZES, check=True, autotune=True,
+                 graph=True, log=sys.stderr):
+    import torch
+
+    case = ensemble_case(nbox, seed, sizes)
+    ens = ig.Ensemble([c[0] for c in case])
+    cells = 0
+    for k, (cfg, mach, beta) in enumerate(case):
+        Vc, Vs = ic.orszag_tang_like_2d(cfg["n"][0], mach=mach, beta=beta)
+        ens.upload(k, Vc, Vs)
+        cells += cfg["n"][0] * cfg["n"][1]
+    t0 = time.perf_counter()
+    if autotune:
+        ens.autotune(reps=3)
+    t_tune = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ens.run(max_cycles=cycles, graph=graph)
+    t_ens = time.perf_counter() - t0
+    res = {"nbox": nbox, "seed": seed, "cycles": cycles, "active_cells": cells,
+           "ensemble_s": t_ens, "autotune_s": t_tune,
+           "zone_cycles_per_s": cells * cycles / t_ens,
+           "segments": sorted({(c[0]["n"][0], tuple(ens.segments(k)[:2])) for k, c in enumerate(case)})}
+    if not check:
+        ens.close()
+        return res
+    t_single = 0.0
+    mismatched = []
+    for k, (cfg, mach, beta) in enumerate(case):
+        Vc, Vs = ic.orszag_tang_like_2d(cfg["n"][0], mach=mach, beta=beta)
+        blk = ig.GpuBlock(**cfg)
+        blk.upload(Vc, Vs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        blk.run(max_cycles=cycles)
+        t_single += time.perf_counter() - t0
+        vc1, vs1 = blk.download()
+        tt1 = blk.get_time()
+        blk.close()
+        vc2, vs2 = ens.download(k)
+        tt2 = ens.get_time(k)[:3]
+        if not (np.array_equal(vc1, vc2) and np.array_equal(vs1, vs2) and tuple(tt1) == tuple(tt2)):
+            mismatched.append(k)
+        if log and k % 64 == 63:
+            print(f"checked {k + 1}/{nbox} boxes", file=log, flush=True)
+    ens.close()
+    res.update({"single_boxes_s": t_single, "speedup_vs_single": t_single / t_ens,
+                "boxes_identical": nbox - len(mismatched), "mismatched": mismatched})
+    return res
+
+
+def _l1(a, b):
+    """mean over the 8 variables of sum|a - b| / sum|b| (compact prim arrays)"""
+    return float(np.mean([np.abs(a[v] - b[v]).sum() / max(np.abs(b[v]).sum(), 1e-300) for v in range(8)]))
+
+
+def _timed_run(blk, t_end):
+    import torch
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    blk.run(tstop=t_end)
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
+
+
+def _coarse_of(Vc, Vs, n, r, learned):
+    import torch
+
+    p, f, _ = learned.coarsen(torch.from_numpy(Vc).cuda(), torch.from_numpy(Vs).cuda(), n, 2, r)
+    return p, f
+
+
+def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=(200, 201, 202, 203),
+                nsnap=50, t_end=1.0, steps=3000, batch=8192, lr=2e-3, lr_end=2e-5,
+                train_precision="mixed", log=sys.stderr):
+    import torch
+
+    from idefix_gb300 import learned
+
+    nc = n_fine // r
+    res = {"n_fine": n_fine, "n_coarse": nc, "t_end": t_end, "train_runs": len(train_seeds), "snapshots": nsnap,
+           "train_precision": train_precision}
+    # 1. training snapshots through the ensemble path
+    boxes = [dict(dims=3, n=(n_fine,) * 3, cfl=0.6, first_dt=1e-4, precision=train_precision)
+             for _ in train_seeds]
+    ens = ig.Ensemble(boxes)
+    shp_c, shp_s = ens.shapes[0]
+    for k, s in enumerate(train_seeds):
+        Vc, Vs = ic.turbulence_3d(n_fine, seed=s)
+        ens.upload(k, Vc, Vs)
+    S = len(train_seeds) * nsnap
+    prims = torch.empty((S, 8, nc, nc, nc), dtype=torch.float32, device="cuda")
+    tgts = torch.empty((S, 3, 16, nc**3), dtype=torch.float32, device="cuda")
+    vc_buf = torch.empty(shp_c, dtype=torch.float64, device="cuda")
+    vs_buf = torch.empty(shp_s, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for j in range(nsnap):
+        ens.run(tstop=t_end * (j + 1) / nsnap)
+        for k in range(len(train_seeds)):
+            ens.download_device(k, vc_buf.data_ptr(), vs_buf.data_ptr())
+            p, _, tg = learned.coarsen(vc_buf, vs_buf, n_fine, 2, r)
+            prims[k * nsnap + j] = p.float()
+            tgts[k * nsnap + j] = tg.float()
+        if log:
+            print(f"snapshot {j + 1}/{nsnap}", file=log, flush=True)
+    torch.cuda.synchronize()
+    res["data_s"] = time.perf_counter() - t0
+    res["train_cycles"] = ens.get_time(0)[2]
+    ens.close()
+    del vc_buf, vs_buf
+    # 2. training with the library's BF16 tensor-core kernels
+    tr = learned.Trainer(max_batch=batch)
+    tr.set_dataset(prims, tgts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = tr.train(steps, batch, lr=lr, lr_end=lr_end, seed=7)
+    torch.cuda.synchronize()
+    res["train_s"] = time.perf_counter() - t0
+    res["loss_first"] = float(losses[:10].mean())
+    res["loss_last"] = float(losses[-50:].mean())
+    params = tr.get_params()
+    fmin, fmax = tr.feature_range()
+    del prims, tgts
+    # 3. held-out seeds: errors against the coarsened fine FP64 run
+    rows = []
+    for s in eval_seeds:
+        Vc, Vs = ic.turbulence_3d(n_fine, seed=s)
+        fine = ig.GpuBlock(3, (n_fine,) * 3, cfl=0.6, first_dt=1e-4)
+        fine.upload(Vc, Vs)
+        t_fine = _timed_run(fine, t_end)
+        ref, _ = _coarse_of(*fine.download(), n_fine, r, learned)
+        ref = ref.cpu().numpy()
+        fine.close()
+        row = {"seed": s, "fine_s": t_fine}
+        for name, order, nres in (("plain", "plm", nc), ("learned", "learned", nc), ("plain_2x", "plm", 2 * nc)):
+            pc, fc = _coarse_of(Vc, Vs, n_fine, n_fine // nres, learned)
+            Vcc, Vsc = learned.coarse_state(pc, fc)
+            blk = ig.GpuBlock(3, (nres,) * 3, order=order, cfl=0.6, first_dt=1e-4)
+            if order == "learned":
+                blk.set_learned(params, fmin, fmax)
+            blk.upload(Vcc, Vsc)
+            row[name + "_s"] = _timed_run(blk, t_end)
+            out, _ = _coarse_of(*blk.download(), nres, nres // nc, learned) if nres != nc else (None, None)
+            if out is None:
+                vc_out = blk.download()[0][:, 2:2 + nc, 2:2 + nc, 2:2 + nc]
+            else:
+                vc_out = out.cpu().numpy()
+            row[name + "_l1"] = _l1(vc_out, ref)
+            if order == "learned":
+                cells, fall = blk.learned_stats()
+                row["fallback_rate"] = fall / max(cells, 1)
+            blk.close()
+        rows.append(row)
+        if log:
+            print(json.dumps(row), file=log, flush=True)
+    res["eval"] = rows
+    for k in ("plain_l1", "learned_l1", "plain_2x_l1", "fine_s", "learned_s", "plain_s", "fallback_rate"):
+        res[k] = float(np.mean([row[k] for row in rows]))
+    res["learned_over_plain_2x_l1"] = res["learned_l1"] / res["plain_2x_l1"]
+    res["fine_over_learned_time"] = res["fine_s"] / res["learned_s"]
+    return res, params, fmin, fmax
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", choices=["ensemble", "learned"], default="ensemble")
+    ap.add_argument("--nbox", type=int, default=512)
+    ap.add_argument("--n-fine", type=int, default=128)
+    ap.add_argument("--train-runs", type=int, default=40)
+    ap.add_argument("--snapshots", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--t-end", type=float, default=1.0)
+    ap.add_argument("--save", default=None, help="npz file for the trained parameters and range")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cycles", type=int, default=500)
+    ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
+    a = ap.parse_args()
+    if a.workload == "ensemble":
+        r = run_ensemble(a.nbox, a.seed, a.cycles, check=not a.no_check, graph=not a.no_graph)
+    else:
+        r, params, fmin, fmax = run_learned(a.n_fine, train_seeds=tuple(range(100, 100 + a.train_runs)),
+                                            nsnap=a.snapshots, t_end=a.t_end, steps=a.steps)
+        if a.save:
+            np.savez(a.save, params=params, fmin=fmin, fmax=fmax)
+    print(json.dumps(r))

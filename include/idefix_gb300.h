@@ -39,8 +39,10 @@ typedef enum {
   IDFX_ERR_STATE = 7        /* call out of order / null handle             */
 } idfx_status;
 
-/* reconstruction order: Idefix_RECONSTRUCTION (CMakeLists.txt:198-209) */
-enum { IDFX_ORDER1 = 1, IDFX_PLM = 2, IDFX_LIMO3 = 3, IDFX_PPM = 4 };
+/* reconstruction order: Idefix_RECONSTRUCTION (CMakeLists.txt:198-209);
+ * IDFX_LEARNED (no counterpart in the reference) is PLM corrected by the
+ * learned interface-state network, 3-D HLLD FP64 only (idfx_gpu_set_learned) */
+enum { IDFX_ORDER1 = 1, IDFX_PLM = 2, IDFX_LIMO3 = 3, IDFX_PPM = 4, IDFX_LEARNED = 5 };
 /* [Hydro] solver (riemannSolver.hpp:27) */
 enum { IDFX_HLLD = 0, IDFX_HLL = 1, IDFX_ROE = 2, IDFX_TVDLF = 3 };
 /* [Hydro] emf (constrainedTransport.hpp:155-179) */
@@ -136,6 +138,7 @@ enum {
   IDFX_K_STAGE_END,
   IDFX_K_CONTROL,
   IDFX_K_CHECKS,
+  IDFX_K_LEARNED,
   IDFX_K_NUM
 };
 int idfx_gpu_profile(idfx_gpu* h, int enable);
@@ -157,6 +160,91 @@ int idfx_gpu_profile_read(idfx_gpu* h, double* ms, long long* launches, int ncla
 #define IDFX_NOALLOC_SCRATCH_DOUBLES (4u * 1024u * 1024u)
 int idfx_evolve_stage_noalloc(const idfx_gpu_config* cfg, const double* Vc, double* Uc, double* Vs,
                               double t, double dt, void* stream, char* err, size_t errlen);
+
+/* Learned interface-state correction — no counterpart in the reference.
+ * A network (216 -> 128 -> 128 -> 16, SiLU, BF16 tensor-core arithmetic
+ * with FP32 accumulation) reads the 3x3x3 primitive stencil of a cell in
+ * the frame rotated to the sweep direction, scaled by the centre cell, and
+ * corrects the cell's two PLM face states; cells whose stencil leaves the
+ * trained feature range, or whose corrected density or pressure is not
+ * positive, keep the plain PLM states.  Parameters: packed FP32 host array
+ * W1[216][128] b1[128] W2[128][128] b2[128] W3[128][16] b3[16]. */
+#define IDFX_MLP_NPARAM 46352
+#define IDFX_MLP_NIN 216
+/* loads the network into a handle created with order IDFX_LEARNED; fmin /
+ * fmax: trained feature range (IDFX_MLP_NIN each), or NULL for no range
+ * check.  Resets the counters of idfx_gpu_learned_stats. */
+int idfx_gpu_set_learned(idfx_gpu* h, const float* params, const float* fmin, const float* fmax);
+/* Boundary::SetBoundaries, then the learned face states of the current Vc:
+ * ls[3][16][ncell] doubles (direction, minus-face vars 0-7 / plus-face vars
+ * 8-15 in the solver's variable order, cell of the ghosted layout); cells
+ * without a full 3x3x3 stencil hold zeros */
+int idfx_gpu_learned_states(idfx_gpu* h, double* ls);
+/* cells evaluated (per direction and stage) and cells that fell back to PLM */
+int idfx_gpu_learned_stats(idfx_gpu* h, long long* cells, long long* fallbacks);
+
+/* Trainer of the network (Adam, masked squared error of the normalised
+ * corrections).  The *_device entry points take pointers to this process's
+ * GPU memory; the training snapshots stay owned by the caller. */
+typedef struct idfx_mlp idfx_mlp;
+int idfx_mlp_create(int max_batch, void* stream, idfx_mlp** out);
+int idfx_mlp_destroy(idfx_mlp* h);
+int idfx_mlp_set_params(idfx_mlp* h, const float* params); /* host; resets Adam */
+int idfx_mlp_get_params(idfx_mlp* h, float* params);
+/* snapshots: coarse primitives float[nsnap][8][nc^3] and raw face targets
+ * float[nsnap][3][16][nc^3] (idfx_learn_coarsen_device, converted) */
+int idfx_mlp_set_dataset_device(idfx_mlp* h, const float* prims, const float* targets, int nsnap, int nc,
+                                double gamma);
+/* steps of Adam on random batches (cosine learning rate lr -> lr_end);
+ * losses: host float[steps] or NULL */
+int idfx_mlp_train(idfx_mlp* h, int steps, int batch, float lr, float lr_end, unsigned long long seed,
+                   float* losses);
+/* loss of one random batch with the network and with no correction */
+int idfx_mlp_eval(idfx_mlp* h, int batch, unsigned long long seed, double* loss, double* loss_zero);
+/* range of every feature over the training batches so far (host arrays) */
+int idfx_mlp_feature_range(idfx_mlp* h, float* fmin, float* fmax);
+/* one batch: features X (bfloat16 [batch][224]) and targets T (float [batch][16]) */
+int idfx_mlp_batch_device(idfx_mlp* h, int batch, unsigned long long seed, long long base, void* X, float* T);
+/* loss and gradient (host float[IDFX_MLP_NPARAM]) of a given batch */
+int idfx_mlp_grad_device(idfx_mlp* h, const void* X, const float* T, int batch, float* grad, double* loss);
+/* network output Y (device float [batch][16]) of a given batch */
+int idfx_mlp_forward_device(idfx_mlp* h, const void* X, int batch, float* Y);
+/* coarsening of a 3-D periodic snapshot by r: Vc / Vs in the reference
+ * layout (device); outputs compact double prim[8][nc^3], faces[3][nc^3]
+ * (left faces) and targets[3][16][nc^3] (face-layer means, rotated order) */
+int idfx_learn_coarsen_device(const double* Vc, const double* Vs, int nf, int nghost, int r, double gamma,
+                              double* prim, double* faces, double* targets, void* stream);
+
+/* Ensemble of independent periodic blocks of uneven sizes advanced together
+ * — no counterpart in the reference, which runs one block per process
+ * (main.cpp:190-225 loops TimeIntegrator::Cycle on one DataBlock).  Every
+ * box has its own grid, gamma, CFL and first_dt and its own time step (per-box
+ * CFL dt); the scheme (dims, order, solver, emf, nstages, precision, log and
+ * NaN-check periods) is shared.  Each phase of a stage is one launch over the
+ * blocks of every box and one cycle is replayed as a CUDA graph; each box
+ * evolves exactly as an idfx_gpu handle with the same config would. */
+typedef struct idfx_ens idfx_ens;
+int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_ens** out);
+int idfx_ens_destroy(idfx_ens* h);
+int idfx_ens_last_error(const idfx_ens* h, char* buf, size_t len);
+int idfx_ens_sizes(const idfx_ens* h, int box, int* nvar, int* nghost, long long* vc_len, long long* vs_len);
+/* host arrays of one box, same layout as idfx_gpu_upload_prim */
+int idfx_ens_upload_prim(idfx_ens* h, int box, const double* Vc, const double* Vs);
+int idfx_ens_download_prim(idfx_ens* h, int box, double* Vc, double* Vs);
+/* same, into device arrays of this process */
+int idfx_ens_download_prim_device(idfx_ens* h, int box, double* Vc, double* Vs);
+/* t, dt, cycle count and status (idfx_status) of one box */
+int idfx_ens_get_time(idfx_ens* h, int box, double* t, double* dt, long long* ncycles, int* status);
+/* every box cycles until its t reaches tstop (< 0: no limit), at most
+ * max_cycles cycles (< 0: no limit); a box that stops or fails leaves the
+ * others running.  use_graph = 0 queues the launches one by one. */
+int idfx_ens_run(idfx_ens* h, double tstop, long long max_cycles, int use_graph);
+/* Autotuner: per box size and direction, the march segment length of the
+ * fastest batched sweep (timed over reps launches); the state is restored. */
+int idfx_ens_autotune(idfx_ens* h, int reps);
+int idfx_ens_get_segments(const idfx_ens* h, int box, int* seg);
+/* block order of the batched launches: 0 largest box first, 1 box order */
+int idfx_ens_set_schedule(idfx_ens* h, int schedule);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,143 @@
+"""The batched ensemble (idfx_ens_*): independent periodic boxes of uneven
+sizes advanced by shared launches, each with its own CFL time step.
+
+Every box must evolve exactly as the same box run alone through the
+single-block entry points (GpuBlock, itself bit-identical to the reference),
+so every comparison here is exact equality of the state, the time, the time
+step and the cycle count: with and without the CUDA graph, after the
+autotuner, with the divB / NaN diagnostics on, with boxes that stop at
+tstop after different numbers of cycles, and with a box that fails.
+"""
+import numpy as np
+import pytest
+
+import idefix_gb300 as ig
+from idefix_gb300 import ic
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from idefix_gb300 import build
+
+    build.build_library()
+    ig.load_library()
+
+
+def _box2d(n, mach, beta, **kw):
+    Vc, Vs = ic.orszag_tang_like_2d(n, mach=mach, beta=beta)
+    cfg = dict(dims=2, n=(n, n), **kw)
+    return cfg, Vc, Vs
+
+
+def _single(cfg, Vc, Vs, tstop=-1.0, cycles=-1):
+    blk = ig.GpuBlock(**cfg)
+    blk.upload(Vc, Vs)
+    rc = None
+    try:
+        blk.run(tstop=tstop, max_cycles=cycles)
+    except (ig.IdefixError, RuntimeError) as exc:
+        rc = exc
+    out = blk.download()
+    t, dt, nc = blk.get_time()
+    blk.close()
+    return out, (t, dt, nc), rc
+
+
+def _ensemble(boxes, tstop=-1.0, cycles=-1, graph=True, autotune=False, schedule=None):
+    ens = ig.Ensemble([b[0] for b in boxes])
+    for k, (_, Vc, Vs) in enumerate(boxes):
+        ens.upload(k, Vc, Vs)
+    if schedule:
+        ens.set_schedule(schedule)
+    if autotune:
+        ens.autotune(reps=2)
+    err = None
+    try:
+        ens.run(tstop=tstop, max_cycles=cycles, graph=graph)
+    except (ig.IdefixError, RuntimeError) as exc:
+        err = exc
+    res = [(ens.download(k), ens.get_time(k)) for k in range(len(boxes))]
+    segs = [ens.segments(k) for k in range(len(boxes))]
+    ens.close()
+    return res, err, segs
+
+
+def _mixed_boxes(**kw):
+    kw.setdefault("first_dt", 1e-4)
+    spec = [(16, 0.5, 0.1, 0.6), (32, 2.0, 10.0, 0.8), (24, 1.0, 1.0, 0.5), (16, 1.7, 0.3, 0.9),
+            (40, 0.8, 4.0, 0.7)]
+    return [_box2d(n, m, b, cfl=c, **kw) for n, m, b, c in spec]
+
+
+def _assert_same(res, boxes, tstop=-1.0, cycles=-1):
+    for k, (cfg, Vc, Vs) in enumerate(boxes):
+        (vc1, vs1), (t1, dt1, nc1), _ = _single(cfg, Vc, Vs, tstop=tstop, cycles=cycles)
+        (vc2, vs2), (t2, dt2, nc2, st2) = res[k]
+        assert st2 == 0, f"box {k} status {st2}"
+        assert (t2, dt2, nc2) == (t1, dt1, nc1), f"box {k}"
+        assert np.array_equal(vc1, vc2), f"box {k}: Vc differs"
+        assert np.array_equal(vs1, vs2), f"box {k}: Vs differs"
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_ensemble_matches_single_boxes(graph):
+    boxes = _mixed_boxes()
+    res, err, _ = _ensemble(boxes, cycles=10, graph=graph)
+    assert err is None
+    _assert_same(res, boxes, cycles=10)
+
+
+def test_ensemble_with_diagnostics_and_rk3():
+    boxes = _mixed_boxes(log_period=3, check_nan_period=2, nstages=3)
+    res, err, _ = _ensemble(boxes, cycles=9)
+    assert err is None
+    _assert_same(res, boxes, cycles=9)
+
+
+def test_ensemble_tstop_boxes_stop_independently():
+    # per-box CFL dt: the boxes reach tstop after different cycle counts
+    boxes = _mixed_boxes(log_period=4, check_nan_period=5)
+    res, err, _ = _ensemble(boxes, tstop=0.1)
+    assert err is None
+    counts = {r[1][2] for r in res}
+    assert len(counts) > 1
+    _assert_same(res, boxes, tstop=0.1)
+
+
+def test_ensemble_autotune_and_schedule_keep_results():
+    boxes = _mixed_boxes()
+    res, err, segs = _ensemble(boxes, cycles=6, autotune=True, schedule="box_order")
+    assert err is None
+    assert all(s[0] in (2, 4, 8, 16, 32, 64) and s[1] in (2, 4, 8, 16, 32, 64) for s in segs)
+    _assert_same(res, boxes, cycles=6)
+
+
+def test_ensemble_3d_and_mixed_precision():
+    boxes = []
+    for n, seed in ((12, 1), (8, 2)):
+        Vc, Vs = ic.turbulence_3d(n, seed=seed, kmax=3)
+        boxes.append((dict(dims=3, n=(n, n, n), cfl=0.6, precision="mixed"), Vc, Vs))
+    res, err, _ = _ensemble(boxes, cycles=5)
+    assert err is None
+    _assert_same(res, boxes, cycles=5)
+
+
+def test_ensemble_failed_box_leaves_the_others_running():
+    boxes = _mixed_boxes()
+    # a first_dt far above the CFL step fails at the end of the first cycle
+    bad_cfg = dict(boxes[2][0], first_dt=1.0)
+    boxes[2] = (bad_cfg, boxes[2][1], boxes[2][2])
+    res, err, _ = _ensemble(boxes, cycles=7)
+    assert isinstance(err, ig.IdefixError) and "box 2" in str(err)
+    assert res[2][1][3] == ig.ERR_FIRST_DT
+    good = [k for k in range(len(boxes)) if k != 2]
+    _assert_same([res[k] for k in good], [boxes[k] for k in good], cycles=7)
+
+
+def test_ensemble_rejects_mixed_schemes():
+    cfg_a = dict(dims=2, n=(16, 16))
+    cfg_b = dict(dims=2, n=(16, 16), solver="hll")
+    with pytest.raises(ig.IdefixError):
+        ig.Ensemble([cfg_a, cfg_b])
