@@ -77,7 +77,8 @@ EXPORTS = [
     "idfx_gpu_set_learned", "idfx_gpu_learned_states", "idfx_gpu_learned_stats", "idfx_mlp_create", "idfx_mlp_destroy",
     "idfx_mlp_set_params", "idfx_mlp_get_params", "idfx_mlp_set_dataset_device", "idfx_mlp_train",
     "idfx_mlp_eval", "idfx_mlp_feature_range", "idfx_mlp_batch_device", "idfx_mlp_grad_device",
-    "idfx_mlp_forward_device", "idfx_learn_coarsen_device",
+    "idfx_mlp_forward_device", "idfx_learn_coarsen_device", "idfx_measure_fp64_peak",
+    "idfx_gpu_autotune", "idfx_gpu_get_segments",
 ]
 
 KERNEL_CLASSES = ["fill_faces", "stage_begin", "sweep_x", "sweep_y", "sweep_z", "ct_corner",
@@ -137,6 +138,9 @@ def load_library(path=LIB_PATH):
     lib.idfx_ens_download_prim_device.argtypes = [P, I, P, P]
     fp = ctypes.POINTER(ctypes.c_float)
     U64 = ctypes.c_ulonglong
+    lib.idfx_measure_fp64_peak.argtypes = [dp, P]
+    lib.idfx_gpu_autotune.argtypes = [P, I]
+    lib.idfx_gpu_get_segments.argtypes = [P, ctypes.POINTER(I)]
     lib.idfx_gpu_set_learned.argtypes = [P, fp, fp, fp]
     lib.idfx_gpu_learned_states.argtypes = [P, P]
     lib.idfx_gpu_learned_stats.argtypes = [P, ctypes.POINTER(LL), ctypes.POINTER(LL)]
@@ -157,6 +161,16 @@ def load_library(path=LIB_PATH):
             getattr(lib, f).restype = I
     _lib = lib
     return lib
+
+
+def measure_fp64_peak(stream=None):
+    """measured FP64 FMA throughput of the current GPU, Gop/s"""
+    lib = load_library()
+    g = ctypes.c_double()
+    rc = lib.idfx_measure_fp64_peak(ctypes.byref(g), ctypes.c_void_p(stream))
+    if rc != OK:
+        raise IdefixError(f"idfx_measure_fp64_peak failed with status {rc}")
+    return g.value
 
 
 def make_config(dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm", solver="hlld",
@@ -317,6 +331,15 @@ class GpuBlock:
 
 
     # -- per-kernel timing --------------------------------------------------
+    def autotune(self, reps=3):
+        """pick the march segment length of every sweep direction by timing"""
+        self._check(self.lib.idfx_gpu_autotune(self.h, int(reps)))
+
+    def segments(self):
+        seg = (ctypes.c_int * 3)()
+        self._check(self.lib.idfx_gpu_get_segments(self.h, seg))
+        return list(seg)
+
     def set_learned(self, params, fmin=None, fmax=None):
         """Load the learned-reconstruction network (order "learned")."""
         fp = ctypes.POINTER(ctypes.c_float)

@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libidefix_gb300.so")
 
 SOURCES = ["engine.cu", "sweep_hlld.cu", "sweep_hll.cu", "sweep_roe.cu", "sweep_tvdlf.cu",
-           "noalloc.cu", "ensemble.cu", "learned.cu"]
+           "noalloc.cu", "ensemble.cu", "learned.cu", "peak.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xptxas", "-warn-spills"]

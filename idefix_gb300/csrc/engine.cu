@@ -433,6 +433,75 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   return IDFX_OK;
 }
 
+// Autotuner of the march segment length per direction: the sweeps of each
+// direction are timed alone for every candidate (min over reps launches);
+// they accumulate into Uc, InvDt and the EMF arrays, so the whole field pool
+// and the control block are saved first and put back afterwards.  Results
+// do not depend on the segment length (each face is solved once either way).
+int idfx_gpu_autotune(idfx_gpu* h, int reps) {
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  if (e.g.order == IDFX_LEARNED && !e.learned)
+    return fail(e, IDFX_ERR_STATE, "the learned reconstruction needs idfx_gpu_set_learned first");
+  if (reps < 1) reps = 1;
+  double* backup = nullptr;
+  IDFX_CK(cudaMalloc(&backup, e.pool_len * sizeof(double)));
+  int rc = read_ctl(e);
+  const Ctl saved = *e.ctl_host;
+  if (!rc) rc = cuda_check(e, cudaMemcpyAsync(backup, e.pool, e.pool_len * sizeof(double),
+                                              cudaMemcpyDeviceToDevice, e.stream), "autotune backup");
+  if (!rc) {
+    e.ctl_host->done = 0;
+    rc = cuda_check(e, cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream), "ctl");
+  }
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  const bool prof = e.profile;
+  e.profile = false;
+  if (!rc && e.g.order == IDFX_LEARNED) launch_learned_recon(e);
+  for (int d = 0; d < e.g.D && !rc; d++) {
+    e.only_dir = d;
+    int best = e.seg[d];
+    float best_ms = 1e30f;
+    for (int s = 4; s <= 64 && s <= e.g.n[d]; s *= 2) {
+      e.seg[d] = s;
+      launch_sweeps(e, 2, 0);  // warm-up
+      for (int r = 0; r < reps; r++) {
+        cudaEventRecord(a, e.stream);
+        launch_sweeps(e, 2, 0);
+        cudaEventRecord(b, e.stream);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = s;
+        }
+      }
+    }
+    e.seg[d] = best;
+  }
+  e.only_dir = -1;
+  e.profile = prof;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (!rc) rc = cuda_check(e, cudaGetLastError(), "autotune");
+  cudaMemcpyAsync(e.pool, backup, e.pool_len * sizeof(double), cudaMemcpyDeviceToDevice, e.stream);
+  *e.ctl_host = saved;
+  cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream);
+  const cudaError_t se = cudaStreamSynchronize(e.stream);
+  cudaFree(backup);
+  if (!rc) rc = cuda_check(e, se, "autotune restore");
+  return rc;
+}
+
+int idfx_gpu_get_segments(const idfx_gpu* h, int* seg) {
+  if (!h || !seg) return IDFX_ERR_STATE;
+  for (int d = 0; d < 3; d++) seg[d] = h->e.seg[d];
+  return IDFX_OK;
+}
+
 int idfx_gpu_profile(idfx_gpu* h, int enable) {
   if (!h) return IDFX_ERR_STATE;
   Engine& e = h->e;

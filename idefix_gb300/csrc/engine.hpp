@@ -23,6 +23,7 @@ struct Engine {
   int log_period = 0, check_nan_period = 0;
   long long ncycles = 0;     // host mirror of the cycle counter
   int seg[3] = {32, 32, 32}; // marching segment per direction
+  int only_dir = -1;         // >= 0: sweeps launch that direction alone (autotuner)
   std::string err;
   double* pool = nullptr;    // one allocation for every field
   size_t pool_len = 0;

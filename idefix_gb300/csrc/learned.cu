@@ -202,9 +202,11 @@ __global__ void k_refresh_bf16(const float* __restrict__ w, __nv_bfloat16* __res
 // ---------------------------------------------------------------------------
 // Coarsening of a fine snapshot (ghosted reference layout, 3-D, periodic):
 // conserved averages over r^3 cells, face fields over r^2 faces, cell field
-// from the coarse faces, ConsToPrim; and the face-layer targets: per
-// direction d, the fine primitives averaged over the first and the last
-// fine layer of the coarse cell along d (rotated variable order).
+// from the coarse faces, ConsToPrim; and the face targets: per direction d,
+// the fine primitives extrapolated to the coarse cell's two faces from the
+// two fine layers next to each face (1.5 x outer layer - 0.5 x next layer;
+// the outer layer alone when r = 1), averaged over the face (rotated
+// variable order).
 // One thread per coarse cell.  Outputs (compact, C order z, y, x):
 //   prim[8][nc^3], faces[3][nc^3] (left faces), tgt[3][16][nc^3]
 // ---------------------------------------------------------------------------
@@ -222,6 +224,8 @@ __global__ void k_coarsen(const double* __restrict__ Vc, const double* __restric
   auto fi = [&](int k, int j, int i) { return ((long long)k * ntv + j) * ntv + i; };
   const double g1 = gamma - 1.0;
   double U[5] = {0, 0, 0, 0, 0};
+  // face extrapolation weights of the fine layers along d (offset 0..r-1)
+  const double wo = (r > 1) ? 1.5 : 1.0, wi = (r > 1) ? -0.5 : 0.0;
   double first[3][8], last[3][8];
   for (int d = 0; d < 3; d++)
     for (int n = 0; n < 8; n++) first[d][n] = last[d][n] = 0.0;
@@ -241,10 +245,12 @@ __global__ void k_coarsen(const double* __restrict__ Vc, const double* __restric
         U[4] += V[4] / g1 + 0.5 * V[0] * v2 + 0.5 * b2;
         const int off[3] = {c, b, a};
         for (int d = 0; d < 3; d++) {
-          if (off[d] == 0)
-            for (int n = 0; n < 8; n++) first[d][n] += V[n];
-          if (off[d] == r - 1)
-            for (int n = 0; n < 8; n++) last[d][n] += V[n];
+          const double w0 = (off[d] == 0) ? wo : ((off[d] == 1 && r > 1) ? wi : 0.0);
+          const double w1 = (off[d] == r - 1) ? wo : ((off[d] == r - 2 && r > 1) ? wi : 0.0);
+          if (w0 != 0.0)
+            for (int n = 0; n < 8; n++) first[d][n] += w0 * V[n];
+          if (w1 != 0.0)
+            for (int n = 0; n < 8; n++) last[d][n] += w1 * V[n];
         }
       }
   const double inv3 = 1.0 / ((double)r * r * r), inv2 = 1.0 / ((double)r * r);

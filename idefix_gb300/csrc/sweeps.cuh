@@ -22,9 +22,12 @@ void launch_dir(Engine& e, int invdt, int last) {
 // invdt: 0 none, 1 first contribution of the cycle (InvDt reset), 2 accumulate
 template <int D, int ORDER, int SOLVER, typename T>
 void launch_sweeps_tt(Engine& e, int invdt, int fold_max) {
-  launch_dir<D, 0, ORDER, SOLVER, T>(e, invdt, 0);
-  launch_dir<D, 1, ORDER, SOLVER, T>(e, invdt == 0 ? 0 : 2, fold_max && D == 2);
-  if constexpr (D == 3) launch_dir<D, 2, ORDER, SOLVER, T>(e, invdt == 0 ? 0 : 2, fold_max);
+  // e.only_dir >= 0 (autotuner): that direction alone
+  if (e.only_dir < 0 || e.only_dir == 0) launch_dir<D, 0, ORDER, SOLVER, T>(e, invdt, 0);
+  if (e.only_dir < 0 || e.only_dir == 1)
+    launch_dir<D, 1, ORDER, SOLVER, T>(e, invdt == 0 ? 0 : 2, fold_max && D == 2);
+  if constexpr (D == 3)
+    if (e.only_dir < 0 || e.only_dir == 2) launch_dir<D, 2, ORDER, SOLVER, T>(e, invdt == 0 ? 0 : 2, fold_max);
 }
 
 // precision: FP64 (bit-exact) or mixed (FP32 reconstruction + Riemann)

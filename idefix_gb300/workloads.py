@@ -7,6 +7,11 @@ then on held-out seeds the coarse learned run, the coarse plain run and a
 plain run at twice the coarse resolution are compared with the coarsened
 fine FP64 run at the same end time (L1 error and wall time).
 
+lowbeta: 3-D low-beta (1e-3) box, HLLD + LimO3 + CT, a fixed number of
+cycles in FP64 and in the mixed precision mode (FP32 reconstruction and
+Riemann solve, FP64 state, ConsToPrim and face update) from the same
+initial state; per-variable L1 / Linf differences and div B of both.
+
 ensemble: 512 Orszag-Tang-like 2-D boxes of sizes drawn from
 {64..512}^2 (sonic Mach U[0.5, 2], beta log-U[0.1, 10], seeded), HLLD + PLM
 + CT (uct_contact), RK2, CFL 0.6, FP64, a fixed number of cycles with each
@@ -85,6 +90,54 @@ def run_ensemble(nbox=512, seed=0, cycles=500, sizes=ic.ENSEMBLE_SIZES, check=Tr
     return res
 
 
+VAR3 = ("RHO", "VX1", "VX2", "VX3", "PRS", "BX1", "BX2", "BX3")
+
+
+def run_lowbeta(n=384, cycles=200, seed=0, cfl=0.6, log=sys.stderr):
+    import torch
+
+    Vc, Vs = ic.low_beta_3d(n, seed=seed)
+    res = {"n": n, "cycles": cycles, "seed": seed, "cfl": cfl, "scheme": "HLLD + LimO3 + uct_contact, RK2"}
+    out = {}
+    g = 2
+    a = slice(g, g + n)
+    for prec in ("fp64", "mixed"):
+        blk = ig.GpuBlock(3, (n, n, n), order="limo3", cfl=cfl, first_dt=1e-4, precision=prec)
+        blk.upload(Vc, Vs)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        blk.run(max_cycles=cycles)
+        torch.cuda.synchronize()
+        res[prec + "_s"] = time.perf_counter() - t0
+        res[prec + "_zone_cycles_per_s"] = n**3 * cycles / res[prec + "_s"]
+        res[prec + "_divb"] = blk.check_divb()
+        t, dt, nc = blk.get_time()
+        res[prec + "_t"] = t
+        vc, vs = blk.download()
+        out[prec] = (vc[:, a, a, a].copy(), vs)
+        blk.close()
+        if log:
+            print(f"{prec}: {res[prec + '_s']:.2f} s, t = {t}", file=log, flush=True)
+    err = {}
+    for v, name in enumerate(VAR3):
+        x, y = out["mixed"][0][v], out["fp64"][0][v]
+        d = np.abs(x - y)
+        err[name] = {"l1": float(d.sum() / max(np.abs(y).sum(), 1e-300)),
+                     "linf": float(d.max() / max(np.abs(y).max(), 1e-300))}
+    fs = [(out["mixed"][1][d], out["fp64"][1][d]) for d in range(3)]
+    res["face_field_linf"] = float(max(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300) for x, y in fs))
+    res["errors_mixed_vs_fp64"] = err
+    res["speedup_mixed"] = res["fp64_s"] / res["mixed_s"]
+    return res
+
+
+OW3 = 216 * 128 + 128 + 128 * 128 + 128  # offset of W3 (then b3) in the packed parameters
+
+
+def _l1_vars(a, b):
+    return [float(np.abs(a[v] - b[v]).sum() / max(np.abs(b[v]).sum(), 1e-300)) for v in range(8)]
+
+
 def _l1(a, b):
     """mean over the 8 variables of sum|a - b| / sum|b| (compact prim arrays)"""
     return float(np.mean([np.abs(a[v] - b[v]).sum() / max(np.abs(b[v]).sum(), 1e-300) for v in range(8)]))
@@ -109,73 +162,96 @@ def _coarse_of(Vc, Vs, n, r, learned):
 
 def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=(200, 201, 202, 203),
                 nsnap=50, t_end=1.0, steps=3000, batch=8192, lr=2e-3, lr_end=2e-5,
-                train_precision="mixed", log=sys.stderr):
+                train_precision="mixed", kmax=None, params=None, alphas=(1.0,), log=sys.stderr):
+    """kmax: largest wavenumber of the initial fields; by default 8 x n_fine
+    / 512, i.e. the spectrum of the 512^3 fine run scaled with the grid, so
+    that the coarse grid resolves it as the 128^3 coarse grid of the
+    512^3 run would.  params: (params, fmin, fmax) of a trained network, which
+    skips data generation and training.  alphas: scale factors of the
+    network's correction evaluated on the held-out seeds (the output layer
+    is linear, so alpha scales W3 and b3)."""
     import torch
 
     from idefix_gb300 import learned
 
     nc = n_fine // r
+    if kmax is None:
+        kmax = max(1, int(round(8 * n_fine / 512)))
     res = {"n_fine": n_fine, "n_coarse": nc, "t_end": t_end, "train_runs": len(train_seeds), "snapshots": nsnap,
-           "train_precision": train_precision}
-    # 1. training snapshots through the ensemble path
-    boxes = [dict(dims=3, n=(n_fine,) * 3, cfl=0.6, first_dt=1e-4, precision=train_precision)
-             for _ in train_seeds]
-    ens = ig.Ensemble(boxes)
-    shp_c, shp_s = ens.shapes[0]
-    for k, s in enumerate(train_seeds):
-        Vc, Vs = ic.turbulence_3d(n_fine, seed=s)
-        ens.upload(k, Vc, Vs)
-    S = len(train_seeds) * nsnap
-    prims = torch.empty((S, 8, nc, nc, nc), dtype=torch.float32, device="cuda")
-    tgts = torch.empty((S, 3, 16, nc**3), dtype=torch.float32, device="cuda")
-    vc_buf = torch.empty(shp_c, dtype=torch.float64, device="cuda")
-    vs_buf = torch.empty(shp_s, dtype=torch.float64, device="cuda")
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for j in range(nsnap):
-        ens.run(tstop=t_end * (j + 1) / nsnap)
-        for k in range(len(train_seeds)):
-            ens.download_device(k, vc_buf.data_ptr(), vs_buf.data_ptr())
-            p, _, tg = learned.coarsen(vc_buf, vs_buf, n_fine, 2, r)
-            prims[k * nsnap + j] = p.float()
-            tgts[k * nsnap + j] = tg.float()
-        if log:
-            print(f"snapshot {j + 1}/{nsnap}", file=log, flush=True)
-    torch.cuda.synchronize()
-    res["data_s"] = time.perf_counter() - t0
-    res["train_cycles"] = ens.get_time(0)[2]
-    ens.close()
-    del vc_buf, vs_buf
-    # 2. training with the library's BF16 tensor-core kernels
-    tr = learned.Trainer(max_batch=batch)
-    tr.set_dataset(prims, tgts)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    losses = tr.train(steps, batch, lr=lr, lr_end=lr_end, seed=7)
-    torch.cuda.synchronize()
-    res["train_s"] = time.perf_counter() - t0
-    res["loss_first"] = float(losses[:10].mean())
-    res["loss_last"] = float(losses[-50:].mean())
-    params = tr.get_params()
-    fmin, fmax = tr.feature_range()
-    del prims, tgts
+           "train_precision": train_precision, "kmax": kmax, "steps": steps, "batch": batch}
+    tr = None
+    if params is None:
+        # 1. training snapshots through the ensemble path
+        boxes = [dict(dims=3, n=(n_fine,) * 3, cfl=0.6, first_dt=1e-4, precision=train_precision)
+                 for _ in train_seeds]
+        ens = ig.Ensemble(boxes)
+        shp_c, shp_s = ens.shapes[0]
+        for k, s in enumerate(train_seeds):
+            Vc, Vs = ic.turbulence_3d(n_fine, seed=s, kmax=kmax)
+            ens.upload(k, Vc, Vs)
+        S = len(train_seeds) * nsnap
+        prims = torch.empty((S, 8, nc, nc, nc), dtype=torch.float32, device="cuda")
+        tgts = torch.empty((S, 3, 16, nc**3), dtype=torch.float32, device="cuda")
+        vc_buf = torch.empty(shp_c, dtype=torch.float64, device="cuda")
+        vs_buf = torch.empty(shp_s, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for j in range(nsnap):
+            ens.run(tstop=t_end * (j + 1) / nsnap)
+            for k in range(len(train_seeds)):
+                ens.download_device(k, vc_buf.data_ptr(), vs_buf.data_ptr())
+                p, _, tg = learned.coarsen(vc_buf, vs_buf, n_fine, 2, r)
+                prims[k * nsnap + j] = p.float()
+                tgts[k * nsnap + j] = tg.float()
+            if log:
+                print(f"snapshot {j + 1}/{nsnap}", file=log, flush=True)
+        torch.cuda.synchronize()
+        res["data_s"] = time.perf_counter() - t0
+        res["train_cycles"] = ens.get_time(0)[2]
+        ens.close()
+        del vc_buf, vs_buf
+        # 2. training with the library's BF16 tensor-core kernels
+        tr = learned.Trainer(max_batch=batch)
+        tr.set_dataset(prims, tgts)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        losses = tr.train(steps, batch, lr=lr, lr_end=lr_end, seed=7)
+        torch.cuda.synchronize()
+        res["train_s"] = time.perf_counter() - t0
+        res["loss_first"] = float(losses[:10].mean())
+        res["loss_last"] = float(losses[-50:].mean())
+        params = tr.get_params()
+        fmin, fmax = tr.feature_range()
+        del prims, tgts
+    else:
+        params, fmin, fmax = params
+        tr = learned.Trainer(max_batch=batch, params=params)
     # 3. held-out seeds: errors against the coarsened fine FP64 run
     rows = []
+    held_p, held_t = [], []
     for s in eval_seeds:
-        Vc, Vs = ic.turbulence_3d(n_fine, seed=s)
+        Vc, Vs = ic.turbulence_3d(n_fine, seed=s, kmax=kmax)
         fine = ig.GpuBlock(3, (n_fine,) * 3, cfl=0.6, first_dt=1e-4)
         fine.upload(Vc, Vs)
         t_fine = _timed_run(fine, t_end)
-        ref, _ = _coarse_of(*fine.download(), n_fine, r, learned)
-        ref = ref.cpu().numpy()
+        fv = fine.download()
+        ref_d, _, tg_d = learned.coarsen(torch.from_numpy(fv[0]).cuda(), torch.from_numpy(fv[1]).cuda(), n_fine, 2, r)
+        held_p.append(ref_d.float())
+        held_t.append(tg_d.float())
+        ref = ref_d.cpu().numpy()
         fine.close()
         row = {"seed": s, "fine_s": t_fine}
-        for name, order, nres in (("plain", "plm", nc), ("learned", "learned", nc), ("plain_2x", "plm", 2 * nc)):
+        runs = [("plain", "plm", nc, 0.0)]
+        runs += [("learned" if a == alphas[0] else f"learned_a{a:g}", "learned", nc, a) for a in alphas]
+        runs += [("plain_2x", "plm", 2 * nc, 0.0)]
+        for name, order, nres, alpha in runs:
             pc, fc = _coarse_of(Vc, Vs, n_fine, n_fine // nres, learned)
             Vcc, Vsc = learned.coarse_state(pc, fc)
             blk = ig.GpuBlock(3, (nres,) * 3, order=order, cfl=0.6, first_dt=1e-4)
             if order == "learned":
-                blk.set_learned(params, fmin, fmax)
+                pa = np.array(params, dtype=np.float32, copy=True)
+                pa[OW3:] *= alpha
+                blk.set_learned(pa, fmin, fmax)
             blk.upload(Vcc, Vsc)
             row[name + "_s"] = _timed_run(blk, t_end)
             out, _ = _coarse_of(*blk.download(), nres, nres // nc, learned) if nres != nc else (None, None)
@@ -184,6 +260,7 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
             else:
                 vc_out = out.cpu().numpy()
             row[name + "_l1"] = _l1(vc_out, ref)
+            row[name + "_l1_vars"] = _l1_vars(vc_out, ref)
             if order == "learned":
                 cells, fall = blk.learned_stats()
                 row["fallback_rate"] = fall / max(cells, 1)
@@ -192,8 +269,12 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
         if log:
             print(json.dumps(row), file=log, flush=True)
     res["eval"] = rows
-    for k in ("plain_l1", "learned_l1", "plain_2x_l1", "fine_s", "learned_s", "plain_s", "fallback_rate"):
-        res[k] = float(np.mean([row[k] for row in rows]))
+    # supervised loss on the held-out final snapshots, with and without the network
+    tr.set_dataset(torch.stack(held_p).contiguous(), torch.stack(held_t).contiguous())
+    res["heldout_loss"], res["heldout_loss_plm"] = tr.eval(batch, seed=4242)
+    for k in rows[0]:
+        if k != "seed" and not k.endswith("_vars"):
+            res[k] = float(np.mean([row[k] for row in rows]))
     res["learned_over_plain_2x_l1"] = res["learned_l1"] / res["plain_2x_l1"]
     res["fine_over_learned_time"] = res["fine_s"] / res["learned_s"]
     return res, params, fmin, fmax
@@ -203,7 +284,8 @@ if __name__ == "__main__":
     import argparse
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["ensemble", "learned"], default="ensemble")
+    ap.add_argument("--workload", choices=["ensemble", "learned", "lowbeta"], default="ensemble")
+    ap.add_argument("--n", type=int, default=384)
     ap.add_argument("--nbox", type=int, default=512)
     ap.add_argument("--n-fine", type=int, default=128)
     ap.add_argument("--train-runs", type=int, default=40)
@@ -211,16 +293,25 @@ if __name__ == "__main__":
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--save", default=None, help="npz file for the trained parameters and range")
+    ap.add_argument("--load", default=None, help="npz file of a trained network (skips training)")
+    ap.add_argument("--alphas", default="1.0", help="comma-separated correction scale factors")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--cycles", type=int, default=500)
+    ap.add_argument("--cycles", type=int, default=None, help="default: 500 (ensemble), 200 (lowbeta)")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     a = ap.parse_args()
     if a.workload == "ensemble":
-        r = run_ensemble(a.nbox, a.seed, a.cycles, check=not a.no_check, graph=not a.no_graph)
+        r = run_ensemble(a.nbox, a.seed, a.cycles or 500, check=not a.no_check, graph=not a.no_graph)
+    elif a.workload == "lowbeta":
+        r = run_lowbeta(a.n, a.cycles or 200, a.seed)
     else:
+        pre = None
+        if a.load:
+            z = np.load(a.load)
+            pre = (z["params"], z["fmin"], z["fmax"])
         r, params, fmin, fmax = run_learned(a.n_fine, train_seeds=tuple(range(100, 100 + a.train_runs)),
-                                            nsnap=a.snapshots, t_end=a.t_end, steps=a.steps)
+                                            nsnap=a.snapshots, t_end=a.t_end, steps=a.steps, params=pre,
+                                            alphas=tuple(float(x) for x in a.alphas.split(",")))
         if a.save:
             np.savez(a.save, params=params, fmin=fmin, fmax=fmax)
     print(json.dumps(r))

@@ -143,6 +143,15 @@ enum {
 };
 int idfx_gpu_profile(idfx_gpu* h, int enable);
 int idfx_gpu_profile_read(idfx_gpu* h, double* ms, long long* launches, int nclasses);
+/* Autotuner (no counterpart in the reference): picks, per sweep direction,
+ * the march segment length (cells per thread along the sweep) of the fastest
+ * sweep, timed over reps launches; the state is saved and restored, and the
+ * results do not depend on the choice.  get_segments reads the choice. */
+int idfx_gpu_autotune(idfx_gpu* h, int reps);
+int idfx_gpu_get_segments(const idfx_gpu* h, int* seg);
+/* measured FP64 FMA throughput of the current device (thread operations
+ * per second / 1e9), the roof of the FP64-bound sweeps; stream may be NULL */
+int idfx_measure_fp64_peak(double* gops, void* stream);
 
 /* Allocation-free Fluid::EvolveStage — no counterpart in the reference.
  * For callers that may not allocate GPU memory while they step (state held

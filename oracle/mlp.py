@@ -15,8 +15,9 @@ in float64:
 * MLP 216 -> 128 -> 128 -> 16, SiLU, outputs = normalised corrections of
   the cell's minus-face and plus-face states (8 + 8, rotated frame), scaled
   back with the same factors;
-* training target: the mean of the fine-grid primitives over the fine-cell
-  layer adjacent to each coarse face, minus the coarse PLM (van Leer) state;
+* training target: the fine-grid primitives extrapolated to each coarse
+  face from the two fine layers next to it (1.5 x outer - 0.5 x next),
+  averaged over the face, minus the coarse PLM (van Leer) state;
   the normal field component (taken from the face field by the solver) is
   masked out of the loss;
 * coarse state of a fine snapshot: conserved variables averaged over the
@@ -205,20 +206,27 @@ def plm_states(prim, d):
 
 def face_layers(fine_prim, r):
     """fine prim[8, nf, nf, nf] -> raw face targets [3, 16, nc^3]: for each
-    direction d, the mean of the fine primitives over the first and the last
-    fine layer of every coarse cell along d (rotated variable order)"""
+    direction d, the fine primitives extrapolated to the two faces of every
+    coarse cell along d from the two fine layers next to each face
+    (1.5 x outer - 0.5 x next; the outer layer alone when r = 1), averaged
+    over the face (rotated variable order)"""
     nf = fine_prim.shape[1]
     nc = nf // r
     out = np.zeros((3, 16, nc**3))
     blk = fine_prim.reshape(NVAR, nc, r, nc, r, nc, r)  # var, kz, z, jy, y, ix, x
     for d in range(3):
         ax = {0: 6, 1: 4, 2: 2}[d]  # fine-offset axis of direction d
-        first = np.take(blk, 0, axis=ax)
-        last = np.take(blk, r - 1, axis=ax)
         other = [a for a in (2, 4, 6) if a != ax]
         red = tuple(o - (1 if o > ax else 0) for o in other)
-        mf = first.mean(axis=red)
-        ml = last.mean(axis=red)
+
+        def layer(i):
+            return np.take(blk, i, axis=ax).mean(axis=red)
+
+        if r > 1:
+            mf = 1.5 * layer(0) - 0.5 * layer(1)
+            ml = 1.5 * layer(r - 1) - 0.5 * layer(r - 2)
+        else:
+            mf = ml = layer(0)
         out[d, :8] = _rotate_vars(mf, d).reshape(NVAR, -1)
         out[d, 8:] = _rotate_vars(ml, d).reshape(NVAR, -1)
     return out

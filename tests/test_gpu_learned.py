@@ -222,6 +222,7 @@ def test_learned_run_keeps_div_b_and_conservation():
     params = mlp.init_params(7, out_scale=0.05).astype(np.float32)
     blk = _learned_block(n, params)
     blk.upload(Vc, Vs)
+    blk.set_boundaries()
     blk.prim_to_cons()
     u0 = blk.download_cons()
     blk.run(max_cycles=6)

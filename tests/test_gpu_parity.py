@@ -257,3 +257,25 @@ def test_gpu_turbulence_256_cube_properties():
         s1 = np.sum(U1[q][act])
         scale = np.sum(np.abs(U0[q][act]))
         assert abs(s1 - s0) <= 1e-12 * scale, (q, s0, s1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_autotuned_segments_keep_results(precision):
+    """the march segment length changes the launch shape only"""
+    n = (24, 20, 16)
+    Vc, Vs = ic.turbulence_3d(24, seed=9, kmax=4)
+    Vc = np.ascontiguousarray(Vc[:, : n[2] + 4, : n[1] + 4, :])
+    Vs = np.ascontiguousarray(Vs[:, : n[2] + 5, : n[1] + 5, :])
+    out = []
+    for tune in (False, True):
+        blk = ig.GpuBlock(3, n, cfl=0.6, first_dt=1e-4, precision=precision)
+        blk.upload(Vc, Vs)
+        if tune:
+            blk.autotune(2)
+            assert all(s in (4, 8, 16, 32, 64) for s in blk.segments())
+        blk.run(max_cycles=3)
+        out.append((blk.download(), blk.get_time()))
+        blk.close()
+    (a, ta), (b, tb) = out
+    assert ta == tb
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])

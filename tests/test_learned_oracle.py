@@ -95,13 +95,20 @@ def test_features_and_plm_known_answers():
     assert np.allclose(vp[0].reshape(n, n, n)[:, :, 1:-1], (1.0 + 0.1 * np.arange(1, n - 1) + 0.05)[None, None, :])
 
 
-def test_face_layers_of_uniform_blocks():
-    r, nc = 2, 3
-    fine = np.zeros((8, nc * r, nc * r, nc * r))
-    for v in range(8):
-        fine[v] = np.arange((nc * r) ** 3).reshape(nc * r, nc * r, nc * r) * (v + 1)
+def test_face_targets_are_exact_for_linear_profiles():
+    # a field linear in x: the extrapolation from the two fine layers next
+    # to a coarse face gives the field's value on that face
+    r, nc = 4, 3
+    nf = nc * r
+    x = (np.arange(nf) + 0.5) / nf
+    fine = np.ones((8, nf, nf, nf))
+    fine[0] = 2.0 + 3.0 * x[None, None, :]
     t = mlp.face_layers(fine, r)
-    # x first layer of coarse cell (0,0,0): fine x index 0, y, z in {0,1}
-    idx = np.array([[0, 0, 0], [0, 1, 0], [1, 0, 0], [1, 1, 0]])
-    vals = [fine[0][z, y, x] for z, y, x in idx]
-    assert np.isclose(t[0, 0, 0], np.mean(vals))
+    faces = np.arange(nc + 1) / nc
+    got_left = t[0, 0].reshape(nc, nc, nc)[0, 0, :]
+    got_right = t[0, 8].reshape(nc, nc, nc)[0, 0, :]
+    assert np.allclose(got_left, 2.0 + 3.0 * faces[:-1])
+    assert np.allclose(got_right, 2.0 + 3.0 * faces[1:])
+    # r = 1: the cell values themselves
+    t1 = mlp.face_layers(fine[:, :3, :3, :3], 1)
+    assert np.allclose(t1[0, 0], fine[0, :3, :3, :3].ravel())
