@@ -31,6 +31,13 @@ METRIC = "zone-cycles/s (256^3 MHD)"
 UNIT = "zone-cycles/s"
 H100_PUBLISHED = 3.079643e8  # doc/source/bench.json:84-90 (128^3 per GPU, FP64, H100)
 BYTES_PER_ZONE_CYCLE = 320.0  # 8 FP64 state values x 5 transfers per RK2 cycle
+# FP64 thread instructions (dadd + dmul + dfma + the rest of the FP64 pipe,
+# predicated on) per active cell of one sweep launch, and DRAM bytes per
+# active cell of one sweep launch: ncu on the 128^3 case of this workload
+# (stage 0; profiles/sweep_fp64_hlld_plm_turb3d_128.md).  Both scale with the
+# cells processed; at 256^3 the CT-extension columns add 1.6 % instead of 3.1 %.
+FP64_INST_PER_CELL = {"sweep_x": 640.0, "sweep_y": 638.0, "sweep_z": 633.0}
+DRAM_BYTES_PER_CELL = {"sweep_x": 193.1, "sweep_y": 173.2, "sweep_z": 171.6}
 
 
 def parse():
@@ -117,7 +124,7 @@ def dist_setup():
     return world, rank, local
 
 
-def cpu_baseline(size=128, cycles=24, seed=1):
+def cpu_baseline(size=128, cycles=12, seed=1):
     """the CPU path (oracle restatement, OpenMP on every host core) on a
     bounded sample: a size^3 box of the same workload for `cycles` cycles"""
     from idefix_gb300 import build, ic
@@ -263,6 +270,17 @@ def run_ours(args, world, rank, local):
     dom_avg_s = dom_ms / max(dom_n, 1) * 1e-3
     achieved_gbs = sweep_bytes_per_cell * cells / dom_avg_s / 1e9 if dom in sweep_classes else None
     cycle_gbs = BYTES_PER_ZONE_CYCLE * cells / (ms_step * 1e-3) / 1e9
+    traffic = DRAM_BYTES_PER_CELL[dom] * cells if dom in DRAM_BYTES_PER_CELL else None
+    # the binding roof: FP64 issue of the dominant sweep against the DFMA
+    # throughput measured on this GPU in this run
+    fp64_peak = ig.measure_fp64_peak(stream.cuda_stream)
+    fp64_roof = None
+    if dom in FP64_INST_PER_CELL and args.precision == "fp64":
+        ach = FP64_INST_PER_CELL[dom] * cells / dom_avg_s / 1e9
+        fp64_roof = {"achieved": ach, "peak": fp64_peak, "unit": "G FP64 thread-op/s", "frac": ach / fp64_peak,
+                     "kernel": dom, "inst_per_cell": FP64_INST_PER_CELL[dom],
+                     "peak_kind": "measured in this run (DFMA, idfx_measure_fp64_peak)",
+                     "inst_source": "ncu FP64-pipe thread instructions per active cell, 128^3 stage-0 sweep"}
 
     out = None
     if rank == 0:
@@ -283,9 +301,12 @@ def run_ours(args, world, rank, local):
             "gpu_launches": gpu_launches,
             "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                          "frac": (achieved_gbs / hbm_peak) if achieved_gbs else None,
-                         "traffic": None, "kernel": dom, "peak_kind": peak_kind,
+                         "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
                          "bytes_per_cell": sweep_bytes_per_cell,
-                         "note": "FP64-issue bound (GB300 FP64 ~1.2 TFLOP/s); see fp64 fields"},
+                         "traffic_note": "ncu dram read+write per active cell of the 128^3 sweep x 256^3 cells",
+                         "note": "FP64-issue bound (GB300 FP64 ~1.2 TFLOP/s): see fp64_roofline"},
+            "fp64_roofline": fp64_roof,
+            "segments": blk.segments(),
             "cycle_hbm": {"achieved": cycle_gbs, "unit": "GB/s", "frac": cycle_gbs / hbm_peak,
                           "bytes_per_zone_cycle": BYTES_PER_ZONE_CYCLE},
             "kernel_ms_per_cycle": {k: v[0] / prof_cycles for k, v in prof.items() if v[1]},

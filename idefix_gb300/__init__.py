@@ -78,7 +78,7 @@ EXPORTS = [
     "idfx_mlp_set_params", "idfx_mlp_get_params", "idfx_mlp_set_dataset_device", "idfx_mlp_train",
     "idfx_mlp_eval", "idfx_mlp_feature_range", "idfx_mlp_batch_device", "idfx_mlp_grad_device",
     "idfx_mlp_forward_device", "idfx_learn_coarsen_device", "idfx_measure_fp64_peak",
-    "idfx_gpu_autotune", "idfx_gpu_get_segments",
+    "idfx_gpu_autotune", "idfx_gpu_get_segments", "idfx_gpu_set_segments", "idfx_check_division",
 ]
 
 KERNEL_CLASSES = ["fill_faces", "stage_begin", "sweep_x", "sweep_y", "sweep_z", "ct_corner",
@@ -140,7 +140,9 @@ def load_library(path=LIB_PATH):
     U64 = ctypes.c_ulonglong
     lib.idfx_measure_fp64_peak.argtypes = [dp, P]
     lib.idfx_gpu_autotune.argtypes = [P, I]
+    lib.idfx_check_division.argtypes = [LL, ctypes.c_ulonglong, ctypes.POINTER(LL)]
     lib.idfx_gpu_get_segments.argtypes = [P, ctypes.POINTER(I)]
+    lib.idfx_gpu_set_segments.argtypes = [P, ctypes.POINTER(I)]
     lib.idfx_gpu_set_learned.argtypes = [P, fp, fp, fp]
     lib.idfx_gpu_learned_states.argtypes = [P, P]
     lib.idfx_gpu_learned_stats.argtypes = [P, ctypes.POINTER(LL), ctypes.POINTER(LL)]
@@ -339,6 +341,10 @@ class GpuBlock:
         seg = (ctypes.c_int * 3)()
         self._check(self.lib.idfx_gpu_get_segments(self.h, seg))
         return list(seg)
+
+    def set_segments(self, seg):
+        s = (ctypes.c_int * 3)(*(list(seg) + [1] * (3 - len(seg))))
+        self._check(self.lib.idfx_gpu_set_segments(self.h, s))
 
     def set_learned(self, params, fmin=None, fmax=None):
         """Load the learned-reconstruction network (order "learned")."""

@@ -79,7 +79,7 @@ __global__ void k_prim_to_cons_all(Geo g, Fields f) {
   if (c >= g.ncell) return;
   double V[v::NV], U[v::NV];
   for (int n = 0; n < v::NV; n++) V[n] = f.Vc[n * g.ncell + c];
-  prim_to_cons<D>(g.gm1, U, V);
+  prim_to_cons<D, true>(g.gm1, U, V);
   for (int n = 0; n < v::NV; n++) f.Uc[n * g.ncell + c] = U[n];
 }
 
@@ -103,7 +103,7 @@ __global__ void k_uc_field_all(Geo g, Fields f, int to_prim) {
     f.Uc[(v::BX1 + d) * g.ncell + c] = U[v::BX1 + d];
   }
   if (!to_prim) return;
-  cons_to_prim<D>(g.gm1, V, U);
+  cons_to_prim<D, true>(g.gm1, V, U);
   for (int n = 0; n < v::NV; n++) f.Vc[n * g.ncell + c] = V[n];
 }
 
@@ -120,6 +120,14 @@ __global__ void k_cell_emf_all(Geo g, Fields f) {
     f.Ex2[c] = (vx1 * Bx3 - vx3 * Bx1);
   }
   f.Ex3[c] = (vx2 * Bx1 - vx1 * Bx2);
+}
+
+// FP32 copy of the primitives for the mixed-precision sweeps (the building
+// blocks run the sweeps without a stage begin)
+__global__ void k_vc32(Geo g, Fields f, int nv) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.ncell) return;
+  for (int n = 0; n < nv; n++) f.Vc32[n * g.ncell + c] = (float)f.Vc[n * g.ncell + c];
 }
 
 template <int D>
@@ -376,7 +384,8 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   size_t len = 3 * NV * nc + 2 * g.D * nf + nc  // Vc, Uc, Uc0, Vs, Vs0, InvDt
                + 6 * nc + 3 * nc + 3 * nc + 3 * nc  // face EMFs, sv, cell EMFs, corner EMFs
                + (hll_emf ? 12 * nc : 0)
-               + (g.order == IDFX_LEARNED ? 48 * nc : 0);  // learned face states
+               + (g.order == IDFX_LEARNED ? 48 * nc : 0)   // learned face states
+               + (cfg->precision == IDFX_MIXED ? (NV * nc + 1) / 2 : 0);  // FP32 primitives
   int rc = IDFX_OK;
   if (stream) {
     e.stream = (cudaStream_t)stream;
@@ -414,6 +423,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
     f.dR[d] = hll_emf ? take(nc) : nullptr;
   }
   f.ls = (g.order == IDFX_LEARNED) ? take(48 * nc) : nullptr;
+  f.Vc32 = (cfg->precision == IDFX_MIXED) ? reinterpret_cast<float*>(take((NV * nc + 1) / 2)) : nullptr;
   Ctl c{};
   c.t = 0.0;
   c.dt = cfg->first_dt;
@@ -494,6 +504,14 @@ int idfx_gpu_autotune(idfx_gpu* h, int reps) {
   cudaFree(backup);
   if (!rc) rc = cuda_check(e, se, "autotune restore");
   return rc;
+}
+
+int idfx_gpu_set_segments(idfx_gpu* h, const int* seg) {
+  if (!h || !seg) return IDFX_ERR_STATE;
+  for (int d = 0; d < h->e.g.D; d++)
+    if (seg[d] < 1 || seg[d] > 1024) return IDFX_ERR_CONFIG;
+  for (int d = 0; d < h->e.g.D; d++) h->e.seg[d] = seg[d];
+  return IDFX_OK;
 }
 
 int idfx_gpu_get_segments(const idfx_gpu* h, int* seg) {
@@ -726,6 +744,7 @@ int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt) {
   if (e.g.order == IDFX_LEARNED && !e.learned)
     return fail(e, IDFX_ERR_STATE, "the learned reconstruction needs idfx_gpu_set_learned first");
   k_set_stage_dt<<<1, 1, 0, e.stream>>>(e.g, e.ctl, dt);
+  if (e.f.Vc32) k_vc32<<<nblocks(e.g.ncell), kThreads, 0, e.stream>>>(e.g, e.f, 2 * e.g.D + 2);
   if (e.g.order == IDFX_LEARNED) launch_learned_recon(e);
   if (e.g.emf == kEmfContact || e.g.emf == kEmfUct0)
     IDFX_DISPATCH_D(k_cell_emf_all, nblocks(e.g.ncell), kThreads, e.g, e.f);

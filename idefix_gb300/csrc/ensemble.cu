@@ -485,7 +485,8 @@ int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_en
     Geo& g = e.boxes[b].g;
     box_geometry(&cfgs[b], g);
     const size_t nc = up32((size_t)g.ncell), nf = up32((size_t)g.nface);
-    box_len[b] = 3 * NV * nc + 2 * g.D * nf + nc + 15 * nc + (hll_emf ? 12 * nc : 0);
+    box_len[b] = 3 * NV * nc + 2 * g.D * nf + nc + 15 * nc + (hll_emf ? 12 * nc : 0) +
+                 (e.precision == IDFX_MIXED ? up32((NV * nc + 1) / 2) : 0);  // FP32 primitives
     len += box_len[b];
   }
   int rc = IDFX_OK;
@@ -536,6 +537,7 @@ int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_en
       f.dL[d] = hll_emf ? take(nc) : nullptr;
       f.dR[d] = hll_emf ? take(nc) : nullptr;
     }
+    f.Vc32 = (e.precision == IDFX_MIXED) ? reinterpret_cast<float*>(take(up32((NV * nc + 1) / 2))) : nullptr;
     B.ctl = e.d_ctl + b;
     for (int d = 0; d < 3; d++) B.seg[d] = d < e.D ? default_seg(g, d, sms) : 1;
     Ctl c{};

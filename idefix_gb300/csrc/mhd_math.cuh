@@ -15,6 +15,8 @@
 #pragma once
 #include <cstdint>
 
+#include "intdiv.cuh"
+
 namespace idfx {
 
 template <int D>
@@ -46,6 +48,19 @@ __device__ __forceinline__ T dv(T a, T b) {
   return a / b;
 }
 
+// the same quotient computed on the integer pipe for FP64 (intdiv.cuh): used
+// by the memory-bound whole-array kernels (cons <-> prim), where it takes the
+// division off the FP64 pipe; the sweeps keep the hardware sequence, whose
+// shorter dependency chain suits their low occupancy
+template <typename T>
+__device__ __forceinline__ T dvi(T a, T b) {
+  if constexpr (sizeof(T) == 8) {
+    return div_rn(a, b);
+  } else {
+    return a / b;
+  }
+}
+
 // sum of squares of the first D entries, in reference order
 template <int D, typename T>
 __device__ __forceinline__ T sumsq(T a, T b, T c) {
@@ -58,7 +73,8 @@ __device__ __forceinline__ T sumsq(T a, T b, T c) {
 // cons <-> prim (convertConsToPrim.hpp:15-100; eos_adiabatic.hpp:38-45)
 // gm1 = gamma - 1.0, evaluated once on the host
 // ---------------------------------------------------------------------------
-template <int D, typename T>
+// INTDIV: quotients on the integer pipe (whole-array kernels)
+template <int D, bool INTDIV = false, typename T>
 __device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V) {
   using v = Var<D>;
   U[v::RHO] = V[v::RHO];
@@ -77,16 +93,17 @@ __device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V) {
     kin = sumsq<2>(V[v::MX1], V[v::MX2], z);
     mag = sumsq<2>(U[v::BX1], U[v::BX2], z);
   }
-  U[v::ENG] = dv(V[v::PRS], gm1) + T(0.5) * V[v::RHO] * kin + T(0.5) * mag;
+  U[v::ENG] = (INTDIV ? dvi(V[v::PRS], gm1) : dv(V[v::PRS], gm1)) + T(0.5) * V[v::RHO] * kin + T(0.5) * mag;
 }
 
-template <int D, typename T>
+template <int D, bool INTDIV = false, typename T>
 __device__ __forceinline__ void cons_to_prim(T gm1, T* V, const T* U) {
   using v = Var<D>;
+  auto q = [](T a, T b) { return INTDIV ? dvi(a, b) : dv(a, b); };
   V[v::RHO] = U[v::RHO];
-  V[v::MX1] = dv(U[v::MX1], U[v::RHO]);
-  V[v::MX2] = dv(U[v::MX2], U[v::RHO]);
-  if constexpr (D == 3) V[v::MX3] = dv(U[v::MX3], U[v::RHO]);
+  V[v::MX1] = q(U[v::MX1], U[v::RHO]);
+  V[v::MX2] = q(U[v::MX2], U[v::RHO]);
+  if constexpr (D == 3) V[v::MX3] = q(U[v::MX3], U[v::RHO]);
   V[v::BX1] = U[v::BX1];
   V[v::BX2] = U[v::BX2];
   if constexpr (D == 3) V[v::BX3] = U[v::BX3];
@@ -99,7 +116,7 @@ __device__ __forceinline__ void cons_to_prim(T gm1, T* V, const T* U) {
     m2 = sumsq<2>(U[v::MX1], U[v::MX2], z);
     b2 = sumsq<2>(U[v::BX1], U[v::BX2], z);
   }
-  const T kin = dv(T(0.5), U[v::RHO]) * m2;
+  const T kin = q(T(0.5), U[v::RHO]) * m2;
   const T mag = T(0.5) * b2;
   V[v::PRS] = (U[v::ENG] - kin - mag) * gm1;
   // floor; the reference's energy repair only touches a discarded local copy

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/idefix_gb300.h"
+#include "intdiv.cuh"
 
 namespace {
 
@@ -23,7 +24,53 @@ __global__ void k_dfma_peak(double* out, int iters, double a, double b) {
   if (s == 12345.678) out[0] = s;  // keeps the chains live
 }
 
+__device__ __forceinline__ unsigned long long mix(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// random operand pairs: full normal range, a moderate range, significands
+// near 1 and 2, and quotients at the edges of the normal range
+__global__ void k_check_division(long long n, unsigned long long seed, unsigned long long* bad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long h1 = mix(seed ^ (2 * i)), h2 = mix(seed ^ (2 * i + 1)), h3 = mix(h1 ^ h2);
+  const unsigned long long M = (1ull << 52) - 1;
+  unsigned long long ea, eb, ma = h1 & M, mb = h2 & M;
+  switch (h3 % 4) {
+    case 0: ea = 1 + (h1 >> 53) % 2046; eb = 1 + (h2 >> 53) % 2046; break;
+    case 1: ea = 900 + (h1 >> 53) % 250; eb = 900 + (h2 >> 53) % 250; break;
+    case 2:
+      ea = 1000 + (h1 >> 58) % 40;
+      eb = 1000 + (h2 >> 58) % 40;
+      if (h3 & 16) mb = (h3 & 32) ? (h2 >> 40) : M - (h2 >> 40);
+      if (h3 & 64) ma = (h3 & 128) ? (h1 >> 40) : M - (h1 >> 40);
+      break;
+    default: ea = 1 + (h1 >> 58) % 60; eb = 1000 + (h2 >> 58) % 60; break;
+  }
+  const double a = __longlong_as_double((long long)(((h1 & (1ull << 63))) | (ea << 52) | ma));
+  const double b = __longlong_as_double((long long)(((h2 & (1ull << 63))) | (eb << 52) | mb));
+  const double r0 = a / b, r1 = idfx::div_rn(a, b);
+  if (__double_as_longlong(r0) != __double_as_longlong(r1)) atomicAdd(bad, 1ull);
+}
+
 }  // namespace
+
+extern "C" int idfx_check_division(long long n, unsigned long long seed, long long* mismatches) {
+  if (!mismatches || n < 0) return IDFX_ERR_STATE;
+  unsigned long long* bad = nullptr;
+  if (cudaMalloc(&bad, sizeof(*bad)) != cudaSuccess) return IDFX_ERR_CUDA;
+  cudaMemset(bad, 0, sizeof(*bad));
+  if (n > 0) k_check_division<<<(unsigned)((n + 255) / 256), 256>>>(n, seed, bad);
+  unsigned long long h = 0;
+  const cudaError_t rc = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (rc != cudaSuccess || cudaGetLastError() != cudaSuccess) return IDFX_ERR_CUDA;
+  *mismatches = (long long)h;
+  return IDFX_OK;
+}
 
 extern "C" int idfx_measure_fp64_peak(double* gops, void* stream) {
   if (!gops) return IDFX_ERR_STATE;

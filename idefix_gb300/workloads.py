@@ -162,14 +162,16 @@ def _coarse_of(Vc, Vs, n, r, learned):
 
 def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=(200, 201, 202, 203),
                 nsnap=50, t_end=1.0, steps=3000, batch=8192, lr=2e-3, lr_end=2e-5,
-                train_precision="mixed", kmax=None, params=None, alphas=(1.0,), log=sys.stderr):
+                train_precision="mixed", kmax=None, params=None, alphas=(0.25, 0.5, 0.75, 1.0),
+                val_seeds=(300, 301), log=sys.stderr):
     """kmax: largest wavenumber of the initial fields; by default 8 x n_fine
     / 512, i.e. the spectrum of the 512^3 fine run scaled with the grid, so
     that the coarse grid resolves it as the 128^3 coarse grid of the
     512^3 run would.  params: (params, fmin, fmax) of a trained network, which
-    skips data generation and training.  alphas: scale factors of the
-    network's correction evaluated on the held-out seeds (the output layer
-    is linear, so alpha scales W3 and b3)."""
+    skips data generation and training.  alphas: candidate scale factors of
+    the network's correction (the output layer is linear, so alpha scales W3
+    and b3); the one with the lowest error on the validation seeds is used
+    on the held-out seeds."""
     import torch
 
     from idefix_gb300 import learned
@@ -226,24 +228,23 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
     else:
         params, fmin, fmax = params
         tr = learned.Trainer(max_batch=batch, params=params)
-    # 3. held-out seeds: errors against the coarsened fine FP64 run
-    rows = []
+    # 3. validation seeds pick the correction scale alpha, held-out seeds
+    #    measure: errors against the coarsened fine FP64 run at t_end
     held_p, held_t = [], []
-    for s in eval_seeds:
+
+    def evaluate(s, alist, plain=True):
         Vc, Vs = ic.turbulence_3d(n_fine, seed=s, kmax=kmax)
         fine = ig.GpuBlock(3, (n_fine,) * 3, cfl=0.6, first_dt=1e-4)
         fine.upload(Vc, Vs)
         t_fine = _timed_run(fine, t_end)
         fv = fine.download()
         ref_d, _, tg_d = learned.coarsen(torch.from_numpy(fv[0]).cuda(), torch.from_numpy(fv[1]).cuda(), n_fine, 2, r)
-        held_p.append(ref_d.float())
-        held_t.append(tg_d.float())
         ref = ref_d.cpu().numpy()
         fine.close()
         row = {"seed": s, "fine_s": t_fine}
-        runs = [("plain", "plm", nc, 0.0)]
-        runs += [("learned" if a == alphas[0] else f"learned_a{a:g}", "learned", nc, a) for a in alphas]
-        runs += [("plain_2x", "plm", 2 * nc, 0.0)]
+        runs = [("plain", "plm", nc, 0.0)] if plain else []
+        runs += [(f"learned_a{a:g}", "learned", nc, a) for a in alist]
+        runs += [("plain_2x", "plm", 2 * nc, 0.0)] if plain else []
         for name, order, nres, alpha in runs:
             pc, fc = _coarse_of(Vc, Vs, n_fine, n_fine // nres, learned)
             Vcc, Vsc = learned.coarse_state(pc, fc)
@@ -254,20 +255,36 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
                 blk.set_learned(pa, fmin, fmax)
             blk.upload(Vcc, Vsc)
             row[name + "_s"] = _timed_run(blk, t_end)
-            out, _ = _coarse_of(*blk.download(), nres, nres // nc, learned) if nres != nc else (None, None)
-            if out is None:
-                vc_out = blk.download()[0][:, 2:2 + nc, 2:2 + nc, 2:2 + nc]
+            if nres != nc:
+                vc_out = _coarse_of(*blk.download(), nres, nres // nc, learned)[0].cpu().numpy()
             else:
-                vc_out = out.cpu().numpy()
+                vc_out = blk.download()[0][:, 2:2 + nc, 2:2 + nc, 2:2 + nc]
             row[name + "_l1"] = _l1(vc_out, ref)
             row[name + "_l1_vars"] = _l1_vars(vc_out, ref)
             if order == "learned":
                 cells, fall = blk.learned_stats()
-                row["fallback_rate"] = fall / max(cells, 1)
+                row[name + "_fallback_rate"] = fall / max(cells, 1)
             blk.close()
-        rows.append(row)
         if log:
             print(json.dumps(row), file=log, flush=True)
+        return row, ref_d, tg_d
+
+    val = [evaluate(s, alphas, plain=False)[0] for s in val_seeds]
+    if val:
+        alpha = min(alphas, key=lambda a: np.mean([row[f"learned_a{a:g}_l1"] for row in val]))
+    else:
+        alpha = alphas[0]
+    res["validation"] = val
+    res["alpha"] = alpha
+    rows = []
+    for s in eval_seeds:
+        row, ref_d, tg_d = evaluate(s, sorted({alpha, 1.0}))
+        held_p.append(ref_d.float())
+        held_t.append(tg_d.float())
+        row["learned_s"] = row[f"learned_a{alpha:g}_s"]
+        row["learned_l1"] = row[f"learned_a{alpha:g}_l1"]
+        row["fallback_rate"] = row[f"learned_a{alpha:g}_fallback_rate"]
+        rows.append(row)
     res["eval"] = rows
     # supervised loss on the held-out final snapshots, with and without the network
     tr.set_dataset(torch.stack(held_p).contiguous(), torch.stack(held_t).contiguous())
@@ -275,8 +292,10 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
     for k in rows[0]:
         if k != "seed" and not k.endswith("_vars"):
             res[k] = float(np.mean([row[k] for row in rows]))
+    res["learned_over_plain_l1"] = res["learned_l1"] / res["plain_l1"]
     res["learned_over_plain_2x_l1"] = res["learned_l1"] / res["plain_2x_l1"]
     res["fine_over_learned_time"] = res["fine_s"] / res["learned_s"]
+    res["plain_2x_over_learned_time"] = res["plain_2x_s"] / res["learned_s"]
     return res, params, fmin, fmax
 
 
@@ -294,7 +313,7 @@ if __name__ == "__main__":
     ap.add_argument("--t-end", type=float, default=1.0)
     ap.add_argument("--save", default=None, help="npz file for the trained parameters and range")
     ap.add_argument("--load", default=None, help="npz file of a trained network (skips training)")
-    ap.add_argument("--alphas", default="1.0", help="comma-separated correction scale factors")
+    ap.add_argument("--alphas", default="0.25,0.5,0.75,1.0", help="comma-separated correction scale factors")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cycles", type=int, default=None, help="default: 500 (ensemble), 200 (lowbeta)")
     ap.add_argument("--no-check", action="store_true")

@@ -146,12 +146,17 @@ int idfx_gpu_profile_read(idfx_gpu* h, double* ms, long long* launches, int ncla
 /* Autotuner (no counterpart in the reference): picks, per sweep direction,
  * the march segment length (cells per thread along the sweep) of the fastest
  * sweep, timed over reps launches; the state is saved and restored, and the
- * results do not depend on the choice.  get_segments reads the choice. */
+ * results do not depend on the choice.  get/set_segments read and set it. */
 int idfx_gpu_autotune(idfx_gpu* h, int reps);
 int idfx_gpu_get_segments(const idfx_gpu* h, int* seg);
+int idfx_gpu_set_segments(idfx_gpu* h, const int* seg);  /* 1..1024 cells per thread */
 /* measured FP64 FMA throughput of the current device (thread operations
  * per second / 1e9), the roof of the FP64-bound sweeps; stream may be NULL */
 int idfx_measure_fp64_peak(double* gops, void* stream);
+/* self-check of the library's FP64 division computed on the integer pipe
+ * (used by the whole-array cons <-> prim passes): n random operand pairs
+ * compared bit for bit with the hardware division */
+int idfx_check_division(long long n, unsigned long long seed, long long* mismatches);
 
 /* Allocation-free Fluid::EvolveStage — no counterpart in the reference.
  * For callers that may not allocate GPU memory while they step (state held
