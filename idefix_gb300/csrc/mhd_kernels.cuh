@@ -494,6 +494,177 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
   }
 }
 
+// ---------------------------------------------------------------------------
+// x sweep by warp chunks (FP32 path).  The march above gives every lane its
+// own x row, so a warp's loads touch 32 rows: one sector each, reused over
+// the next steps only while it survives in L1 - at 256^3 the FP32 x march
+// runs from DRAM at a fraction of the y march's speed.  Here a warp owns one
+// row and walks it in chunks of 32 consecutive cells: lane l holds cell
+// base + 32 k + l, so every load and store of the warp is contiguous; the
+// reconstruction stencil comes from the neighbouring lanes by shuffles (the
+// previous and the next chunk stay in registers), lane l solves the face on
+// the left of its cell and updates the cell on its left, and the values that
+// cross a chunk boundary (the right state, flux and wave speed of the last
+// lane) are carried to lane 0 of the next chunk.  Arithmetic per face and
+// per cell is the march's, term for term.
+// One warp per column (y, z incl. the CT extension); blocks of kXW warps.
+// ---------------------------------------------------------------------------
+constexpr int kXW = 4;
+
+template <typename T>
+__device__ __forceinline__ T lane_from(T cur, T other, int src, bool use_other) {
+  const T a = __shfl_sync(0xffffffffu, cur, src & 31);
+  const T b = __shfl_sync(0xffffffffu, other, src & 31);
+  return use_other ? b : a;
+}
+
+template <int D, int ORDER, int SOLVER, typename T>
+__device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, const Ctl* ctl, int invdt, int last_dir,
+                                              dim3 bid) {
+  if (ctl->done) return;
+  using v = Var<D>;
+  using dd = Dir<D, 0>;
+  constexpr int NV = v::NV;
+  constexpr int H = Recon<ORDER>::H;
+  static_assert(ORDER >= 1 && ORDER <= 4, "warp-chunk x sweep: reconstruction orders 1-4");
+  const int lane = threadIdx.x & 31;
+  const int nA = g.n[1] + 2 * g.ext;
+  const int nB = (D == 3) ? g.n[2] + 2 * g.ext : 1;
+  const long long col = (long long)bid.x * kXW + (threadIdx.x >> 5);
+  if (col >= (long long)nA * nB) return;  // whole warp
+  const int ca = g.beg[1] - g.ext + (int)(col % nA);
+  const int cb = (D == 3) ? g.beg[2] - g.ext + (int)(col / nA) : 0;
+  bool active_col = (ca >= g.beg[1] && ca < g.end[1]);
+  if constexpr (D == 3) active_col = active_col && cb >= g.beg[2] && cb < g.end[2];
+  const long long row = cidx(g, cb, ca, 0);   // cell (0, ca, cb)
+  const long long frow = fidx(g, cb, ca, 0);  // x face (0, ca, cb)
+  const double* vs = f.Vs;                    // x component
+  const T* vcT;
+  if constexpr (sizeof(T) == 4) {
+    vcT = f.Vc32;
+  } else {
+    vcT = f.Vc;
+  }
+  const int nx = g.nt[0];
+  const int beg = g.beg[0], end = g.end[0];
+  const int base = beg - 1;  // first cell reconstructed (left state of face beg)
+  const T gam = (T)g.gamma;
+  const T dxd = (T)g.dx[0];
+  const T dtdVT = (T)ctl->dtdV;
+  const T areaT = (T)g.A[0];
+  const T invdxT = T(1) / (T)g.dx[0];
+  auto load = [&](int n, int i) -> T { return (i >= 0 && i < nx) ? vcT[n * g.ncell + row + i] : T(0); };
+  T prv[NV], cur[NV], nxt[NV];
+#pragma unroll
+  for (int n = 0; n < NV; n++) {
+    prv[n] = load(n, base - 32 + lane);
+    cur[n] = load(n, base + lane);
+    nxt[n] = load(n, base + 32 + lane);
+  }
+  // carried from lane 31 of the previous chunk
+  T cvr[NV];
+  T cFA[v::BX1];
+  T ccp = T(0);
+#pragma unroll
+  for (int n = 0; n < NV; n++) cvr[n] = T(0);
+#pragma unroll
+  for (int n = 0; n < v::BX1; n++) cFA[n] = T(0);
+  const int nchunks = (end - base + 1 + 31) / 32;  // cells base .. end
+  for (int k = 0; k < nchunks; k++) {
+    const int i = base + 32 * k + lane;  // this lane's cell
+    // reconstruction of cell i from the lanes around it
+    T vl[NV], vr[NV];
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      if (n == dd::BXn) continue;
+      T w[2 * H + 1];
+#pragma unroll
+      for (int m = -H; m <= H; m++) {
+        const int src = lane + m;
+        if (m == 0) {
+          w[H] = cur[n];
+        } else if (m < 0) {
+          w[H + m] = lane_from(cur[n], prv[n], src, src < 0);
+        } else {
+          w[H + m] = lane_from(cur[n], nxt[n], src, src > 31);
+        }
+      }
+      Recon<ORDER>::cell(w, dxd, n == v::RHO || n == v::PRS, vl[n], vr[n]);
+    }
+    // face on the left of cell i: left state = right state of cell i-1
+    T vL[NV], vR[NV];
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      if (n == dd::BXn) continue;
+      const T up = __shfl_up_sync(0xffffffffu, vr[n], 1);
+      vL[n] = lane == 0 ? cvr[n] : up;
+      vR[n] = vl[n];
+    }
+    const bool face = (i >= beg && i <= end);
+    const long long cc = row + i;
+    T FA[v::BX1];
+    T cm = T(0);
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) FA[n] = T(0);
+    if (face) {
+      const T bn = (T)vs[frow + i];
+      vL[dd::BXn] = bn;
+      vR[dd::BXn] = bn;
+      RiemannOut<D, T> r;
+      riemann<D, 0, SOLVER>(gam, vL, vR, r);
+      store_emf<D, 0>(g, f, cc, r, vL, vR);
+#pragma unroll
+      for (int n = 0; n < v::BX1; n++) FA[n] = r.F[n] * areaT;
+      cm = r.cmax;
+    }
+    // update of cell i-1 with the faces i-1 (left) and i (right)
+    T FAp[v::BX1];
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) {
+      const T up = __shfl_up_sync(0xffffffffu, FA[n], 1);
+      FAp[n] = lane == 0 ? cFA[n] : up;
+    }
+    const T cpu = __shfl_up_sync(0xffffffffu, cm, 1);
+    const T cp = lane == 0 ? ccp : cpu;
+    if (active_col && face && i - 1 >= beg) {
+      const long long cu = cc - 1;
+#pragma unroll
+      for (int n = 0; n < v::BX1; n++) {
+        const T rhs = -dtdVT * (FA[n] - FAp[n]);
+        f.Uc[n * g.ncell + cu] = f.Uc[n * g.ncell + cu] + (double)rhs;
+      }
+      if (invdt) {
+        const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
+        double inv;
+        if constexpr (sizeof(T) == 8) {
+          inv = prev + 0.5 * (cm + cp) / (g.dx[0]);
+        } else {
+          inv = prev + (double)(T(0.5) * (cm + cp) * invdxT);
+        }
+        f.InvDt[cu] = inv;
+        if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
+      }
+    }
+    // carry lane 31 to the next chunk and shift the register window
+#pragma unroll
+    for (int n = 0; n < NV; n++) cvr[n] = __shfl_sync(0xffffffffu, vr[n], 31);
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) cFA[n] = __shfl_sync(0xffffffffu, FA[n], 31);
+    ccp = __shfl_sync(0xffffffffu, cm, 31);
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      prv[n] = cur[n];
+      cur[n] = nxt[n];
+      nxt[n] = load(n, base + 32 * (k + 2) + lane);
+    }
+  }
+}
+
+template <int D, int ORDER, int SOLVER, typename T>
+__global__ void __launch_bounds__(32 * kXW) k_sweep_xwarp(Geo g, Fields f, const Ctl* ctl, int invdt, int last_dir) {
+  d_sweep_xwarp<D, ORDER, SOLVER, T>(g, f, ctl, invdt, last_dir, blockIdx);
+}
+
 template <int D, int DIR, int ORDER, int SOLVER, typename T>
 __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl* ctl, int invdt, int last_dir, int seg) {
   d_sweep_march<D, DIR, ORDER, SOLVER, T>(g, f, ctl, invdt, last_dir, seg, blockIdx);

@@ -13,9 +13,15 @@ void launch_dir(Engine& e, int invdt, int last) {
   constexpr int B = (DIR == 2) ? 1 : 2;
   const int nseg = (g.n[DIR] + e.seg[DIR] - 1) / e.seg[DIR];
   const long long cols = (long long)(g.n[A] + 2 * g.ext) * (D == 3 ? g.n[B] + 2 * g.ext : 1);
-  dim3 grid((unsigned)((cols + kTM - 1) / kTM), nseg, 1);
   mark_begin(e, kKSweepX + DIR);
-  k_sweep_march<D, DIR, ORDER, SOLVER, T><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt, last, e.seg[DIR]);
+  if constexpr (DIR == 0 && sizeof(T) == 4 && ORDER <= 4) {
+    // FP32 x sweep: warp chunks along each row (coalesced)
+    k_sweep_xwarp<D, ORDER, SOLVER, T><<<(unsigned)((cols + kXW - 1) / kXW), 32 * kXW, 0, e.stream>>>(
+        g, e.f, e.ctl, invdt, last);
+  } else {
+    dim3 grid((unsigned)((cols + kTM - 1) / kTM), nseg, 1);
+    k_sweep_march<D, DIR, ORDER, SOLVER, T><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt, last, e.seg[DIR]);
+  }
   mark_end(e);
 }
 

@@ -116,7 +116,7 @@ def test_ensemble_autotune_and_schedule_keep_results():
 
 def test_ensemble_3d_and_mixed_precision():
     boxes = []
-    for n, seed in ((12, 1), (8, 2)):
+    for n, seed in ((40, 1), (12, 2), (8, 3)):
         Vc, Vs = ic.turbulence_3d(n, seed=seed, kmax=3)
         boxes.append((dict(dims=3, n=(n, n, n), cfl=0.6, precision="mixed"), Vc, Vs))
     res, err, _ = _ensemble(boxes, cycles=5)
@@ -141,3 +141,12 @@ def test_ensemble_rejects_mixed_schemes():
     cfg_b = dict(dims=2, n=(16, 16), solver="hll")
     with pytest.raises(ig.IdefixError):
         ig.Ensemble([cfg_a, cfg_b])
+
+
+def test_ensemble_2d_mixed_precision():
+    # the ensemble's FP32 x sweep is the per-thread march, the single block's
+    # the warp-chunk sweep: equal bits check one against the other
+    boxes = _mixed_boxes(precision="mixed")
+    res, err, _ = _ensemble(boxes, cycles=6)
+    assert err is None
+    _assert_same(res, boxes, cycles=6)
