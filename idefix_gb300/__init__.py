@@ -79,6 +79,7 @@ EXPORTS = [
     "idfx_mlp_eval", "idfx_mlp_feature_range", "idfx_mlp_batch_device", "idfx_mlp_grad_device",
     "idfx_mlp_forward_device", "idfx_learn_coarsen_device", "idfx_measure_fp64_peak",
     "idfx_gpu_autotune", "idfx_gpu_get_segments", "idfx_gpu_set_segments", "idfx_check_division",
+    "idfx_dump_write", "idfx_dump_read",
 ]
 
 KERNEL_CLASSES = ["fill_faces", "stage_begin", "sweep_x", "sweep_y", "sweep_z", "ct_corner",
@@ -140,6 +141,8 @@ def load_library(path=LIB_PATH):
     U64 = ctypes.c_ulonglong
     lib.idfx_measure_fp64_peak.argtypes = [dp, P]
     lib.idfx_gpu_autotune.argtypes = [P, I]
+    lib.idfx_dump_write.argtypes = [ctypes.c_char_p, ctypes.POINTER(Config), P, P, D, D, I]
+    lib.idfx_dump_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(Config), P, P, dp, dp]
     lib.idfx_check_division.argtypes = [LL, ctypes.c_ulonglong, ctypes.POINTER(LL)]
     lib.idfx_gpu_get_segments.argtypes = [P, ctypes.POINTER(I)]
     lib.idfx_gpu_set_segments.argtypes = [P, ctypes.POINTER(I)]
@@ -173,6 +176,42 @@ def measure_fp64_peak(stream=None):
     if rc != OK:
         raise IdefixError(f"idfx_measure_fp64_peak failed with status {rc}")
     return g.value
+
+
+def _shapes(cfg):
+    dims = cfg.dims
+    ng = 3 if cfg.order == ORDER["ppm"] else 2
+    nt = [cfg.n[d] + 2 * ng if d < dims else 1 for d in range(3)]
+    ntv = [nt[d] + (1 if d < dims else 0) for d in range(3)]
+    return (2 * dims + 2, nt[2], nt[1], nt[0]), (dims, ntv[2], ntv[1], ntv[0])
+
+
+def write_dump(path, cfg, Vc, Vs, t, dt, vtk_file_number=0):
+    """idfx_dump_write: host arrays of one block -> reference-format dump."""
+    lib = load_library()
+    sc, ss = _shapes(cfg)
+    Vc = np.ascontiguousarray(Vc, dtype=np.float64)
+    Vs = np.ascontiguousarray(Vs, dtype=np.float64)
+    if Vc.shape != sc or Vs.shape != ss:
+        raise IdefixError(f"state shapes {Vc.shape}/{Vs.shape} != {sc}/{ss}")
+    rc = lib.idfx_dump_write(os.fsencode(path), ctypes.byref(cfg), _as_ptr(Vc), _as_ptr(Vs), float(t), float(dt),
+                             int(vtk_file_number))
+    if rc != OK:
+        raise IdefixError(f"idfx_dump_write failed with status {rc}")
+
+
+def read_dump(path, cfg):
+    """idfx_dump_read -> (Vc, Vs, t, dt), ghosts zero."""
+    lib = load_library()
+    sc, ss = _shapes(cfg)
+    Vc = np.zeros(sc)
+    Vs = np.zeros(ss)
+    t, dt = ctypes.c_double(), ctypes.c_double()
+    rc = lib.idfx_dump_read(os.fsencode(path), ctypes.byref(cfg), _as_ptr(Vc), _as_ptr(Vs), ctypes.byref(t),
+                            ctypes.byref(dt))
+    if rc != OK:
+        raise IdefixError(f"idfx_dump_read failed with status {rc}")
+    return Vc, Vs, t.value, dt.value
 
 
 def make_config(dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm", solver="hlld",
@@ -226,6 +265,7 @@ class GpuBlock:
         if rc != OK:
             raise IdefixError(f"idfx_gpu_create failed with status {rc}")
         self.h = h
+        self.cfg = cfg
         self.dims, self.n = dims, n
         nvar, ng, vcl, vsl = ctypes.c_int(), ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
         self.lib.idfx_gpu_sizes(self.h, ctypes.byref(nvar), ctypes.byref(ng), ctypes.byref(vcl),
@@ -333,6 +373,18 @@ class GpuBlock:
 
 
     # -- per-kernel timing --------------------------------------------------
+    def write_dump(self, path, vtk_file_number=0):
+        """Restart dump of the current state in the reference's format."""
+        Vc, Vs = self.download()
+        t, dt, _ = self.get_time()
+        write_dump(path, self.cfg, Vc, Vs, t, dt, vtk_file_number)
+
+    def read_dump(self, path, ncycles=0):
+        """Load a restart dump (reference format) as the current state."""
+        Vc, Vs, t, dt = read_dump(path, self.cfg)
+        self.upload(Vc, Vs)
+        self.set_time(t, dt, ncycles)
+
     def autotune(self, reps=3):
         """pick the march segment length of every sweep direction by timing"""
         self._check(self.lib.idfx_gpu_autotune(self.h, int(reps)))
@@ -503,6 +555,18 @@ class Ensemble:
 
     def run(self, tstop=-1.0, max_cycles=-1, graph=True):
         self._check(self.lib.idfx_ens_run(self.h, float(tstop), int(max_cycles), 1 if graph else 0))
+
+    def write_dump(self, path, vtk_file_number=0):
+        """Restart dump of the current state in the reference's format."""
+        Vc, Vs = self.download()
+        t, dt, _ = self.get_time()
+        write_dump(path, self.cfg, Vc, Vs, t, dt, vtk_file_number)
+
+    def read_dump(self, path, ncycles=0):
+        """Load a restart dump (reference format) as the current state."""
+        Vc, Vs, t, dt = read_dump(path, self.cfg)
+        self.upload(Vc, Vs)
+        self.set_time(t, dt, ncycles)
 
     def autotune(self, reps=3):
         self._check(self.lib.idfx_ens_autotune(self.h, int(reps)))

@@ -18,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libidefix_gb300.so")
 
 SOURCES = ["engine.cu", "sweep_hlld.cu", "sweep_hll.cu", "sweep_roe.cu", "sweep_tvdlf.cu",
-           "noalloc.cu", "ensemble.cu", "learned.cu", "peak.cu"]
+           "noalloc.cu", "ensemble.cu", "learned.cu", "peak.cu", "dump.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xptxas", "-warn-spills"]
@@ -46,13 +46,13 @@ def build_library(verbose=False, jobs=None, extra=()):
     cmds = []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if _needs(o, [s] + headers):
             cmds.append([nvcc(), *ARCH, *NVFLAGS, *extra, "-c", s, "-o", o])
 
     def run(cmd):
-        r = subprocess.run(cmd, capture_output=True, text=True)
+        r = subprocess.run(cmd, capture_output=True, text=True, errors="replace")
         return cmd, r
 
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(SOURCES), os.cpu_count() or 4)) as ex:

@@ -175,6 +175,16 @@ int idfx_check_division(long long n, unsigned long long seed, long long* mismatc
 int idfx_evolve_stage_noalloc(const idfx_gpu_config* cfg, const double* Vc, double* Uc, double* Vs,
                               double t, double dt, void* stream, char* err, size_t errlen);
 
+/* Restart dumps in the reference's format: Dump::Write / Dump::Read
+ * (output/dump.cpp:30-985).  Host arrays of one block in the layout above;
+ * the dump holds the active cells of RHO, VX1..VXd, PRS, the active faces of
+ * the face field, time, dt and vtkFileNumber (read skips fields of other
+ * modules, as the reference does).  Reading needs the same grid; ghost
+ * values are left as they are (the next boundary pass fills them). */
+int idfx_dump_write(const char* path, const idfx_gpu_config* cfg, const double* Vc, const double* Vs, double t,
+                    double dt, int vtk_file_number);
+int idfx_dump_read(const char* path, const idfx_gpu_config* cfg, double* Vc, double* Vs, double* t, double* dt);
+
 /* Learned interface-state correction — no counterpart in the reference.
  * A network (216 -> 128 -> 128 -> 16, SiLU, BF16 tensor-core arithmetic
  * with FP32 accumulation) reads the 3x3x3 primitive stencil of a cell in
