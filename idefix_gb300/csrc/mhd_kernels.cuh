@@ -386,6 +386,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
   const T dtdVT = (T)ctl->dtdV;
   const T areaT = (T)g.A[DIR];
   const T invdxT = T(1) / (T)g.dx[DIR];  // FP32 path only
+  double run_max = 0.0;                  // max of InvDt over this thread's cells
   for (int c = m0 - 1; c <= m1; c++) {
     const long long cc = c0 + (long long)(c - m0) * sd;
     const bool more = c < m1;
@@ -481,7 +482,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
               inv = prev + (double)(T(0.5) * (r.cmax + cp) * invdxT);
             }
             f.InvDt[cu] = inv;
-            if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
+            if (inv > run_max) run_max = inv;  // NaN never compares greater
           }
         }
 #pragma unroll
@@ -492,6 +493,9 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
 #pragma unroll
     for (int n = 0; n < NV; n++) vrp[n] = vr[n];
   }
+  // CFL maximum of the last direction: one atomic per thread, not per cell
+  // (a per-cell atomic on one address serialises the whole z sweep)
+  if (last_dir && invdt && active_col) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, run_max);
 }
 
 // ---------------------------------------------------------------------------
@@ -570,6 +574,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
 #pragma unroll
   for (int n = 0; n < v::BX1; n++) cFA[n] = T(0);
   const int nchunks = (end - base + 1 + 31) / 32;  // cells base .. end
+  double run_max = 0.0;
   for (int k = 0; k < nchunks; k++) {
     const int i = base + 32 * k + lane;  // this lane's cell
     // reconstruction of cell i from the lanes around it
@@ -642,7 +647,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
           inv = prev + (double)(T(0.5) * (cm + cp) * invdxT);
         }
         f.InvDt[cu] = inv;
-        if (last_dir) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, inv);
+        if (inv > run_max) run_max = inv;
       }
     }
     // carry lane 31 to the next chunk and shift the register window
@@ -658,6 +663,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
       nxt[n] = load(n, base + 32 * (k + 2) + lane);
     }
   }
+  if (last_dir && invdt && active_col) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, run_max);
 }
 
 template <int D, int ORDER, int SOLVER, typename T>
@@ -922,9 +928,11 @@ template <int D>
 __device__ __forceinline__ void d_divb(const Geo& g, const Fields& f, Ctl* ctl, dim3 bid) {
   const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
   const long long tot = (long long)g.n[0] * g.n[1] * (D == 3 ? g.n[2] : 1);
-  if (tid >= tot) return;
-  const int i = g.beg[0] + (int)(tid % g.n[0]);
-  const long long r = tid / g.n[0];
+  // every lane reaches the warp reduction below; lanes past the end give 0
+  const bool in = tid < tot;
+  const long long t = in ? tid : 0;
+  const int i = g.beg[0] + (int)(t % g.n[0]);
+  const long long r = t / g.n[0];
   const int j = g.beg[1] + (int)(r % g.n[1]);
   const int k = (D == 3) ? g.beg[2] + (int)(r / g.n[1]) : 0;
   const long long fc = fidx(g, k, j, i);
@@ -949,7 +957,14 @@ __device__ __forceinline__ void d_divb(const Geo& g, const Fields& f, Ctl* ctl, 
     amplitude += fabs(b1) * d1 + fabs(b2) * d2 + fabs(b3) * d3;
     val = fabs(dB1 + dB2 + dB3) / amplitude;
   }
-  atomic_max_pos(&ctl->divb_bits, val);
+  // max over the warp, then one atomic per warp (NaN ignored, as before)
+  if (!in || !(val >= 0.0)) val = 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double w = __shfl_xor_sync(0xffffffffu, val, o);
+    if (w > val) val = w;
+  }
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(&ctl->divb_bits, val);
 }
 
 template <int D>
