@@ -58,6 +58,8 @@ class Config(ctypes.Structure):
         ("log_period", ctypes.c_int),
         ("check_nan_period", ctypes.c_int),
         ("precision", ctypes.c_int),
+        ("shock_flattening", ctypes.c_int),
+        ("shock_smoothing", ctypes.c_double),
     ]
 
 
@@ -216,7 +218,8 @@ def read_dump(path, cfg):
 
 def make_config(dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm", solver="hlld",
                 emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.9, cfl_max_var=1.1,
-                first_dt=1.0e-10, maxdivb=1e-6, log_period=0, check_nan_period=0, precision="fp64"):
+                first_dt=1.0e-10, maxdivb=1e-6, log_period=0, check_nan_period=0, precision="fp64",
+                shock_flattening=None):
     """idfx_gpu_config from the input-file style arguments of GpuBlock."""
     lib = load_library()
     n = list(n) + [1] * (3 - len(n))
@@ -234,6 +237,8 @@ def make_config(dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm"
     cfg.gamma, cfg.cfl, cfg.cfl_max_var = gamma, cfl, cfl_max_var
     cfg.first_dt, cfg.maxdivb = first_dt, maxdivb
     cfg.log_period, cfg.check_nan_period = log_period, check_nan_period
+    if shock_flattening is not None:  # [Hydro] shockFlattening <smoothing>
+        cfg.shock_flattening, cfg.shock_smoothing = 1, float(shock_flattening)
     return cfg
 
 
@@ -255,11 +260,11 @@ class GpuBlock:
     def __init__(self, dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm",
                  solver="hlld", emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.9,
                  cfl_max_var=1.1, first_dt=1.0e-10, maxdivb=1e-6, log_period=0,
-                 check_nan_period=0, precision="fp64", stream=None):
+                 check_nan_period=0, precision="fp64", stream=None, shock_flattening=None):
         self.lib = load_library()
         n = list(n) + [1] * (3 - len(n))
         cfg = make_config(dims, n, xbeg, xend, order, solver, emf, nstages, gamma, cfl, cfl_max_var,
-                          first_dt, maxdivb, log_period, check_nan_period, precision)
+                          first_dt, maxdivb, log_period, check_nan_period, precision, shock_flattening)
         h = ctypes.c_void_p()
         rc = self.lib.idfx_gpu_create(ctypes.byref(cfg), ctypes.c_void_p(stream), ctypes.byref(h))
         if rc != OK:

@@ -199,6 +199,13 @@ void launch_ct(Engine& e, int combine, double wc, double w0) {
   IDFX_DISPATCH_D(k_ct_faces, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl, combine, wc, w0);
   mark_end(e);
 }
+void launch_find_shock(Engine& e) {
+  const long long m = (long long)(e.g.n[0] + 2) * (e.g.n[1] + 2) * (e.g.D == 3 ? e.g.n[2] + 2 : 1);
+  mark_begin(e, kKStageBegin);
+  IDFX_DISPATCH_D(k_find_shock, nblocks(m), kThreads, e.g, e.f, e.ctl);
+  mark_end(e);
+}
+
 void launch_nan_check(Engine& e) {
   cudaMemsetAsync(&e.ctl->nan_count, 0, sizeof(unsigned long long), e.stream);
   IDFX_DISPATCH_D(k_nan_count, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
@@ -221,6 +228,7 @@ void queue_cycle(Engine& e, int use_tstop) {
     const int save = (e.nstages > 1 && stage == 0);
     launch_fill_faces(e, save);
     launch_stage_begin(e, kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
+    if (e.f.shock) launch_find_shock(e);  // RiemannSolver::CalcFlux (calcFlux.hpp:33)
     if (g.order == IDFX_LEARNED) launch_learned_recon(e);
     launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
     const int combine = stage > 0;
@@ -311,7 +319,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   if (cfg->order < 1 || cfg->order > 5 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
   // the learned reconstruction: 3-D, HLLD, FP64 arithmetic around the network
   if (cfg->order == IDFX_LEARNED &&
-      (cfg->dims != 3 || cfg->solver != IDFX_HLLD || cfg->precision != IDFX_FP64))
+      (cfg->dims != 3 || cfg->solver != IDFX_HLLD || cfg->precision != IDFX_FP64 || cfg->shock_flattening))
     return IDFX_ERR_CONFIG;
   if (cfg->emf < 0 || cfg->emf > 4 || cfg->nstages < 1 || cfg->nstages > 3) return IDFX_ERR_CONFIG;
   if (cfg->precision != IDFX_FP64 && cfg->precision != IDFX_MIXED) return IDFX_ERR_CONFIG;
@@ -362,6 +370,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   g.gm1 = cfg->gamma - 1.0;
   g.ext = 1;  // hlldMHD.hpp:30-49: uct_hll(d) with HLLD/HLL needs nghost cells
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
+  g.shock_smoothing = cfg->shock_smoothing;
   e.nstages = cfg->nstages;
   e.precision = cfg->precision;
   if (e.nstages == 2) {  // timeIntegrator.cpp:62-71
@@ -385,7 +394,8 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
                + 6 * nc + 3 * nc + 3 * nc + 3 * nc  // face EMFs, sv, cell EMFs, corner EMFs
                + (hll_emf ? 12 * nc : 0)
                + (g.order == IDFX_LEARNED ? 48 * nc : 0)   // learned face states
-               + (cfg->precision == IDFX_MIXED ? (NV * nc + 1) / 2 : 0);  // FP32 primitives
+               + (cfg->precision == IDFX_MIXED ? (NV * nc + 1) / 2 : 0)   // FP32 primitives
+               + (cfg->shock_flattening ? (nc + 7) / 8 : 0);               // shock flags
   int rc = IDFX_OK;
   if (stream) {
     e.stream = (cudaStream_t)stream;
@@ -424,6 +434,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   }
   f.ls = (g.order == IDFX_LEARNED) ? take(48 * nc) : nullptr;
   f.Vc32 = (cfg->precision == IDFX_MIXED) ? reinterpret_cast<float*>(take((NV * nc + 1) / 2)) : nullptr;
+  f.shock = cfg->shock_flattening ? reinterpret_cast<unsigned char*>(take((nc + 7) / 8)) : nullptr;
   Ctl c{};
   c.t = 0.0;
   c.dt = cfg->first_dt;
@@ -745,6 +756,7 @@ int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt) {
     return fail(e, IDFX_ERR_STATE, "the learned reconstruction needs idfx_gpu_set_learned first");
   k_set_stage_dt<<<1, 1, 0, e.stream>>>(e.g, e.ctl, dt);
   if (e.f.Vc32) k_vc32<<<nblocks(e.g.ncell), kThreads, 0, e.stream>>>(e.g, e.f, 2 * e.g.D + 2);
+  if (e.f.shock) launch_find_shock(e);
   if (e.g.order == IDFX_LEARNED) launch_learned_recon(e);
   if (e.g.emf == kEmfContact || e.g.emf == kEmfUct0)
     IDFX_DISPATCH_D(k_cell_emf_all, nblocks(e.g.ncell), kThreads, e.g, e.f);

@@ -38,6 +38,12 @@ __global__ void ke_stage_begin(const EnsBox* boxes, const int4* items, int flags
   d_stage_begin<D>(B.g, B.f, B.ctl, flags, dim3(it.y, it.z, it.w));
 }
 template <int D>
+__global__ void ke_find_shock(const EnsBox* boxes, const int4* items) {
+  const int4 it = items[blockIdx.x];
+  const EnsBox& B = boxes[it.x];
+  d_find_shock<D>(B.g, B.f, B.ctl, dim3(it.y, it.z, it.w));
+}
+template <int D>
 __global__ void ke_ct_corner(const EnsBox* boxes, const int4* items) {
   const int4 it = items[blockIdx.x];
   const EnsBox& B = boxes[it.x];
@@ -210,6 +216,8 @@ void queue_cycle(EnsEngine& e, bool checks) {
     IDFX_ENS_D(ke_fill_faces, e.fill.n, e.d_boxes, e.fill.items, save);
     IDFX_ENS_D(ke_stage_begin, e.begin.n, e.d_boxes, e.begin.items,
                kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
+    // shock flags: the stage-begin table covers (n + 2)^D cells of every box
+    if (e.shock) IDFX_ENS_D(ke_find_shock, e.begin.n, e.d_boxes, e.begin.items);
     for (int d = 0; d < e.D; d++)
       launch_sweep(e, d, e.sweep[d], stage == 0 ? (d == 0 ? 1 : 2) : 0, stage == 0 && d == e.D - 1);
     const int combine = stage > 0;
@@ -302,6 +310,7 @@ bool box_geometry(const idfx_gpu_config* cfg, Geo& g) {
   g.gm1 = cfg->gamma - 1.0;
   g.ext = 1;
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
+  g.shock_smoothing = cfg->shock_smoothing;
   return true;
 }
 
@@ -443,7 +452,7 @@ int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_en
     // time-step parameters are per box
     if (c.dims != c0.dims || c.order != c0.order || c.solver != c0.solver || c.emf != c0.emf ||
         c.nstages != c0.nstages || c.precision != c0.precision || c.log_period != c0.log_period ||
-        c.check_nan_period != c0.check_nan_period)
+        c.check_nan_period != c0.check_nan_period || (c.shock_flattening != 0) != (c0.shock_flattening != 0))
       return IDFX_ERR_CONFIG;
     if (c.order < 1 || c.order > 4 || c.solver < 0 || c.solver > 3) return IDFX_ERR_CONFIG;
     if (c.emf < 0 || c.emf > 4 || c.nstages < 1 || c.nstages > 3) return IDFX_ERR_CONFIG;
@@ -464,6 +473,7 @@ int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_en
   e.precision = c0.precision;
   e.log_period = c0.log_period;
   e.check_nan_period = c0.check_nan_period;
+  e.shock = c0.shock_flattening != 0;
   if (e.nstages == 2) {  // timeIntegrator.cpp:62-71
     e.wc[0] = 0.5;
     e.w0[0] = 0.5;
@@ -486,7 +496,8 @@ int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_en
     box_geometry(&cfgs[b], g);
     const size_t nc = up32((size_t)g.ncell), nf = up32((size_t)g.nface);
     box_len[b] = 3 * NV * nc + 2 * g.D * nf + nc + 15 * nc + (hll_emf ? 12 * nc : 0) +
-                 (e.precision == IDFX_MIXED ? up32((NV * nc + 1) / 2) : 0);  // FP32 primitives
+                 (e.precision == IDFX_MIXED ? up32((NV * nc + 1) / 2) : 0) +  // FP32 primitives
+                 (e.shock ? up32((nc + 7) / 8) : 0);                          // shock flags
     len += box_len[b];
   }
   int rc = IDFX_OK;
@@ -538,6 +549,7 @@ int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_en
       f.dR[d] = hll_emf ? take(nc) : nullptr;
     }
     f.Vc32 = (e.precision == IDFX_MIXED) ? reinterpret_cast<float*>(take(up32((NV * nc + 1) / 2))) : nullptr;
+    f.shock = e.shock ? reinterpret_cast<unsigned char*>(take(up32((nc + 7) / 8))) : nullptr;
     B.ctl = e.d_ctl + b;
     for (int d = 0; d < 3; d++) B.seg[d] = d < e.D ? default_seg(g, d, sms) : 1;
     Ctl c{};

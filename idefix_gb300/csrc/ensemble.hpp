@@ -32,6 +32,7 @@ struct EnsEngine {
   int nbox = 0;
   int D = 2, order = 2, solver = 0, emf = 0, nstages = 2, precision = 0;
   int log_period = 0, check_nan_period = 0;
+  bool shock = false;  // shock flattening (flags per box)
   double wc[2] = {0, 0}, w0[2] = {0, 0};
   long long ncycles = 0;  // host mirror (all boxes cycle together)
   std::vector<EnsBox> boxes;

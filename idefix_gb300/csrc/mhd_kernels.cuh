@@ -40,6 +40,7 @@ struct Geo {
   double A[3];  // face areas (makeGeometry.cpp:146-147,178-179,201-202)
   double gamma, gm1;
   int ext;  // perpendicular extension of the flux sweeps for CT
+  double shock_smoothing;  // [Hydro] shockFlattening value (flags in Fields::shock)
 };
 
 // Device-resident time-integrator control block.
@@ -65,6 +66,7 @@ struct Fields {
   double *aL[3], *aR[3], *dL[3], *dR[3];
   double* ls;   // learned face states [3][16][ncell] (ORDER 5)
   float* Vc32;  // FP32 copy of Vc read by the mixed-precision sweeps (else null)
+  unsigned char* shock;  // FlagShock per cell when shock flattening is on (else null)
 };
 
 __device__ __forceinline__ long long cidx(const Geo& g, int k, int j, int i) {
@@ -202,6 +204,56 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
 template <int D>
 __global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
   d_stage_begin<D>(g, f, ctl, flags, blockIdx);
+}
+
+// ---------------------------------------------------------------------------
+// ShockFlattening::FindShock (shockFlattening.hpp:82-168, 185-201): a cell of
+// [beg-1, end] is flagged when div v < 0 and the pressure jump across it
+// exceeds smoothing x the smallest pressure of its stencil; the sweeps then
+// give it the minmod slope.  One thread per cell of that range.
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ void d_find_shock(const Geo& g, const Fields& f, const Ctl* ctl, dim3 bid) {
+  if (ctl->done) return;
+  using v = Var<D>;
+  const int m0 = g.n[0] + 2, m1 = g.n[1] + 2, m2 = (D == 3) ? g.n[2] + 2 : 1;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
+  if (tid >= (long long)m0 * m1 * m2) return;
+  const int i = g.beg[0] - 1 + (int)(tid % m0);
+  const int j = g.beg[1] - 1 + (int)((tid / m0) % m1);
+  const int k = (D == 3) ? g.beg[2] - 1 + (int)(tid / ((long long)m0 * m1)) : 0;
+  const long long c = cidx(g, k, j, i);
+  const long long si = 1, sj = g.s[1], sk = g.s[2];
+  const double* vx = f.Vc + v::MX1 * g.ncell;
+  const double* vy = f.Vc + v::MX2 * g.ncell;
+  const double* p = f.Vc + v::PRS * g.ncell;
+  double divV = (vx[c + si] - vx[c - si]) / (2 * g.dx[0]) + (vy[c + sj] - vy[c - sj]) / (2 * g.dx[1]);
+  if constexpr (D == 3) {
+    const double* vz = f.Vc + v::MX3 * g.ncell;
+    divV = divV + (vz[c + sk] - vz[c - sk]) / (2 * g.dx[2]);
+  }
+  unsigned char flag = 0;
+  if (divV < 0.0) {
+    double pmin = p[c];
+    pmin = fmin(pmin, p[c + si]);
+    pmin = fmin(pmin, p[c - si]);
+    double gradP = fabs(p[c + si] - p[c - si]);
+    pmin = fmin(pmin, p[c + sj]);
+    pmin = fmin(pmin, p[c - sj]);
+    gradP += fabs(p[c + sj] - p[c - sj]);
+    if constexpr (D == 3) {
+      pmin = fmin(pmin, p[c + sk]);
+      pmin = fmin(pmin, p[c - sk]);
+      gradP += fabs(p[c + sk] - p[c - sk]);
+    }
+    if (gradP > g.shock_smoothing * pmin) flag = 1;
+  }
+  f.shock[c] = flag;
+}
+
+template <int D>
+__global__ void k_find_shock(Geo g, Fields f, const Ctl* ctl) {
+  d_find_shock<D>(g, f, ctl, blockIdx);
 }
 
 // ---------------------------------------------------------------------------
@@ -420,6 +472,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
       }
     }
     T vl[NV], vr[NV];
+    const bool shk = f.shock && f.shock[cc];  // shock flag of cell c
 #pragma unroll
     for (int n = 0; n < NV; n++) {
       if (n == dd::BXn) continue;
@@ -435,7 +488,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
         vl[n] = (T)f.ls[((long long)DIR * 16 + n) * g.ncell + cc];
         vr[n] = (T)f.ls[((long long)DIR * 16 + 8 + n) * g.ncell + cc];
       } else {
-        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n]);
+        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk);
       }
     }
     if (c >= m0) {
@@ -579,6 +632,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
     const int i = base + 32 * k + lane;  // this lane's cell
     // reconstruction of cell i from the lanes around it
     T vl[NV], vr[NV];
+    const bool shk = f.shock && i >= 0 && i < nx && f.shock[row + i];
 #pragma unroll
     for (int n = 0; n < NV; n++) {
       if (n == dd::BXn) continue;
@@ -594,7 +648,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
           w[H + m] = lane_from(cur[n], nxt[n], src, src > 31);
         }
       }
-      Recon<ORDER>::cell(w, dxd, n == v::RHO || n == v::PRS, vl[n], vr[n]);
+      Recon<ORDER>::cell(w, dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk);
     }
     // face on the left of cell i: left state = right state of cell i-1
     T vL[NV], vR[NV];

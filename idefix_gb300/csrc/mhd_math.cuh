@@ -269,27 +269,29 @@ __device__ __forceinline__ void ppm_states(T vm2, T vm1, T v0, T vp1, T vp2, T& 
 template <int ORDER>
 struct Recon {
   static constexpr int H = (ORDER == 1 ? 0 : (ORDER == 4 ? 2 : 1));  // ORDER 5: 1
+  // shock: the cell is flagged by shock flattening (minmod slope, PLM and
+  // LimO3 only, extrapolateToFaces.hpp:96-218)
   template <typename T>
-  __device__ __forceinline__ static void cell(const T* w, T dx, bool pos, T& vl, T& vr) {
+  __device__ __forceinline__ static void cell(const T* w, T dx, bool pos, T& vl, T& vr, bool shock = false) {
     if constexpr (ORDER == 1) {
       vl = w[0];
       vr = w[0];
     } else if constexpr (ORDER == 2) {
       const T dvm = w[1] - w[0];
       const T dvp = w[2] - w[1];
-      const T d = lim_vanleer(dvp, dvm);
+      const T d = shock ? lim_minmod(dvp, dvm) : lim_vanleer(dvp, dvm);
       vr = w[1] + T(0.5) * d;
       vl = w[1] - T(0.5) * d;
     } else if constexpr (ORDER == 3) {
       const T dm = w[1] - w[0];
       const T dp = w[2] - w[1];
-      T d = dp * lim_limo3(dp, dm, dx);
+      T d = shock ? lim_minmod(dp, dm) : dp * lim_limo3(dp, dm, dx);
       vr = w[1] + T(0.5) * d;
       if (pos && vr <= T(0)) {
         d = lim_minmod(dp, dm);
         vr = w[1] + T(0.5) * d;
       }
-      d = dm * lim_limo3(dm, dp, dx);
+      d = shock ? lim_minmod(dp, dm) : dm * lim_limo3(dm, dp, dx);
       vl = w[1] - T(0.5) * d;
       if (pos && vl <= T(0)) {
         d = lim_minmod(dp, dm);

@@ -102,6 +102,7 @@ int na_geometry(const idfx_gpu_config* cfg, Geo& g) {
   if (!cfg) return IDFX_ERR_STATE;
   if (cfg->dims != 2 && cfg->dims != 3) return IDFX_ERR_CONFIG;
   if (cfg->order < 1 || cfg->order > 4 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
+  if (cfg->shock_flattening) return IDFX_ERR_CONFIG;  // not supported by this entry point
   if (cfg->emf < 0 || cfg->emf > 4 || cfg->precision != IDFX_FP64) return IDFX_ERR_CONFIG;
   if (cfg->emf == IDFX_EMF_UCT_HLLD && (cfg->solver == IDFX_HLL || cfg->solver == IDFX_TVDLF))
     return IDFX_ERR_CONFIG;

@@ -75,6 +75,8 @@ typedef struct {
   int log_period;           /* [Output] log: divB check period, 0 = off           */
   int check_nan_period;     /* [TimeIntegrator] check_nan, 0 = off                */
   int precision;            /* IDFX_FP64 or IDFX_MIXED                            */
+  int shock_flattening;     /* [Hydro] shockFlattening present (0 = off)          */
+  double shock_smoothing;   /* its value (shockFlattening.hpp:164)                */
 } idfx_gpu_config;
 
 typedef struct idfx_gpu idfx_gpu;

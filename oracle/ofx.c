@@ -34,6 +34,9 @@ struct ofx {
   double *ezi, *ezj, *exj, *exk, *eyi, *eyk, *svx, *svy, *svz;
   double *Ex1, *Ex2, *Ex3, *ex, *ey, *ez;
   double *aL[3], *aR[3], *dL[3], *dR[3];
+  int shock;            /* [Hydro] shockFlattening present              */
+  double smoothing;     /* its value                                    */
+  unsigned char* flag;  /* FlagShock per cell (1 = Shock), zero outside */
 };
 
 #define OFX_IDX(o, k, j, i) (((size_t)(k) * (o)->nt[1] + (size_t)(j)) * (o)->nt[0] + (size_t)(i))
@@ -312,6 +315,7 @@ ofx* ofx_create(int dims, int nx, int ny, int nz, double xb0, double xe0, double
     o->dL[d] = ofx_zalloc(nc);
     o->dR[d] = ofx_zalloc(nc);
   }
+  o->flag = (unsigned char*)calloc(nc ? nc : 1, 1);
   return o;
 }
 
@@ -327,6 +331,7 @@ void ofx_destroy(ofx* o) {
     free(o->dL[d]);
     free(o->dR[d]);
   }
+  free(o->flag);
   free(o);
 }
 
@@ -355,6 +360,11 @@ void ofx_get_time(const ofx* o, double* t, double* dt, long* ncycles) {
   if (dt) *dt = o->dt;
   if (ncycles) *ncycles = o->ncycles;
 }
+void ofx_set_shock(ofx* o, int enabled, double smoothing) {
+  o->shock = enabled != 0;
+  o->smoothing = smoothing;
+}
+
 void ofx_set_checks(ofx* o, int log_period, int check_nan_period, double maxdivb) {
   o->log_period = log_period;
   o->check_nan_period = check_nan_period;

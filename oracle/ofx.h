@@ -59,6 +59,10 @@ void   ofx_get_time(const ofx* o, double* t, double* dt, long* ncycles);
 /* diagnostic periods: 0 disables (TimeIntegrator "log" and "check_nan") */
 void   ofx_set_checks(ofx* o, int log_period, int check_nan_period, double maxdivb);
 
+/* [Hydro] shockFlattening <smoothing> (riemannSolver.hpp:153-159): cells
+ * flagged by ShockFlattening::FindShock use the minmod slope */
+void   ofx_set_shock(ofx* o, int enabled, double smoothing);
+
 /* building blocks (one call = one reference method) */
 void   ofx_set_boundaries(ofx* o);                 /* Boundary::SetBoundaries       */
 void   ofx_prim_to_cons(ofx* o);                   /* Fluid::ConvertPrimToCons      */

@@ -537,6 +537,9 @@ static void SFX(roe)(int dir, double gamma, const double* vL, const double* vR, 
 static void SFX(recon)(const ofx* o, int dir, size_t base, double* vL, double* vR) {
   const size_t s = o->stride[dir];
   const double dxv = o->dx[dir];
+  /* shock flags of the two cells (extrapolateToFaces.hpp:96-121, 139-218) */
+  const int shL = o->shock && o->flag[base - s];
+  const int shR = o->shock && o->flag[base];
   for (int nv = 0; nv < NV; nv++) {
     const double* q = o->Vc + (size_t)nv * o->ncell + base;
     if (o->order == 1) {
@@ -545,16 +548,16 @@ static void SFX(recon)(const ofx* o, int dir, size_t base, double* vL, double* v
     } else if (o->order == 2) {
       double dvm = q[-(ptrdiff_t)s] - q[-2 * (ptrdiff_t)s];
       double dvp = q[0] - q[-(ptrdiff_t)s];
-      double dv = ofx_vanleer(dvp, dvm);
+      double dv = shL ? ofx_minmod(dvp, dvm) : ofx_vanleer(dvp, dvm);
       vL[nv] = q[-(ptrdiff_t)s] + 0.5 * dv;
       dvm = dvp;
       dvp = q[s] - q[0];
-      dv = ofx_vanleer(dvp, dvm);
+      dv = shR ? ofx_minmod(dvp, dvm) : ofx_vanleer(dvp, dvm);
       vR[nv] = q[0] - 0.5 * dv;
     } else if (o->order == 3) {
       double dvm = q[-(ptrdiff_t)s] - q[-2 * (ptrdiff_t)s];
       double dvp = q[0] - q[-(ptrdiff_t)s];
-      double dv = dvp * ofx_limo3(dvp, dvm, dxv);
+      double dv = shL ? ofx_minmod(dvp, dvm) : dvp * ofx_limo3(dvp, dvm, dxv);
       vL[nv] = q[-(ptrdiff_t)s] + 0.5 * dv;
       if (nv == RHO || nv == PRS) {
         if (vL[nv] <= 0.0) {
@@ -564,7 +567,7 @@ static void SFX(recon)(const ofx* o, int dir, size_t base, double* vL, double* v
       }
       dvm = dvp;
       dvp = q[s] - q[0];
-      dv = dvm * ofx_limo3(dvm, dvp, dxv);
+      dv = shR ? ofx_minmod(dvp, dvm) : dvm * ofx_limo3(dvm, dvp, dxv);
       vR[nv] = q[0] - 0.5 * dv;
       if (nv == RHO || nv == PRS) {
         if (vR[nv] <= 0.0) {
@@ -751,8 +754,49 @@ static void SFX(riemann_emf)(ofx* o) {
 /* ---------------------------------------------------------------------- */
 /* Flux sweep along dir: RiemannSolver::CalcFlux<dir> + K_Store*         */
 /* ---------------------------------------------------------------------- */
+/* ---------------------------------------------------------------------- */
+/* ShockFlattening::FindShock (shockFlattening.hpp:82-168, 185-201):       */
+/* flag cells with div v < 0 and a pressure jump above smoothing x pmin    */
+/* ---------------------------------------------------------------------- */
+static void SFX(find_shock)(ofx* o) {
+  const int kb = o->beg[2] - (OFX_D == 3), ke = o->end[2] + (OFX_D == 3);
+  const size_t si = o->stride[0], sj = o->stride[1], sk = o->stride[2];
+  const double* vx = o->Vc + (size_t)1 * o->ncell;
+  const double* vy = o->Vc + (size_t)2 * o->ncell;
+  const double* p = o->Vc + (size_t)PRS * o->ncell;
+#if OFX_D == 3
+  const double* vz = o->Vc + (size_t)MX3 * o->ncell;
+#endif
+  (void)sk;
+#pragma omp parallel for collapse(2) schedule(static) num_threads(o->nthreads)
+  for (int k = kb; k < ke; k++)
+    for (int j = o->beg[1] - 1; j < o->end[1] + 1; j++)
+      for (int i = o->beg[0] - 1; i < o->end[0] + 1; i++) {
+        const size_t c = OFX_IDX(o, k, j, i);
+        o->flag[c] = 0;
+        double divV = CX((vx[c + si] - vx[c - si]) / (2 * o->dx[0]), + (vy[c + sj] - vy[c - sj]) / (2 * o->dx[1]),
+                         + (vz[c + sk] - vz[c - sk]) / (2 * o->dx[2]));
+        if (divV < 0.0) {
+          double pmin = p[c];
+          pmin = fmin(pmin, p[c + si]);
+          pmin = fmin(pmin, p[c - si]);
+          double gradP = fabs(p[c + si] - p[c - si]);
+          pmin = fmin(pmin, p[c + sj]);
+          pmin = fmin(pmin, p[c - sj]);
+          gradP += fabs(p[c + sj] - p[c - sj]);
+#if OFX_D == 3
+          pmin = fmin(pmin, p[c + sk]);
+          pmin = fmin(pmin, p[c - sk]);
+          gradP += fabs(p[c + sk] - p[c - sk]);
+#endif
+          if (gradP > o->smoothing * pmin) o->flag[c] = 1;
+        }
+      }
+}
+
 static void SFX(calc_flux)(ofx* o, int dir) {
   const int io = dir == 0, jo = dir == 1, ko = dir == 2;
+  if (o->shock) SFX(find_shock)(o);  /* RiemannSolver::CalcFlux (calcFlux.hpp:33) */
   int ext = 1;
   if ((o->emf == OFX_UCT_HLL || o->emf == OFX_UCT_HLLD) && (o->solver == OFX_HLLD || o->solver == OFX_HLL))
     ext = o->ng;

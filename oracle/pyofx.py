@@ -50,6 +50,7 @@ def load(kind="port"):
     lib.ofx_set_time.argtypes = [P, D, D, L]
     lib.ofx_get_time.argtypes = [P, dp, dp, ctypes.POINTER(L)]
     lib.ofx_set_checks.argtypes = [P, I, I, D]
+    lib.ofx_set_shock.argtypes = [P, I, D]
     for f in ("ofx_set_boundaries", "ofx_prim_to_cons", "ofx_cons_to_prim", "ofx_reset_stage"):
         getattr(lib, f).argtypes = [P]
     lib.ofx_evolve_stage.argtypes = [P, D, D]
@@ -77,7 +78,7 @@ class Oracle:
     def __init__(self, dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm",
                  solver="hlld", emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.6,
                  cfl_max_var=1.1, first_dt=1e-4, kind="port", threads=1, log_period=0,
-                 check_nan_period=0, maxdivb=1e-6):
+                 check_nan_period=0, maxdivb=1e-6, shock_flattening=None):
         self.lib = load(kind)
         n = list(n) + [1] * (3 - len(n))
         self.dims, self.n = dims, n
@@ -94,6 +95,8 @@ class Oracle:
         self.ntv = [self.nt[d] + (1 if d < dims else 0) for d in range(3)]
         self.lib.ofx_set_threads(self.h, threads)
         self.lib.ofx_set_checks(self.h, log_period, check_nan_period, maxdivb)
+        if shock_flattening is not None:  # [Hydro] shockFlattening <smoothing>
+            self.lib.ofx_set_shock(self.h, 1, float(shock_flattening))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -52,7 +52,6 @@
 #define FLUID_RIEMANNSOLVER_RIEMANNSOLVER_HPP_
 #define FLUID_CONSTRAINEDTRANSPORT_CONSTRAINEDTRANSPORT_HPP_
 #define FLUID_BOUNDARY_BOUNDARY_HPP_
-#define FLUID_RIEMANNSOLVER_SHOCKFLATTENING_HPP_
 #define FLUID_TRACER_TRACER_HPP_
 #define GRAVITY_GRAVITY_HPP_
 #define DATABLOCK_FARGO_HPP_
@@ -245,16 +244,12 @@ class DataBlock {
   std::unique_ptr<Fargo> fargo;
   bool haveGravity{false};
   std::unique_ptr<Gravity> gravity;
+  real t{0};  // read by ShockFlattening::FindShock's user hook (not used here)
 };
 
 #include "eos.hpp"  // NOLINT  (adiabatic EquationOfState)
 
-enum class FlagShock { None, Shock };
-template <typename Phys>
-class ShockFlattening {
- public:
-  IdefixArray3D<FlagShock> flagArray;
-};
+#include "shockFlattening.hpp"  // NOLINT  (FindShock, real functor)
 
 #include "slopeLimiter.hpp"        // NOLINT
 #include "extrapolateToFaces.hpp"  // NOLINT
@@ -576,6 +571,22 @@ void ofx_get_time(const ofx* o, double* t, double* dt, long* ncycles) {
   if (dt) *dt = o->dt;
   if (ncycles) *ncycles = o->ncycles;
 }
+void ofx_set_shock(ofx* o, int enabled, double smoothing) {
+  // RiemannSolver constructor (riemannSolver.hpp:153-159), then the
+  // extrapolators, which read the flag array when they are built
+  RiemannSolver<Phys>* rs = o->fluid.rSolver.get();
+  rs->haveShockFlattening = enabled != 0;
+  rs->shockFlattening.reset();
+  if (rs->haveShockFlattening) rs->shockFlattening = std::make_unique<ShockFlattening<Phys>>(&o->fluid, smoothing);
+  rs->slopeLimIDIR = std::make_unique<ExtrapolateToFaces<Phys, IDIR>>(rs);
+#if DIMENSIONS >= 2
+  rs->slopeLimJDIR = std::make_unique<ExtrapolateToFaces<Phys, JDIR>>(rs);
+#endif
+#if DIMENSIONS == 3
+  rs->slopeLimKDIR = std::make_unique<ExtrapolateToFaces<Phys, KDIR>>(rs);
+#endif
+}
+
 void ofx_set_checks(ofx* o, int log_period, int check_nan_period, double maxdivb) {
   o->log_period = log_period;
   o->check_nan_period = check_nan_period;
@@ -642,6 +653,7 @@ static void ofx_ref_loopdir(ofx* o, real t, real dt) {
   // Fluid::LoopDir (evolveStage.hpp:13-35) with the RiemannSolver::CalcFlux
   // dispatch of calcFlux.hpp:26-85 (MHD solvers)
   RiemannSolver<Phys>* rs = o->fluid.rSolver.get();
+  if (rs->haveShockFlattening) rs->shockFlattening->FindShock();  // calcFlux.hpp:33
   switch (rs->mySolver) {
     case RiemannSolver<Phys>::TVDLF_MHD: rs->template TvdlfMHD<dir>(o->fluid.FluxRiemann); break;
     case RiemannSolver<Phys>::HLL_MHD: rs->template HllMHD<dir>(o->fluid.FluxRiemann); break;

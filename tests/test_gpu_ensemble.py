@@ -150,3 +150,10 @@ def test_ensemble_2d_mixed_precision():
     res, err, _ = _ensemble(boxes, cycles=6)
     assert err is None
     _assert_same(res, boxes, cycles=6)
+
+
+def test_ensemble_with_shock_flattening():
+    boxes = _mixed_boxes(shock_flattening=0.0)
+    res, err, _ = _ensemble(boxes, cycles=8)
+    assert err is None
+    _assert_same(res, boxes, cycles=8)

@@ -279,3 +279,36 @@ def test_autotuned_segments_keep_results(precision):
     (a, ta), (b, tb) = out
     assert ta == tb
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+SHOCK_GPU = [(dims, order, smoothing) for dims in (2, 3) for order in ("plm", "limo3", "ppm")
+             for smoothing in (0.0, 0.5)]
+
+
+@pytest.mark.parametrize("dims,order,smoothing", SHOCK_GPU)
+def test_gpu_shock_flattening_matches_oracle(dims, order, smoothing):
+    """[Hydro] shockFlattening: flags and minmod slopes bit-identical to the
+    oracle (itself pinned to the reference's FindShock)"""
+    from oracle.pyofx import Oracle
+
+    if dims == 2:
+        n = (48, 48)
+        Vc, Vs = ic.orszag_tang_2d(48, nghost=2)
+    else:
+        n = (12, 12, 12)
+        Vc, Vs = ic.turbulence_3d(12, seed=7, nghost=2, kmax=4)
+    state = extract(dims, n, 2, Vc, Vs)
+    cfl = 0.6 if dims == 2 else 0.4
+    cycles = 30 if dims == 2 else 8
+    o = Oracle(dims, n, order=order, cfl=cfl, first_dt=1e-4, shock_flattening=smoothing)
+    o.set_prim(*embed(dims, n, o.ng, *state))
+    o.run(max_cycles=cycles)
+    ref = extract(dims, n, o.ng, *o.get_prim())
+    blk = ig.GpuBlock(dims, n, order=order, cfl=cfl, first_dt=1e-4, shock_flattening=smoothing)
+    blk.upload(*embed(dims, n, blk.ng, *state))
+    blk.run(max_cycles=cycles)
+    out = extract(dims, n, blk.ng, *blk.download())
+    assert np.array_equal(out[0], ref[0])
+    for c in range(dims):
+        assert np.array_equal(out[1][c], ref[1][c])
+    assert blk.get_time()[:2] == o.get_time()[:2]
