@@ -34,6 +34,7 @@ struct ofx {
   double *ezi, *ezj, *exj, *exk, *eyi, *eyk, *svx, *svy, *svz;
   double *Ex1, *Ex2, *Ex3, *ex, *ey, *ez;
   double *aL[3], *aR[3], *dL[3], *dR[3];
+  int lbound[3], rbound[3]; /* 0 periodic, 1 reflective, 2 outflow    */
   int shock;            /* [Hydro] shockFlattening present              */
   double smoothing;     /* its value                                    */
   unsigned char* flag;  /* FlagShock per cell (1 = Shock), zero outside */
@@ -171,10 +172,89 @@ static void ofx_reconstruct_vc_field(ofx* o, double* arr) {
 /* ---------------------------------------------------------------------- */
 static int ofx_wrap(int i, int g, int n) { return g + (i + g * (n - 1)) % n; }
 
+/* reference index of a ghost point along dir for one boundary type
+   (boundary.hpp:582-600 periodic, 687-689 reflective, 750-752 outflow);
+   n: active cells along dir, side 0 left / 1 right */
+static int ofx_bc_ref(int type, int idx, int g, int n, int side) {
+  if (type == 0) return ofx_wrap(idx, g, n);
+  if (type == 1) return 2 * (g + side * n) - idx - 1;
+  return g + side * (n - 1);
+}
+
+/* ReconstructNormalField (boundary.hpp:408-532): the normal field in the
+   ghost faces of dir from div B = 0, outwards from the boundary face */
+static void ofx_normal_field(ofx* o, int dir) {
+  const int left = o->lbound[dir] != 0, right = o->rbound[dir] != 0;
+  if (!left && !right) return;
+  double* V1 = o->Vs;
+  double* V2 = o->Vs + o->nface;
+  double* V3 = o->D == 3 ? o->Vs + 2 * o->nface : 0;
+  const double A1 = o->A[0], A2 = o->A[1], A3 = o->A[2];
+  const int nb = o->beg[dir] - 1, ne = o->end[dir];
+#define F1(k, j, i) V1[OFX_FIDX(o, k, j, i)]
+#define F2(k, j, i) V2[OFX_FIDX(o, k, j, i)]
+#define F3(k, j, i) V3[OFX_FIDX(o, k, j, i)]
+  if (dir == 0) {
+    for (int k = 0; k < o->nt[2]; k++)
+      for (int j = 0; j < o->nt[1]; j++) {
+        if (left)
+          for (int i = nb; i >= 0; i--) {
+            double t = 0.0 + A2 * F2(k, j + 1, i) - A2 * F2(k, j, i);
+            if (o->D == 3) t = t + A3 * F3(k + 1, j, i) - A3 * F3(k, j, i);
+            F1(k, j, i) = 1.0 / A1 * (A1 * F1(k, j, i + 1) + (t));
+          }
+        if (right)
+          for (int i = ne; i < o->nt[0]; i++) {
+            double t = 0.0 + A2 * F2(k, j + 1, i) - A2 * F2(k, j, i);
+            if (o->D == 3) t = t + A3 * F3(k + 1, j, i) - A3 * F3(k, j, i);
+            F1(k, j, i + 1) = 1.0 / A1 * (A1 * F1(k, j, i) - (t));
+          }
+      }
+  } else if (dir == 1) {
+    for (int k = 0; k < o->nt[2]; k++)
+      for (int i = 0; i < o->nt[0]; i++) {
+        if (left)
+          for (int j = nb; j >= 0; j--) {
+            double t = A1 * F1(k, j, i + 1) - A1 * F1(k, j, i);
+            if (o->D == 3) t = t + 1 * (A3 * F3(k + 1, j, i) - A3 * F3(k, j, i));
+            F2(k, j, i) = 1.0 / A2 * (A2 * F2(k, j + 1, i) + (t));
+          }
+        if (right)
+          for (int j = ne; j < o->nt[1]; j++) {
+            double t = A1 * F1(k, j, i + 1) - A1 * F1(k, j, i);
+            if (o->D == 3) t = t + 1 * (A3 * F3(k + 1, j, i) - A3 * F3(k, j, i));
+            F2(k, j + 1, i) = 1.0 / A2 * (A2 * F2(k, j, i) - (t));
+          }
+      }
+  } else {
+    for (int j = 0; j < o->nt[1]; j++)
+      for (int i = 0; i < o->nt[0]; i++) {
+        if (left)
+          for (int k = nb; k >= 0; k--) {
+            F3(k, j, i) = 1.0 / A3 * (A3 * F3(k + 1, j, i) + (A1 * F1(k, j, i + 1) - A1 * F1(k, j, i) +
+                                                              A2 * F2(k, j + 1, i) - A2 * F2(k, j, i)));
+          }
+        if (right)
+          for (int k = ne; k < o->nt[2]; k++) {
+            F3(k + 1, j, i) = 1.0 / A3 * (A3 * F3(k, j, i) - (A1 * F1(k, j, i + 1) - A1 * F1(k, j, i) +
+                                                              A2 * F2(k, j + 1, i) - A2 * F2(k, j, i)));
+          }
+      }
+  }
+#undef F1
+#undef F2
+#undef F3
+}
+
+/* Boundary::SetBoundaries (boundary.hpp:240-280): per direction, both sides
+   of the cell-centred variables and of the face field (BoundaryFor* ranges,
+   boundary.hpp:971-1100), then the normal field; finally the cell field. */
 void ofx_set_boundaries(ofx* o) {
   const int g = o->ng;
+  const int BX1v = o->D + 2;
   for (int dir = 0; dir < o->D; dir++) {
     for (int side = 0; side < 2; side++) {
+      const int type = side ? o->rbound[dir] : o->lbound[dir];
       /* cell-centred: BoundaryForAll */
       int lo[3], hi[3];
       for (int d = 0; d < 3; d++) {
@@ -185,18 +265,32 @@ void ofx_set_boundaries(ofx* o) {
       hi[dir] = g + side * (g + o->n[dir]);
       for (int nv = 0; nv < o->nvar; nv++) {
         double* a = o->Vc + (size_t)nv * o->ncell;
+        /* reflective: normal velocity and tangential field change sign */
+        const int sign = (nv == 1 + dir || (nv >= BX1v && nv != BX1v + dir)) ? -1 : 1;
         for (int k = lo[2]; k < hi[2]; k++)
           for (int j = lo[1]; j < hi[1]; j++)
             for (int i = lo[0]; i < hi[0]; i++) {
-              int ir = dir == 0 ? ofx_wrap(i, g, o->n[0]) : i;
-              int jr = dir == 1 ? ofx_wrap(j, g, o->n[1]) : j;
-              int kr = dir == 2 ? ofx_wrap(k, g, o->n[2]) : k;
-              a[OFX_IDX(o, k, j, i)] = a[OFX_IDX(o, kr, jr, ir)];
+              const int ir = dir == 0 ? ofx_bc_ref(type, i, g, o->n[0], side) : i;
+              const int jr = dir == 1 ? ofx_bc_ref(type, j, g, o->n[1], side) : j;
+              const int kr = dir == 2 ? ofx_bc_ref(type, k, g, o->n[2], side) : k;
+              const double src = a[OFX_IDX(o, kr, jr, ir)];
+              double* dst = &a[OFX_IDX(o, k, j, i)];
+              if (type == 0) {
+                *dst = src;
+              } else if (type == 1) {
+                *dst = sign * src;
+              } else {
+                /* outflow: no inflow through the boundary (boundary.hpp:757-762) */
+                const int sg = 1 - 2 * side;
+                if (nv == 1 + dir && sg * src >= 0.0) *dst = 0.0;
+                else *dst = src;
+              }
             }
       }
-      /* face-centred: BoundaryForX{1,2,3}s; the component's own direction
-         has n+1 faces in the loop bounds, but the wrap uses n */
+      /* face-centred: BoundaryForX{1,2,3}s; periodic copies every component,
+         the others only the tangential ones (the normal one is rebuilt) */
       for (int comp = 0; comp < o->D; comp++) {
+        if (type != 0 && comp == dir) continue;
         int flo[3], fhi[3];
         for (int d = 0; d < 3; d++) {
           int nn = o->n[d] + (d == comp);
@@ -212,15 +306,25 @@ void ofx_set_boundaries(ofx* o) {
         for (int k = flo[2]; k < fhi[2]; k++)
           for (int j = flo[1]; j < fhi[1]; j++)
             for (int i = flo[0]; i < fhi[0]; i++) {
-              int ir = dir == 0 ? ofx_wrap(i, g, o->n[0]) : i;
-              int jr = dir == 1 ? ofx_wrap(j, g, o->n[1]) : j;
-              int kr = dir == 2 ? ofx_wrap(k, g, o->n[2]) : k;
-              a[OFX_FIDX(o, k, j, i)] = a[OFX_FIDX(o, kr, jr, ir)];
+              const int ir = dir == 0 ? ofx_bc_ref(type, i, g, o->n[0], side) : i;
+              const int jr = dir == 1 ? ofx_bc_ref(type, j, g, o->n[1], side) : j;
+              const int kr = dir == 2 ? ofx_bc_ref(type, k, g, o->n[2], side) : k;
+              const double src = a[OFX_FIDX(o, kr, jr, ir)];
+              a[OFX_FIDX(o, k, j, i)] = (type == 1) ? -src : src;
             }
       }
     }
+    ofx_normal_field(o, dir);
   }
   ofx_reconstruct_vc_field(o, o->Vc);
+}
+
+int ofx_set_bc(ofx* o, int dir, int left, int right) {
+  if (dir < 0 || dir >= o->D || left < 0 || left > 2 || right < 0 || right > 2) return OFX_ERR_CONFIG;
+  if ((left == 0) != (right == 0)) return OFX_ERR_CONFIG;
+  o->lbound[dir] = left;
+  o->rbound[dir] = right;
+  return OFX_OK;
 }
 
 /* ---------------------------------------------------------------------- */

@@ -63,6 +63,10 @@ void   ofx_set_checks(ofx* o, int log_period, int check_nan_period, double maxdi
  * flagged by ShockFlattening::FindShock use the minmod slope */
 void   ofx_set_shock(ofx* o, int enabled, double smoothing);
 
+/* [Boundary] X?-beg / X?-end of direction dir: 0 periodic, 1 reflective,
+ * 2 outflow (periodic on both sides or on neither); returns a status */
+int    ofx_set_bc(ofx* o, int dir, int left, int right);
+
 /* building blocks (one call = one reference method) */
 void   ofx_set_boundaries(ofx* o);                 /* Boundary::SetBoundaries       */
 void   ofx_prim_to_cons(ofx* o);                   /* Fluid::ConvertPrimToCons      */

@@ -51,6 +51,8 @@ def load(kind="port"):
     lib.ofx_get_time.argtypes = [P, dp, dp, ctypes.POINTER(L)]
     lib.ofx_set_checks.argtypes = [P, I, I, D]
     lib.ofx_set_shock.argtypes = [P, I, D]
+    lib.ofx_set_bc.restype = I
+    lib.ofx_set_bc.argtypes = [P, I, I, I]
     for f in ("ofx_set_boundaries", "ofx_prim_to_cons", "ofx_cons_to_prim", "ofx_reset_stage"):
         getattr(lib, f).argtypes = [P]
     lib.ofx_evolve_stage.argtypes = [P, D, D]
@@ -72,13 +74,18 @@ def _ptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
+BOUNDARY = {"periodic": 0, "reflective": 1, "outflow": 2}
+
+
 class Oracle:
-    """One periodic Cartesian block driven by the CPU oracle."""
+    """One Cartesian block driven by the CPU oracle.  ``bc`` gives, per
+    direction, the (X?-beg, X?-end) boundary types of the reference's
+    [Boundary] block ("periodic", "reflective", "outflow"); default periodic."""
 
     def __init__(self, dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm",
                  solver="hlld", emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.6,
                  cfl_max_var=1.1, first_dt=1e-4, kind="port", threads=1, log_period=0,
-                 check_nan_period=0, maxdivb=1e-6, shock_flattening=None):
+                 check_nan_period=0, maxdivb=1e-6, shock_flattening=None, bc=None):
         self.lib = load(kind)
         n = list(n) + [1] * (3 - len(n))
         self.dims, self.n = dims, n
@@ -97,6 +104,9 @@ class Oracle:
         self.lib.ofx_set_checks(self.h, log_period, check_nan_period, maxdivb)
         if shock_flattening is not None:  # [Hydro] shockFlattening <smoothing>
             self.lib.ofx_set_shock(self.h, 1, float(shock_flattening))
+        for d, sides in enumerate(bc or ()):
+            if self.lib.ofx_set_bc(self.h, d, BOUNDARY[sides[0]], BOUNDARY[sides[1]]) != 0:
+                raise ValueError(f"invalid boundary pair {sides} in direction {d}")
 
     def __del__(self):
         if getattr(self, "h", None):

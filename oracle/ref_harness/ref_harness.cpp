@@ -51,7 +51,7 @@
 #define DATABLOCK_DATABLOCK_HPP_
 #define FLUID_RIEMANNSOLVER_RIEMANNSOLVER_HPP_
 #define FLUID_CONSTRAINEDTRANSPORT_CONSTRAINEDTRANSPORT_HPP_
-#define FLUID_BOUNDARY_BOUNDARY_HPP_
+#define FLUID_BOUNDARY_AXIS_HPP_
 #define FLUID_TRACER_TRACER_HPP_
 #define GRAVITY_GRAVITY_HPP_
 #define DATABLOCK_FARGO_HPP_
@@ -108,6 +108,11 @@ template <typename T> using IdefixHostArray4D = HostView<T, 4>;
 template <typename F>
 inline void idefix_for(const std::string&, int ib, int ie, F f) {
   for (int i = ib; i < ie; i++) f(i);
+}
+template <typename F>
+inline void idefix_for(const std::string&, int jb, int je, int ib, int ie, F f) {
+  for (int j = jb; j < je; j++)
+    for (int i = ib; i < ie; i++) f(j, i);
 }
 template <typename F>
 inline void idefix_for(const std::string&, int kb, int ke, int jb, int je, int ib, int ie, F f) {
@@ -178,10 +183,14 @@ inline std::ostream& cout = std::cout;
 struct OfxRefError {
   std::string msg;
 };
+// messages are strings or string streams (both forms appear in the bodies)
+inline std::string ofx_msg(const std::stringstream& m) { return m.str(); }
+template <typename T>
+inline const T& ofx_msg(const T& m) { return m; }
 #define IDEFIX_ERROR(m)                \
   do {                                 \
     std::stringstream ofx_ss;          \
-    ofx_ss << m;                       \
+    ofx_ss << ofx_msg(m);              \
     throw OfxRefError{ofx_ss.str()};   \
   } while (0)
 #define IDEFIX_WARNING(m) do {} while (0)
@@ -211,6 +220,10 @@ class Input {
 
 struct Grid {
   bool isRegularCartesian{true};
+  std::array<real, 3> xbeg{{0, 0, 0}}, xend{{1, 1, 1}};
+  std::array<int, 3> np_int{{1, 1, 1}};
+  std::array<int, 3> nproc{{1, 1, 1}};
+  std::array<int, 3> xproc{{0, 0, 0}};
 };
 
 class Fargo {
@@ -245,6 +258,9 @@ class DataBlock {
   bool haveGravity{false};
   std::unique_ptr<Gravity> gravity;
   real t{0};  // read by ShockFlattening::FindShock's user hook (not used here)
+  std::array<BoundaryType, 3> lbound{{periodic, periodic, periodic}};
+  std::array<BoundaryType, 3> rbound{{periodic, periodic, periodic}};
+  bool haveAxis{false};
 };
 
 #include "eos.hpp"  // NOLINT  (adiabatic EquationOfState)
@@ -301,24 +317,19 @@ class ConstrainedTransport {
   Fluid<Phys>* hydro;
 };
 
-template <typename Phys>
-class Boundary {
+// the axis is never used here (Cartesian): the members Boundary names
+class Axis {
  public:
-  bool haveFluxBoundary{false};
-  void EnforceFluxBoundaries(int, real) {}
-  IdefixArray4D<real> Vs;
-  DataBlock* data;
-  // restated from src/fluid/boundary/boundary.hpp:388-404
-  void ReconstructVcField(IdefixArray4D<real>& Vc) {
-    IdefixArray4D<real> Vs = this->Vs;
-    idefix_for("ReconstructVcMagField", 0, data->np_tot[KDIR], 0, data->np_tot[JDIR], 0,
-               data->np_tot[IDIR], KOKKOS_LAMBDA(int k, int j, int i) {
-                 D_EXPAND(Vc(BX1, k, j, i) = HALF_F * (Vs(BX1s, k, j, i) + Vs(BX1s, k, j, i + 1));,
-                          Vc(BX2, k, j, i) = HALF_F * (Vs(BX2s, k, j, i) + Vs(BX2s, k, j + 1, i));,
-                          Vc(BX3, k, j, i) = HALF_F * (Vs(BX3s, k, j, i) + Vs(BX3s, k + 1, j, i));)
-               });
-  }
+  template <typename B>
+  explicit Axis(B*) {}
+  bool haveLeftAxis() { return false; }
+  bool haveRightAxis() { return false; }
+  void EnforceAxisBoundary(int) {}
+  void RegularizeBX2s() {}
+  void RegularizeEMFs() {}
 };
+
+#include "boundary.hpp"  // NOLINT  (Boundary<Phys>: SetBoundaries, Enforce*, ReconstructNormalField)
 
 class Tracer {
  public:
@@ -356,6 +367,8 @@ class Fluid {
   real sbS{0};
   std::unique_ptr<Tracer> tracer;
   bool haveTracer{false};
+  int nTracer{0};
+  std::string prefix{"Hydro"};
   IdefixArray4D<real> Vc, Vs, Uc, J;
   std::unique_ptr<ConstrainedTransport<Phys>> emf;
   IdefixArray3D<real> InvDt;
@@ -471,9 +484,7 @@ static void ofx_ref_alloc(ofx* o, const int n[3], const double xb[3], const doub
   f.Vs = IdefixArray4D<real>("Vs", DIMENSIONS, nk + KOFFSET, nj + JOFFSET, ni + IOFFSET);
   o->Uc0 = IdefixArray4D<real>("Uc0", Phys::nvar, nk, nj, ni);
   o->Vs0 = IdefixArray4D<real>("Vs0", DIMENSIONS, nk + KOFFSET, nj + JOFFSET, ni + IOFFSET);
-  f.boundary = std::make_unique<Boundary<Phys>>();
-  f.boundary->Vs = f.Vs;
-  f.boundary->data = &d;
+  f.boundary = std::make_unique<Boundary<Phys>>(&f);  // boundary.hpp:128-190
   f.tracer = std::make_unique<Tracer>();
   f.viscosity = std::make_unique<Viscosity>();
   f.bragViscosity = std::make_unique<BragViscosity>();
@@ -596,46 +607,18 @@ void ofx_set_checks(ofx* o, int log_period, int check_nan_period, double maxdivb
 // Boundary::SetBoundaries for periodic boxes: EnforcePeriodic per direction,
 // left then right, then ReconstructVcField (restated from
 // src/fluid/boundary/boundary.hpp:240-282,576-673,969-1099)
-void ofx_set_boundaries(ofx* o) {
-  DataBlock& d = o->data;
-  auto Vc = o->fluid.Vc;
-  auto Vs = o->fluid.Vs;
-  for (int dir = 0; dir < DIMENSIONS; dir++) {
-    for (int side = 0; side < 2; side++) {
-      const int nxi = d.np_int[IDIR], nxj = d.np_int[JDIR], nxk = d.np_int[KDIR];
-      const int ig = d.nghost[IDIR], jg = d.nghost[JDIR], kg = d.nghost[KDIR];
-      auto ref = [&](int k, int j, int i, int& kr, int& jr, int& ir) {
-        ir = (dir == IDIR) ? ig + (i + ig * (nxi - 1)) % nxi : i;
-        jr = (dir == JDIR) ? jg + (j + jg * (nxj - 1)) % nxj : j;
-        kr = (dir == KDIR) ? kg + (k + kg * (nxk - 1)) % nxk : k;
-      };
-      for (int comp = -1; comp < DIMENSIONS; comp++) {
-        // comp = -1: cell-centred variables; comp >= 0: face component
-        int lo[3], hi[3];
-        for (int dd = 0; dd < 3; dd++) {
-          const int nn = d.np_int[dd] + (dd == comp);
-          lo[dd] = 0;
-          hi[dd] = d.np_tot[dd] + (dd == comp);
-          if (dd == dir) {
-            lo[dd] = side * (d.nghost[dd] + nn);
-            hi[dd] = d.nghost[dd] + side * (d.nghost[dd] + nn);
-          }
-        }
-        for (int k = lo[KDIR]; k < hi[KDIR]; k++)
-          for (int j = lo[JDIR]; j < hi[JDIR]; j++)
-            for (int i = lo[IDIR]; i < hi[IDIR]; i++) {
-              int kr, jr, ir;
-              ref(k, j, i, kr, jr, ir);
-              if (comp < 0) {
-                for (int nv = 0; nv < Phys::nvar; nv++) Vc(nv, k, j, i) = Vc(nv, kr, jr, ir);
-              } else {
-                Vs(comp, k, j, i) = Vs(comp, kr, jr, ir);
-              }
-            }
-      }
-    }
-  }
-  o->fluid.boundary->ReconstructVcField(o->fluid.Vc);
+void ofx_set_boundaries(ofx* o) {  // Boundary::SetBoundaries (boundary.hpp:240-280)
+  o->fluid.boundary->SetBoundaries(o->t);
+}
+
+// [Boundary] X?-beg / X?-end: 0 periodic, 1 reflective, 2 outflow
+int ofx_set_bc(ofx* o, int dir, int left, int right) {
+  static const BoundaryType map[] = {periodic, reflective, outflow};
+  if (dir < 0 || dir >= DIMENSIONS || left < 0 || left > 2 || right < 0 || right > 2) return OFX_ERR_CONFIG;
+  if ((left == 0) != (right == 0)) return OFX_ERR_CONFIG;  // periodic on both sides or neither
+  o->data.lbound[dir] = map[left];
+  o->data.rbound[dir] = map[right];
+  return OFX_OK;
 }
 
 void ofx_prim_to_cons(ofx* o) { o->fluid.ConvertPrimToCons(); }
