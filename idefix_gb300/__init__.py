@@ -60,7 +60,13 @@ class Config(ctypes.Structure):
         ("precision", ctypes.c_int),
         ("shock_flattening", ctypes.c_int),
         ("shock_smoothing", ctypes.c_double),
+        ("lbound", ctypes.c_int * 3),
+        ("rbound", ctypes.c_int * 3),
     ]
+
+
+# [Boundary] types (BoundaryType, idefix.hpp:220)
+BOUNDARY = {"periodic": 0, "reflective": 1, "outflow": 2}
 
 
 EXPORTS = [
@@ -219,7 +225,7 @@ def read_dump(path, cfg):
 def make_config(dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm", solver="hlld",
                 emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.9, cfl_max_var=1.1,
                 first_dt=1.0e-10, maxdivb=1e-6, log_period=0, check_nan_period=0, precision="fp64",
-                shock_flattening=None):
+                shock_flattening=None, bc=None):
     """idfx_gpu_config from the input-file style arguments of GpuBlock."""
     lib = load_library()
     n = list(n) + [1] * (3 - len(n))
@@ -239,6 +245,11 @@ def make_config(dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm"
     cfg.log_period, cfg.check_nan_period = log_period, check_nan_period
     if shock_flattening is not None:  # [Hydro] shockFlattening <smoothing>
         cfg.shock_flattening, cfg.shock_smoothing = 1, float(shock_flattening)
+    for d, sides in enumerate(bc or ()):  # [Boundary] X?-beg, X?-end
+        try:
+            cfg.lbound[d], cfg.rbound[d] = BOUNDARY[sides[0]], BOUNDARY[sides[1]]
+        except KeyError as exc:
+            raise IdefixError(f"unknown boundary type {exc}") from None
     return cfg
 
 
@@ -247,10 +258,12 @@ def _as_ptr(a):
 
 
 class GpuBlock:
-    """One periodic Cartesian block advanced on the GPU.
+    """One Cartesian block advanced on the GPU.
 
     Arguments mirror the reference's input file: [Grid] (dims, n, xbeg,
-    xend), [Hydro] (solver, emf, gamma), [TimeIntegrator] (nstages, CFL,
+    xend), [Hydro] (solver, emf, gamma, shockFlattening), [Boundary] (bc:
+    per direction the (beg, end) pair of "periodic", "reflective",
+    "outflow"; default periodic), [TimeIntegrator] (nstages, CFL,
     CFL_max_var, first_dt, maxdivB, check_nan), [Output] log, and the
     build-time reconstruction order.  precision: "fp64" (bit-identical to
     the reference) or "mixed" (FP32 reconstruction and Riemann solve, FP64
@@ -260,11 +273,12 @@ class GpuBlock:
     def __init__(self, dims, n, xbeg=(0.0, 0.0, 0.0), xend=(1.0, 1.0, 1.0), order="plm",
                  solver="hlld", emf="uct_contact", nstages=2, gamma=5.0 / 3.0, cfl=0.9,
                  cfl_max_var=1.1, first_dt=1.0e-10, maxdivb=1e-6, log_period=0,
-                 check_nan_period=0, precision="fp64", stream=None, shock_flattening=None):
+                 check_nan_period=0, precision="fp64", stream=None, shock_flattening=None, bc=None):
         self.lib = load_library()
         n = list(n) + [1] * (3 - len(n))
         cfg = make_config(dims, n, xbeg, xend, order, solver, emf, nstages, gamma, cfl, cfl_max_var,
-                          first_dt, maxdivb, log_period, check_nan_period, precision, shock_flattening)
+                          first_dt, maxdivb, log_period, check_nan_period, precision, shock_flattening,
+                          bc)
         h = ctypes.c_void_p()
         rc = self.lib.idfx_gpu_create(ctypes.byref(cfg), ctypes.c_void_p(stream), ctypes.byref(h))
         if rc != OK:

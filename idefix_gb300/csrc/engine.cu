@@ -186,6 +186,22 @@ void launch_fill_faces(Engine& e, int save_begin) {
   IDFX_DISPATCH_D(k_fill_faces, grid, kThreads, e.g, e.f, e.ctl, save_begin);
   mark_end(e);
 }
+// Boundary::SetBoundaries of a block with a reflective or outflow direction
+void launch_boundaries(Engine& e) {
+  if (!e.g.nonper) return;
+  for (int dir = 0; dir < e.g.D; dir++) {
+    const int a = (dir == 0) ? 1 : 0, b = (dir == 2) ? 1 : 2;
+    mark_begin(e, kKFillFaces);
+    dim3 grid(nblocks(2LL * e.g.ng * e.g.ntv[a] * e.g.ntv[b]), 1 + e.g.D);
+    IDFX_DISPATCH_D(k_bc_slab, grid, kThreads, e.g, e.f, e.ctl, dir);
+    mark_end(e);
+    if (e.g.bc[dir][0] != 0) {
+      mark_begin(e, kKFillFaces);
+      IDFX_DISPATCH_D(k_normal_field, nblocks((long long)e.g.nt[a] * e.g.nt[b]), kThreads, e.g, e.f, e.ctl, dir);
+      mark_end(e);
+    }
+  }
+}
 void launch_stage_begin(Engine& e, int flags) {
   mark_begin(e, kKStageBegin);
   IDFX_DISPATCH_D(k_stage_begin, nblocks(e.g.ncell), kThreads, e.g, e.f, e.ctl, flags);
@@ -226,6 +242,7 @@ void queue_cycle(Engine& e, int use_tstop) {
   const bool nan_check = e.check_nan_period > 0 && e.ncycles % e.check_nan_period == 0;
   for (int stage = 0; stage < e.nstages; stage++) {
     const int save = (e.nstages > 1 && stage == 0);
+    launch_boundaries(e);
     launch_fill_faces(e, save);
     launch_stage_begin(e, kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
     if (e.f.shock) launch_find_shock(e);  // RiemannSolver::CalcFlux (calcFlux.hpp:33)
@@ -283,6 +300,19 @@ int choose_segments(Engine& e) {
 
 }  // namespace
 
+// Boundary types per direction: IDFX_BC_* on both sides, periodic on both or
+// on neither; a mirror (reflective) needs as many active cells as ghosts.
+static bool boundaries_valid(const idfx_gpu_config* cfg) {
+  const int ng = (cfg->order == 4) ? 3 : 2;
+  for (int d = 0; d < cfg->dims; d++) {
+    const int l = cfg->lbound[d], r = cfg->rbound[d];
+    if (l < IDFX_BC_PERIODIC || l > IDFX_BC_OUTFLOW || r < IDFX_BC_PERIODIC || r > IDFX_BC_OUTFLOW) return false;
+    if ((l == IDFX_BC_PERIODIC) != (r == IDFX_BC_PERIODIC)) return false;
+    if ((l == IDFX_BC_REFLECTIVE || r == IDFX_BC_REFLECTIVE) && cfg->n[d] < ng) return false;
+  }
+  return true;
+}
+
 // ===========================================================================
 // C ABI
 // ===========================================================================
@@ -328,6 +358,7 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
     return IDFX_ERR_CONFIG;
   for (int d = 0; d < cfg->dims; d++)
     if (cfg->n[d] < 2 || !(cfg->xend[d] > cfg->xbeg[d])) return IDFX_ERR_CONFIG;
+  if (!boundaries_valid(cfg)) return IDFX_ERR_CONFIG;
   idfx_gpu* h = new (std::nothrow) idfx_gpu();
   if (!h) return IDFX_ERR_STATE;
   Engine& e = h->e;
@@ -371,6 +402,12 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   g.ext = 1;  // hlldMHD.hpp:30-49: uct_hll(d) with HLLD/HLL needs nghost cells
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
   g.shock_smoothing = cfg->shock_smoothing;
+  g.nonper = 0;
+  for (int d = 0; d < 3; d++) {
+    g.bc[d][0] = d < g.D ? cfg->lbound[d] : 0;
+    g.bc[d][1] = d < g.D ? cfg->rbound[d] : 0;
+    if (g.bc[d][0] || g.bc[d][1]) g.nonper = 1;
+  }
   e.nstages = cfg->nstages;
   e.precision = cfg->precision;
   if (e.nstages == 2) {  // timeIntegrator.cpp:62-71
@@ -719,6 +756,7 @@ int idfx_gpu_set_boundaries(idfx_gpu* h) {
   if (!h) return IDFX_ERR_STATE;
   Engine& e = h->e;
   clear_done(e);
+  launch_boundaries(e);
   launch_fill_faces(e, 0);
   launch_stage_begin(e, 0);
   return sync_status(e);

@@ -270,6 +270,8 @@ int read_ctl(EnsEngine& e) {
 // geometry of one box, as idfx_gpu_create sets it up
 bool box_geometry(const idfx_gpu_config* cfg, Geo& g) {
   if (cfg->dims != 2 && cfg->dims != 3) return false;
+  for (int d = 0; d < 3; d++)  // the boxes are periodic
+    if (cfg->lbound[d] || cfg->rbound[d]) return false;
   for (int d = 0; d < cfg->dims; d++)
     if (cfg->n[d] < 2 || !(cfg->xend[d] > cfg->xbeg[d])) return false;
   g.D = cfg->dims;
@@ -311,6 +313,8 @@ bool box_geometry(const idfx_gpu_config* cfg, Geo& g) {
   g.ext = 1;
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
   g.shock_smoothing = cfg->shock_smoothing;
+  for (int d = 0; d < 3; d++) g.bc[d][0] = g.bc[d][1] = 0;
+  g.nonper = 0;
   return true;
 }
 

@@ -41,6 +41,8 @@ struct Geo {
   double gamma, gm1;
   int ext;  // perpendicular extension of the flux sweeps for CT
   double shock_smoothing;  // [Hydro] shockFlattening value (flags in Fields::shock)
+  int bc[3][2];  // boundary type per direction and side (IDFX_BC_*: 0 periodic)
+  int nonper;    // some direction is not periodic: ghosts filled by k_bc_* first
 };
 
 // Device-resident time-integrator control block.
@@ -120,7 +122,7 @@ __device__ __forceinline__ void d_fill_faces(const Geo& g, const Fields& f, cons
   double* vs = f.Vs + (long long)comp * g.nface;
   const long long fi = fidx(g, k, j, i);
   if (ghost) {
-    vs[fi] = vs[fidx(g, src[2], src[1], src[0])];
+    if (!g.nonper) vs[fi] = vs[fidx(g, src[2], src[1], src[0])];
   } else if (save_begin) {
     f.Vs0[(long long)comp * g.nface + fi] = vs[fi];
   }
@@ -156,9 +158,10 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
   for (int d = 0; d < D; d++) {
     if (idx3[d] < g.beg[d] || idx3[d] >= g.end[d]) {
       ghost = true;
-      src[d] = wrap(idx3[d], g.ng, g.n[d]);
+      if (!g.nonper) src[d] = wrap(idx3[d], g.ng, g.n[d]);
     }
   }
+  const bool copy = ghost && !g.nonper;  // else the ghosts are already filled
   double V[NV];
   const long long cs = cidx(g, src[2], src[1], src[0]);
 #pragma unroll
@@ -169,7 +172,7 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
     const double* vs = f.Vs + d * g.nface;
     V[v::BX1 + d] = 0.5 * (vs[fc] + vs[fc + g.fs[d]]);
   }
-  if (ghost) {
+  if (copy) {
 #pragma unroll
     for (int n = 0; n < v::BX1; n++) f.Vc[n * g.ncell + c] = V[n];
   }
@@ -204,6 +207,157 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
 template <int D>
 __global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
   d_stage_begin<D>(g, f, ctl, flags, blockIdx);
+}
+
+// ---------------------------------------------------------------------------
+// Non-periodic blocks: Boundary::SetBoundaries (boundary.hpp:240-280) one
+// direction after the other, each direction's pass reading what the passes
+// of the previous directions wrote (its loops span their ghosts too):
+//   k_bc_slab(dir)     ghost cells of the non-field variables and ghost faces
+//                      (both sides; boundary.hpp:575-809, loop ranges of
+//                      BoundaryForAll / BoundaryForX?s, boundary.hpp:971-1100)
+//   k_normal_field(dir) the normal field in the ghost faces of a reflective or
+//                      outflow direction from div B = 0, marching outwards
+//                      (ReconstructNormalField, boundary.hpp:408-532)
+// then fill_faces / stage_begin run without the periodic copy.  The cell-
+// centred field of the ghosts is not copied: stage_begin rebuilds it from the
+// faces everywhere (ReconstructVcField, boundary.hpp:388-404).
+// ---------------------------------------------------------------------------
+// source index of ghost idx along a direction: periodic image, mirror
+// (2 ibound - i - 1) or the last active cell (boundary.hpp:582-600, 687-689,
+// 750-752); n active cells, side 0 left / 1 right
+__device__ __forceinline__ int bc_src(int type, int idx, int ng, int n, int side) {
+  if (type == 0) return wrap(idx, ng, n);
+  if (type == 1) return 2 * (ng + side * n) - idx - 1;
+  return ng + side * (n - 1);
+}
+
+// One thread per location of the two ghost slabs of dir (side, depth, and the
+// full extent of the two other directions); blockIdx.y = 0 the cells, 1 + c
+// the faces of component c.
+template <int D>
+__device__ __forceinline__ void d_bc_slab(const Geo& g, const Fields& f, const Ctl* ctl, int dir, dim3 bid) {
+  if (ctl->done) return;
+  using v = Var<D>;
+  const int a = (dir == 0) ? 1 : 0, b = (dir == 2) ? 1 : 2;  // the two other directions
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
+  const long long per_side = (long long)g.ng * g.ntv[a] * g.ntv[b];
+  if (tid >= 2 * per_side) return;
+  const int side = (int)(tid / per_side);
+  long long r = tid - side * per_side;
+  const int depth = (int)(r % g.ng);
+  r /= g.ng;
+  const int ia = (int)(r % g.ntv[a]);
+  const int ib = (int)(r / g.ntv[a]);
+  const int type = g.bc[dir][side];
+  const int comp = (int)bid.y - 1;  // -1: cells
+  // extents of the array along a and b (faces: one more along their own direction)
+  const int ea = g.nt[a] + (comp == a ? 1 : 0), eb = g.nt[b] + (comp == b ? 1 : 0);
+  if (ia >= ea || ib >= eb) return;
+  // along dir: ghosts [0, ng) on the left; on the right [ng + n, 2 ng + n) for
+  // cells and tangential faces, one further for the normal faces
+  const int shift = (comp == dir) ? 1 : 0;
+  if (comp == dir && type != 0) return;  // rebuilt by k_normal_field
+  const int id = side ? g.ng + g.n[dir] + shift + depth : depth;
+  const int is = bc_src(type, id, g.ng, g.n[dir], side);
+  int dst[3], src[3];
+  dst[dir] = id;
+  src[dir] = is;
+  dst[a] = src[a] = ia;
+  dst[b] = src[b] = ib;
+  if (comp < 0) {
+    const long long cd = cidx(g, dst[2], dst[1], dst[0]), cs = cidx(g, src[2], src[1], src[0]);
+    const double sg = (double)(1 - 2 * side);
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) {
+      const double x = f.Vc[n * g.ncell + cs];
+      double y = x;
+      if (type == 1) {
+        if (n == v::MX1 + dir) y = -x;  // only the normal velocity: no field here
+      } else if (type == 2) {
+        if (n == v::MX1 + dir && sg * x >= 0.0) y = 0.0;  // no inflow (boundary.hpp:757-762)
+      }
+      f.Vc[n * g.ncell + cd] = y;
+    }
+  } else {
+    double* vs = f.Vs + (long long)comp * g.nface;
+    const double x = vs[fidx(g, src[2], src[1], src[0])];
+    vs[fidx(g, dst[2], dst[1], dst[0])] = (type == 1) ? -x : x;
+  }
+}
+
+template <int D>
+__global__ void k_bc_slab(Geo g, Fields f, const Ctl* ctl, int dir) {
+  d_bc_slab<D>(g, f, ctl, dir, blockIdx);
+}
+
+// One thread per line along dir (all locations of the two other directions);
+// the recurrence runs outwards from the boundary face, each step reading the
+// face it wrote before.  Face areas are uniform on a Cartesian grid.
+template <int D>
+__device__ __forceinline__ void d_normal_field(const Geo& g, const Fields& f, const Ctl* ctl, int dir, dim3 bid) {
+  if (ctl->done) return;
+  const int a = (dir == 0) ? 1 : 0, b = (dir == 2) ? 1 : 2;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
+  if (tid >= (long long)g.nt[a] * g.nt[b]) return;
+  const int ia = (int)(tid % g.nt[a]), ib = (int)(tid / g.nt[a]);
+  const bool left = g.bc[dir][0] != 0, right = g.bc[dir][1] != 0;
+  double* V1 = f.Vs;
+  double* V2 = f.Vs + g.nface;
+  double* V3 = f.Vs + 2 * g.nface;  // read only when D == 3
+  const double A1 = g.A[0], A2 = g.A[1], A3 = g.A[2];
+  const long long s0 = g.fs[0], s1 = g.fs[1], s2 = g.fs[2];
+  const int nb = g.beg[dir] - 1, ne = g.end[dir], nt = g.nt[dir];
+  if (dir == 0) {
+    const int j = ia, k = ib;
+    if (left)
+      for (int i = nb; i >= 0; i--) {
+        const long long q = fidx(g, k, j, i);
+        double t = 0.0 + A2 * V2[q + s1] - A2 * V2[q];
+        if constexpr (D == 3) t = t + A3 * V3[q + s2] - A3 * V3[q];
+        V1[q] = 1.0 / A1 * (A1 * V1[q + s0] + (t));
+      }
+    if (right)
+      for (int i = ne; i < nt; i++) {
+        const long long q = fidx(g, k, j, i);
+        double t = 0.0 + A2 * V2[q + s1] - A2 * V2[q];
+        if constexpr (D == 3) t = t + A3 * V3[q + s2] - A3 * V3[q];
+        V1[q + s0] = 1.0 / A1 * (A1 * V1[q] - (t));
+      }
+  } else if (dir == 1) {
+    const int i = ia, k = ib;
+    if (left)
+      for (int j = nb; j >= 0; j--) {
+        const long long q = fidx(g, k, j, i);
+        double t = A1 * V1[q + s0] - A1 * V1[q];
+        if constexpr (D == 3) t = t + 1 * (A3 * V3[q + s2] - A3 * V3[q]);
+        V2[q] = 1.0 / A2 * (A2 * V2[q + s1] + (t));
+      }
+    if (right)
+      for (int j = ne; j < nt; j++) {
+        const long long q = fidx(g, k, j, i);
+        double t = A1 * V1[q + s0] - A1 * V1[q];
+        if constexpr (D == 3) t = t + 1 * (A3 * V3[q + s2] - A3 * V3[q]);
+        V2[q + s1] = 1.0 / A2 * (A2 * V2[q] - (t));
+      }
+  } else if constexpr (D == 3) {
+    const int i = ia, j = ib;
+    if (left)
+      for (int k = nb; k >= 0; k--) {
+        const long long q = fidx(g, k, j, i);
+        V3[q] = 1.0 / A3 * (A3 * V3[q + s2] + (A1 * V1[q + s0] - A1 * V1[q] + A2 * V2[q + s1] - A2 * V2[q]));
+      }
+    if (right)
+      for (int k = ne; k < nt; k++) {
+        const long long q = fidx(g, k, j, i);
+        V3[q + s2] = 1.0 / A3 * (A3 * V3[q] - (A1 * V1[q + s0] - A1 * V1[q] + A2 * V2[q + s1] - A2 * V2[q]));
+      }
+  }
+}
+
+template <int D>
+__global__ void k_normal_field(Geo g, Fields f, const Ctl* ctl, int dir) {
+  d_normal_field<D>(g, f, ctl, dir, blockIdx);
 }
 
 // ---------------------------------------------------------------------------

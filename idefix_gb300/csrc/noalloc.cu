@@ -103,6 +103,8 @@ int na_geometry(const idfx_gpu_config* cfg, Geo& g) {
   if (cfg->dims != 2 && cfg->dims != 3) return IDFX_ERR_CONFIG;
   if (cfg->order < 1 || cfg->order > 4 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
   if (cfg->shock_flattening) return IDFX_ERR_CONFIG;  // not supported by this entry point
+  for (int d = 0; d < 3; d++)  // periodic blocks only
+    if (cfg->lbound[d] || cfg->rbound[d]) return IDFX_ERR_CONFIG;
   if (cfg->emf < 0 || cfg->emf > 4 || cfg->precision != IDFX_FP64) return IDFX_ERR_CONFIG;
   if (cfg->emf == IDFX_EMF_UCT_HLLD && (cfg->solver == IDFX_HLL || cfg->solver == IDFX_TVDLF))
     return IDFX_ERR_CONFIG;
@@ -146,6 +148,8 @@ int na_geometry(const idfx_gpu_config* cfg, Geo& g) {
   g.gm1 = cfg->gamma - 1.0;
   g.ext = 1;
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
+  for (int d = 0; d < 3; d++) g.bc[d][0] = g.bc[d][1] = 0;
+  g.nonper = 0;
   return IDFX_OK;
 }
 

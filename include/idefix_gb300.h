@@ -77,7 +77,16 @@ typedef struct {
   int precision;            /* IDFX_FP64 or IDFX_MIXED                            */
   int shock_flattening;     /* [Hydro] shockFlattening present (0 = off)          */
   double shock_smoothing;   /* its value (shockFlattening.hpp:164)                */
+  int lbound[3], rbound[3]; /* [Boundary] X?-beg / X?-end: IDFX_BC_* per direction
+                               (DataBlock::lbound/rbound, boundary.hpp:287-386);
+                               periodic on both sides or on neither               */
 } idfx_gpu_config;
+
+/* boundary types (BoundaryType, idefix.hpp:220), ghosts filled as
+ * Boundary::EnforcePeriodic / EnforceReflective / EnforceOutflow
+ * (boundary.hpp:575-809) with the normal field rebuilt from div B = 0
+ * (ReconstructNormalField, boundary.hpp:408-532) */
+enum { IDFX_BC_PERIODIC = 0, IDFX_BC_REFLECTIVE = 1, IDFX_BC_OUTFLOW = 2 };
 
 typedef struct idfx_gpu idfx_gpu;
 
