@@ -4,7 +4,10 @@ hot-path code (the harness oracle/_ref/libofx_ref_*.so, built by
 
 Each fixture holds the active-region input state, the scheme, and the
 active-region state after a fixed number of TimeIntegrator cycles, plus
-t, dt and the cycle count.  Run from the repository root:
+t, dt and the cycle count.  Optional scheme keys: "bc" ([Boundary] types per
+direction) and "shock" ([Hydro] shockFlattening smoothing).  Fixtures that
+exist already are kept (--force rewrites them).  Run from the repository
+root:
 
     python tests/golden/make_golden.py
 """
@@ -38,6 +41,21 @@ CASES = [
     ("turb3d_hlld_plm_ucthlld", 3, (12, 12, 12), "plm", "hlld", "uct_hlld", 2, 0.6, 6),
 ]
 
+O, R, PER = ("outflow", "outflow"), ("reflective", "reflective"), ("periodic", "periodic")
+# name, dims, n, order, solver, emf, nstages, cfl, cycles, extra scheme keys
+EXTRA_CASES = [
+    ("ot2d_hlld_plm_contact_walls", 2, (32, 32), "plm", "hlld", "uct_contact", 2, 0.6, 20,
+     dict(bc=(R, O))),
+    ("ot2d_roe_ppm_ucthlld_mixedbc", 2, (32, 32), "ppm", "roe", "uct_hlld", 2, 0.6, 20,
+     dict(bc=(("reflective", "outflow"), PER))),
+    ("turb3d_hlld_plm_contact_bc", 3, (12, 12, 12), "plm", "hlld", "uct_contact", 2, 0.6, 6,
+     dict(bc=(O, R, PER))),
+    ("ot2d_hlld_limo3_contact_shock", 2, (32, 32), "limo3", "hlld", "uct_contact", 2, 0.6, 20,
+     dict(shock=0.5)),
+    ("turb3d_hlld_plm_contact_shock", 3, (12, 12, 12), "plm", "hlld", "uct_contact", 2, 0.6, 6,
+     dict(shock=0.0)),
+]
+
 
 def initial(dims, n):
     if dims == 2:
@@ -47,12 +65,15 @@ def initial(dims, n):
     return extract(dims, n, 2, Vc, Vs)
 
 
-def main():
-    for name, dims, n, order, solver, emf, nstages, cfl, cycles in CASES:
+def main(force=False):
+    for case in [c + (dict(),) for c in CASES] + EXTRA_CASES:
+        name, dims, n, order, solver, emf, nstages, cfl, cycles, extra = case
+        if os.path.exists(os.path.join(OUT, name + ".npz")) and not force:
+            continue
         vc0, vs0 = initial(dims, n)
         P.LIB_REF = os.path.join(ROOT, "oracle", "_ref", f"libofx_ref_d{dims}_o{P.ORDER[order]}.so")
         o = P.Oracle(dims, n, order=order, solver=solver, emf=emf, nstages=nstages, cfl=cfl,
-                     kind="ref")
+                     kind="ref", bc=extra.get("bc"), shock_flattening=extra.get("shock"))
         Vc, Vs = embed(dims, n, o.ng, vc0, vs0)
         o.set_prim(Vc, Vs)
         st = o.run(max_cycles=cycles)
@@ -64,10 +85,10 @@ def main():
             arrays[f"vs0_{c}"] = vs0[c]
             arrays[f"vs1_{c}"] = vs1[c]
         meta = dict(dims=dims, n=list(n), order=order, solver=solver, emf=emf, nstages=nstages,
-                    cfl=cfl, cycles=cycles, gamma=5.0 / 3.0, first_dt=1e-4)
+                    cfl=cfl, cycles=cycles, gamma=5.0 / 3.0, first_dt=1e-4, **extra)
         np.savez_compressed(os.path.join(OUT, name + ".npz"), meta=np.array(repr(meta)), **arrays)
         print(name, t, dt, nc)
 
 
 if __name__ == "__main__":
-    main()
+    main(force="--force" in sys.argv)

@@ -67,7 +67,8 @@ def test_gpu_matches_reference_golden_fixture(path):
     dims, n = meta["dims"], tuple(meta["n"])
     state = (z["vc0"], [z[f"vs0_{c}"] for c in range(dims)])
     out, tm = _gpu(dims, n, state, cycles=meta["cycles"], order=meta["order"], solver=meta["solver"],
-                   emf=meta["emf"], nstages=meta["nstages"], cfl=meta["cfl"], first_dt=meta["first_dt"])
+                   emf=meta["emf"], nstages=meta["nstages"], cfl=meta["cfl"], first_dt=meta["first_dt"],
+                   bc=meta.get("bc"), shock_flattening=meta.get("shock"))
     assert tm == (float(z["t"]), float(z["dt"]), int(z["ncycles"]))
     _assert_same(out, (z["vc1"], [z[f"vs1_{c}"] for c in range(dims)]))
 

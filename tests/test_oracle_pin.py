@@ -104,7 +104,7 @@ def test_oracle_matches_golden_fixture(oracle_lib, path):
     state = (z["vc0"], [z[f"vs0_{c}"] for c in range(dims)])
     st, out, tm = _run("port", dims, n, state, meta["cycles"], order=meta["order"],
                        solver=meta["solver"], emf=meta["emf"], nstages=meta["nstages"],
-                       cfl=meta["cfl"])
+                       cfl=meta["cfl"], bc=meta.get("bc"), shock_flattening=meta.get("shock"))
     assert st == 0
     assert tm == (float(z["t"]), float(z["dt"]), int(z["ncycles"]))
     assert np.array_equal(out[0], z["vc1"])
@@ -113,7 +113,7 @@ def test_oracle_matches_golden_fixture(oracle_lib, path):
 
 
 def test_golden_fixtures_present():
-    assert len(_golden_cases()) >= 10
+    assert len(_golden_cases()) >= 16
 
 
 def test_oracle_linear_fast_wave_known_answer(oracle_lib):
