@@ -65,6 +65,69 @@ def orszag_tang_2d(n=256, nghost=2, gamma=5.0 / 3.0):
     return Vc, Vs
 
 
+def rotor_2d(n=512, nghost=2):
+    """MHD rotor on [-0.5,0.5]^2 (test/MHD/RotorCartesian/setup.cpp:17-60,
+    idefix.ini: Roe, CFL 0.2, t_stop 0.15, outflow on all four sides): a
+    dense disc (rho = 10, r < 0.1) spinning at omega = 20 with a linear taper
+    to r = 0.115, in a uniform field B0 = 5 / sqrt(4 pi) along x, p = 1.
+
+    Every cell and face index takes its cell-centre coordinates, as the
+    reference set-up does; the extra face beyond np_tot stays zero (a ghost
+    face, rebuilt by the boundary pass)."""
+    dims = 2
+    nvar, nt, ntv = grid_shapes(dims, (n, n), nghost)
+    xc, _ = _coords(dims, (n, n, 1), nghost, (-0.5, -0.5, 0.0), (0.5, 0.5, 1.0))
+    r0, r1, omega = 0.1, 0.115, 20.0
+    B0 = 5.0 / math.sqrt(4.0 * math.pi)
+    x = np.broadcast_to(xc[0][None, :], (nt[1], nt[0]))
+    y = np.broadcast_to(xc[1][:, None], (nt[1], nt[0]))
+    r = np.power(x * x + y * y, 0.5)
+    f = (r1 - r) / (r1 - r0)
+    inner, taper = r < r0, (r >= r0) & (r <= r1)
+    rho = np.where(inner, 10.0, np.where(taper, 1.0 + 9.0 * f, 1.0))
+    vphi = np.where(inner, omega * r, np.where(taper, f * omega * r0, 0.0))
+    Vc = np.zeros((nvar, nt[2], nt[1], nt[0]))
+    Vs = np.zeros((dims, ntv[2], ntv[1], ntv[0]))
+    Vc[0, 0] = rho
+    Vc[1, 0] = -y / r * vphi
+    Vc[2, 0] = x / r * vphi
+    Vc[3, 0] = 1.0
+    Vs[0, :, : nt[1], : nt[0]] = B0
+    return Vc, Vs
+
+
+def shock_tube_2d(nx=800, ny=4, nghost=2):
+    """MHD shock tube of test/MHD/sod (setup.cpp:30-55, idefix.ini: x in
+    [0,100], Roe, gamma 1.66666666666667, CFL 0.8, t_stop 10, outflow in x):
+    rho, p = 1, 1 for x < 50 and 0.125, 0.1 beyond, v = 0, Bx = 0.75,
+    By = +1 / -1.  The reference runs it in 1-D with two components; here
+    it is a 2-D block uniform in y (periodic, ny cells of the same width),
+    so the y-derivatives vanish and By is a face field evolved by CT."""
+    dims = 2
+    dx = 100.0 / nx
+    nvar, nt, ntv = grid_shapes(dims, (nx, ny), nghost)
+    xc, xl = _coords(dims, (nx, ny, 1), nghost, (0.0, 0.0, 0.0), (100.0, ny * dx, 1.0))
+    left = np.broadcast_to((xc[0] < 50.0)[None, :], (nt[1], nt[0]))
+    Vc = np.zeros((nvar, nt[2], nt[1], nt[0]))
+    Vs = np.zeros((dims, ntv[2], ntv[1], ntv[0]))
+    Vc[0, 0] = np.where(left, 1.0, 0.125)
+    Vc[3, 0] = np.where(left, 1.0, 0.1)
+    Vs[0, :, : nt[1], : nt[0]] = 0.75
+    Vs[1, :, : nt[1], : nt[0]] = np.where(left, 1.0, -1.0)
+    return Vc, Vs
+
+
+SHOCK_TUBE_GAMMA = 1.66666666666667  # test/MHD/sod/idefix.ini
+
+
+def shock_tube_domain(nx=800, ny=4):
+    """(xbeg, xend) of shock_tube_2d: [0,100] x [0, ny dx], square cells"""
+    return (0.0, 0.0, 0.0), (100.0, ny * (100.0 / nx), 1.0)
+
+
+ROTOR_DOMAIN = ((-0.5, -0.5, 0.0), (0.5, 0.5, 1.0))  # (xbeg, xend) of rotor_2d
+
+
 def orszag_tang_like_2d(n, mach=1.0, beta=10.0 / 3.0, nghost=2, gamma=5.0 / 3.0):
     """Orszag-Tang vortex with a chosen sonic Mach number and plasma beta.
 

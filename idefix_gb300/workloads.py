@@ -131,6 +131,48 @@ def run_lowbeta(n=384, cycles=200, seed=0, cfl=0.6, log=sys.stderr):
     return res
 
 
+def run_rotor(n=512, tstop=0.15, repeats=2, log=sys.stderr):
+    """MHD rotor of test/MHD/RotorCartesian at its ini settings (n^2 cells
+    on [-0.5,0.5]^2, Roe, PLM, uct_contact, RK2, CFL 0.2, outflow on all
+    sides) to t_stop, FP64 and mixed precision; the last of `repeats` runs is
+    timed (the first warms the GPU up).  Throughput in zone-cycles/s."""
+    import torch
+
+    Vc, Vs = ic.rotor_2d(n)
+    bc = (("outflow", "outflow"), ("outflow", "outflow"))
+    res = {"n": n, "tstop": tstop, "scheme": "Roe + PLM + uct_contact, RK2, CFL 0.2, outflow"}
+    out = {}
+    g = 2
+    a = slice(g, g + n)
+    for prec in ("fp64", "mixed"):
+        for _ in range(repeats):
+            blk = ig.GpuBlock(2, (n, n), solver="roe", cfl=0.2, first_dt=1e-4, precision=prec, bc=bc,
+                              xbeg=ic.ROTOR_DOMAIN[0], xend=ic.ROTOR_DOMAIN[1])
+            blk.upload(Vc, Vs)
+            dt_s = _timed_run(blk, tstop)
+            t, dt, nc = blk.get_time()
+            vc, vs = blk.download()
+            if prec == "fp64" and "fp64" in out:  # run-to-run determinism
+                res["fp64_deterministic"] = bool(np.array_equal(vc, out["fp64"][0]))
+            out[prec] = (vc, vs)
+            res[prec + "_divb"] = blk.check_divb()
+            blk.close()
+        res[prec + "_s"] = dt_s
+        res[prec + "_cycles"] = nc
+        res[prec + "_zone_cycles_per_s"] = n * n * nc / dt_s
+        res[prec + "_t"] = t
+        if log:
+            print(f"{prec}: {dt_s:.3f} s, {nc} cycles, t = {t}", file=log, flush=True)
+    err = {}
+    for v, name in enumerate(("RHO", "VX1", "VX2", "PRS", "BX1", "BX2")):
+        x, y = out["mixed"][0][v, 0, a, a], out["fp64"][0][v, 0, a, a]
+        d = np.abs(x - y)
+        err[name] = {"l1": float(d.sum() / max(np.abs(y).sum(), 1e-300)),
+                     "linf": float(d.max() / max(np.abs(y).max(), 1e-300))}
+    res["errors_mixed_vs_fp64"] = err
+    return res
+
+
 OW3 = 216 * 128 + 128 + 128 * 128 + 128  # offset of W3 (then b3) in the packed parameters
 
 
@@ -303,7 +345,7 @@ if __name__ == "__main__":
     import argparse
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["ensemble", "learned", "lowbeta"], default="ensemble")
+    ap.add_argument("--workload", choices=["ensemble", "learned", "lowbeta", "rotor"], default="ensemble")
     ap.add_argument("--n", type=int, default=384)
     ap.add_argument("--nbox", type=int, default=512)
     ap.add_argument("--n-fine", type=int, default=128)
@@ -323,6 +365,8 @@ if __name__ == "__main__":
         r = run_ensemble(a.nbox, a.seed, a.cycles or 500, check=not a.no_check, graph=not a.no_graph)
     elif a.workload == "lowbeta":
         r = run_lowbeta(a.n, a.cycles or 200, a.seed)
+    elif a.workload == "rotor":
+        r = run_rotor(a.n if a.n != 384 else 512)
     else:
         pre = None
         if a.load:

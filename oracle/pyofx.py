@@ -88,6 +88,8 @@ class Oracle:
                  check_nan_period=0, maxdivb=1e-6, shock_flattening=None, bc=None):
         self.lib = load(kind)
         n = list(n) + [1] * (3 - len(n))
+        xbeg = tuple(xbeg) + (0.0, 0.0, 0.0)[len(xbeg):]
+        xend = tuple(xend) + (1.0, 1.0, 1.0)[len(xend):]
         self.dims, self.n = dims, n
         h = self.lib.ofx_create(dims, n[0], n[1], n[2], xbeg[0], xend[0], xbeg[1], xend[1],
                                 xbeg[2], xend[2], ORDER[order], SOLVER[solver], EMF[emf],

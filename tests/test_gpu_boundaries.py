@@ -174,3 +174,57 @@ def test_boundary_configs_refused():
         ig.GpuBlock(2, (2, 16), order="ppm", bc=(R, PER))
     with pytest.raises(ig.IdefixError):  # the ensemble's boxes are periodic
         ig.Ensemble([dict(dims=2, n=(16, 16), bc=(O, O))])
+
+
+def _oracle_and_gpu(dims, n, state, tstop, **kw):
+    from oracle.pyofx import Oracle
+
+    o = Oracle(dims, n, threads=os.cpu_count() or 1, **kw)
+    o.set_prim(*embed(dims, n, o.ng, *state))
+    assert o.run(tstop=tstop) == 0
+    ref = extract(dims, n, o.ng, *o.get_prim())
+    blk = ig.GpuBlock(dims, n, **kw)
+    blk.upload(*embed(dims, n, blk.ng, *state))
+    blk.run(tstop=tstop)
+    out = extract(dims, n, blk.ng, *blk.download())
+    return o, ref, blk, out
+
+
+@pytest.mark.gpu
+def test_gpu_rotor_256_to_t015_bit_identical():
+    """test/MHD/RotorCartesian (Roe, CFL 0.2, outflow on all sides) at 256^2
+    to its t_stop = 0.15: bit-identical to the oracle"""
+    n = (256, 256)
+    state = extract(2, n, 2, *ic.rotor_2d(256))
+    xb, xe = ic.ROTOR_DOMAIN
+    o, ref, blk, out = _oracle_and_gpu(2, n, state, 0.15, solver="roe", cfl=0.2, first_dt=1e-4, bc=(O, O),
+                                       xbeg=xb, xend=xe)
+    assert np.array_equal(out[0], ref[0])
+    for c in range(2):
+        assert np.array_equal(out[1][c], ref[1][c])
+    assert blk.get_time() == o.get_time()
+    assert blk.check_divb() < 1e-10
+    blk.close()
+
+
+@pytest.mark.gpu
+def test_gpu_shock_tube_to_t10_bit_identical_and_uniform():
+    """test/MHD/sod (Roe, CFL 0.8, gamma 1.66666666666667, outflow) as a
+    y-uniform 800 x 4 block to its t_stop = 10: bit-identical to the oracle,
+    every row identical, the compound-wave structure inside the tube"""
+    n = (800, 4)
+    state = extract(2, n, 2, *ic.shock_tube_2d(800, 4))
+    xb, xe = ic.shock_tube_domain(800, 4)
+    o, ref, blk, out = _oracle_and_gpu(2, n, state, 10.0, solver="roe", cfl=0.8, first_dt=1e-4,
+                                       gamma=ic.SHOCK_TUBE_GAMMA, bc=(O, PER), xbeg=xb, xend=xe)
+    assert np.array_equal(out[0], ref[0])
+    for c in range(2):
+        assert np.array_equal(out[1][c], ref[1][c])
+    assert blk.get_time() == o.get_time()
+    vc = out[0][:, 0]
+    assert all(np.array_equal(vc[:, j], vc[:, 0]) for j in range(1, 4))
+    rho = vc[0, 0]
+    # the waves have not reached the ends by t = 10: the end states are intact
+    assert rho[0] == 1.0 and rho[-1] == 0.125
+    assert 0.1 < rho.min() and rho.max() < 1.1
+    blk.close()

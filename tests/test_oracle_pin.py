@@ -232,3 +232,24 @@ def test_oracle_matches_reference_with_boundaries(oracle_lib, reference_libs, di
 def test_oracle_refuses_half_periodic_boundaries(oracle_lib):
     with pytest.raises(ValueError):
         P.Oracle(2, (8, 8), bc=(("periodic", "outflow"), PER))
+
+
+@pytest.mark.parametrize("problem", ["rotor", "shock_tube"])
+def test_oracle_matches_reference_on_boundary_problems(oracle_lib, reference_libs, problem):
+    # the reference's own outflow test problems (test/MHD/RotorCartesian,
+    # test/MHD/sod run as a y-uniform 2-D block), Roe, their ini settings
+    if problem == "rotor":
+        n = (48, 48)
+        state = extract(2, n, 2, *ic.rotor_2d(48))
+        scheme = dict(solver="roe", cfl=0.2, bc=(O, O), xbeg=ic.ROTOR_DOMAIN[0], xend=ic.ROTOR_DOMAIN[1])
+    else:
+        n = (200, 2)
+        state = extract(2, n, 2, *ic.shock_tube_2d(200, 2))
+        xb, xe = ic.shock_tube_domain(200, 2)
+        scheme = dict(solver="roe", cfl=0.8, gamma=ic.SHOCK_TUBE_GAMMA, bc=(O, PER), xbeg=xb, xend=xe)
+    P.LIB_REF = os.path.join(reference_libs, "libofx_ref_d2_o2.so")
+    port = _run("port", 2, n, state, 30, **scheme)
+    ref = _run("ref", 2, n, state, 30, **scheme)
+    assert port[0] == ref[0] == 0
+    assert _same(port[1], ref[1])
+    assert port[2] == ref[2]
