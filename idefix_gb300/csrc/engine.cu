@@ -107,19 +107,21 @@ __global__ void k_uc_field_all(Geo g, Fields f, int to_prim) {
   for (int n = 0; n < v::NV; n++) f.Vc[n * g.ncell + c] = V[n];
 }
 
-template <int D>
+// E: type of the EMF buffers (FP32 on the mixed path)
+template <int D, typename E>
 __global__ void k_cell_emf_all(Geo g, Fields f) {
   using v = Var<D>;
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.ncell) return;
-  const double vx1 = f.Vc[v::MX1 * g.ncell + c], vx2 = f.Vc[v::MX2 * g.ncell + c];
-  const double Bx1 = f.Vc[v::BX1 * g.ncell + c], Bx2 = f.Vc[v::BX2 * g.ncell + c];
+  auto V = [&](int n) { return from_f64<E>(f.Vc[n * g.ncell + c]); };
+  const E vx1 = V(v::MX1), vx2 = V(v::MX2);
+  const E Bx1 = V(v::BX1), Bx2 = V(v::BX2);
   if constexpr (D == 3) {
-    const double vx3 = f.Vc[v::MX3 * g.ncell + c], Bx3 = f.Vc[v::BX3 * g.ncell + c];
-    f.Ex1[c] = (vx3 * Bx2 - vx2 * Bx3);
-    f.Ex2[c] = (vx1 * Bx3 - vx3 * Bx1);
+    const E vx3 = V(v::MX3), Bx3 = V(v::BX3);
+    emf<E>(f.Ex1)[c] = (vx3 * Bx2 - vx2 * Bx3);
+    emf<E>(f.Ex2)[c] = (vx1 * Bx3 - vx3 * Bx1);
   }
-  f.Ex3[c] = (vx2 * Bx1 - vx1 * Bx2);
+  emf<E>(f.Ex3)[c] = (vx2 * Bx1 - vx1 * Bx2);
 }
 
 // FP32 copy of the primitives for the mixed-precision sweeps (the building
@@ -127,7 +129,7 @@ __global__ void k_cell_emf_all(Geo g, Fields f) {
 __global__ void k_vc32(Geo g, Fields f, int nv) {
   const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.ncell) return;
-  for (int n = 0; n < nv; n++) f.Vc32[n * g.ncell + c] = (float)f.Vc[n * g.ncell + c];
+  for (int n = 0; n < nv; n++) f.Vc32[n * g.ncell + c] = d2f_rn(f.Vc[n * g.ncell + c]);
 }
 
 template <int D>
@@ -180,6 +182,19 @@ long long n_edges(const Geo& g) {
     else K<3><<<GRID, BLOCK, 0, e.stream>>>(__VA_ARGS__);                   \
   } while (0)
 
+// dimension and EMF type (FP32 EMF buffers on the mixed path)
+#define IDFX_DISPATCH_DE(K, GRID, BLOCK, ...)                                              \
+  do {                                                                                     \
+    const bool f32 = (e.precision == IDFX_MIXED);                                          \
+    if (e.g.D == 2) {                                                                      \
+      if (f32) K<2, float><<<GRID, BLOCK, 0, e.stream>>>(__VA_ARGS__);                     \
+      else K<2, double><<<GRID, BLOCK, 0, e.stream>>>(__VA_ARGS__);                        \
+    } else {                                                                               \
+      if (f32) K<3, float><<<GRID, BLOCK, 0, e.stream>>>(__VA_ARGS__);                     \
+      else K<3, double><<<GRID, BLOCK, 0, e.stream>>>(__VA_ARGS__);                        \
+    }                                                                                      \
+  } while (0)
+
 void launch_fill_faces(Engine& e, int save_begin) {
   dim3 grid(nblocks(e.g.nface), e.g.D);
   mark_begin(e, kKFillFaces);
@@ -204,15 +219,15 @@ void launch_boundaries(Engine& e) {
 }
 void launch_stage_begin(Engine& e, int flags) {
   mark_begin(e, kKStageBegin);
-  IDFX_DISPATCH_D(k_stage_begin, nblocks(e.g.ncell), kThreads, e.g, e.f, e.ctl, flags);
+  IDFX_DISPATCH_DE(k_stage_begin, nblocks(e.g.ncell), kThreads, e.g, e.f, e.ctl, flags);
   mark_end(e);
 }
 void launch_ct(Engine& e, int combine, double wc, double w0) {
   mark_begin(e, kKCtCorner);
-  IDFX_DISPATCH_D(k_ct_corner, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
+  IDFX_DISPATCH_DE(k_ct_corner, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
   mark_end(e);
   mark_begin(e, kKCtFaces);
-  IDFX_DISPATCH_D(k_ct_faces, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl, combine, wc, w0);
+  IDFX_DISPATCH_DE(k_ct_faces, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl, combine, wc, w0);
   mark_end(e);
 }
 void launch_find_shock(Engine& e) {
@@ -797,7 +812,7 @@ int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt) {
   if (e.f.shock) launch_find_shock(e);
   if (e.g.order == IDFX_LEARNED) launch_learned_recon(e);
   if (e.g.emf == kEmfContact || e.g.emf == kEmfUct0)
-    IDFX_DISPATCH_D(k_cell_emf_all, nblocks(e.g.ncell), kThreads, e.g, e.f);
+    IDFX_DISPATCH_DE(k_cell_emf_all, nblocks(e.g.ncell), kThreads, e.g, e.f);
   launch_sweeps(e, 2, 0);
   launch_ct(e, 0, 1.0, 0.0);
   IDFX_DISPATCH_D(k_uc_field_all, nblocks(e.g.ncell), kThreads, e.g, e.f, 0);

@@ -31,11 +31,12 @@ __global__ void ke_fill_faces(const EnsBox* boxes, const int4* items, int save) 
   const EnsBox& B = boxes[it.x];
   d_fill_faces<D>(B.g, B.f, B.ctl, save, dim3(it.y, it.z, it.w));
 }
-template <int D>
+// E: type of the EMF buffers (FP32 on the mixed path)
+template <int D, typename E>
 __global__ void ke_stage_begin(const EnsBox* boxes, const int4* items, int flags) {
   const int4 it = items[blockIdx.x];
   const EnsBox& B = boxes[it.x];
-  d_stage_begin<D>(B.g, B.f, B.ctl, flags, dim3(it.y, it.z, it.w));
+  d_stage_begin<D, E>(B.g, B.f, B.ctl, flags, dim3(it.y, it.z, it.w));
 }
 template <int D>
 __global__ void ke_find_shock(const EnsBox* boxes, const int4* items) {
@@ -43,24 +44,24 @@ __global__ void ke_find_shock(const EnsBox* boxes, const int4* items) {
   const EnsBox& B = boxes[it.x];
   d_find_shock<D>(B.g, B.f, B.ctl, dim3(it.y, it.z, it.w));
 }
-template <int D>
+template <int D, typename E>
 __global__ void ke_ct_corner(const EnsBox* boxes, const int4* items) {
   const int4 it = items[blockIdx.x];
   const EnsBox& B = boxes[it.x];
-  d_ct_corner<D>(B.g, B.f, B.ctl, dim3(it.y, it.z, it.w));
+  d_ct_corner<D, E>(B.g, B.f, B.ctl, dim3(it.y, it.z, it.w));
 }
 // diagnostics are due for a box when its own cycle count is a multiple of
 // the period (timeIntegrator.cpp:268-279 and 393-399 on the host mirror)
 __device__ __forceinline__ bool due(const Ctl* c, int period) { return period > 0 && c->ncycles % period == 0; }
 
-template <int D>
+template <int D, typename E>
 __global__ void ke_ct_faces(const EnsBox* boxes, const int4* items, int combine, double wc, double w0,
                             int nan_period) {
   const int4 it = items[blockIdx.x];
   const EnsBox& B = boxes[it.x];
   // a box with a NaN check this cycle combines its faces after the count
   const int cmb = combine && !due(B.ctl, nan_period);
-  d_ct_faces<D>(B.g, B.f, B.ctl, cmb, cmb ? wc : 1.0, cmb ? w0 : 0.0, dim3(it.y, it.z, it.w));
+  d_ct_faces<D, E>(B.g, B.f, B.ctl, cmb, cmb ? wc : 1.0, cmb ? w0 : 0.0, dim3(it.y, it.z, it.w));
 }
 template <int D>
 __global__ void ke_stage_end(const EnsBox* boxes, const int4* items, int combine, double wc, double w0) {
@@ -124,6 +125,21 @@ __global__ void ke_check_nan(const EnsBox* boxes, int nbox, int period) {
       if (e.D == 2) K<2><<<(N), kT, 0, e.stream>>>(__VA_ARGS__);                \
       else K<3><<<(N), kT, 0, e.stream>>>(__VA_ARGS__);                         \
     }                                                                           \
+  } while (0)
+
+// dimension and EMF type (FP32 EMF buffers on the mixed path)
+#define IDFX_ENS_DE(K, N, ...)                                                       \
+  do {                                                                               \
+    if ((N) > 0) {                                                                   \
+      const bool f32 = (e.precision == IDFX_MIXED);                                  \
+      if (e.D == 2) {                                                                \
+        if (f32) K<2, float><<<(N), kT, 0, e.stream>>>(__VA_ARGS__);                 \
+        else K<2, double><<<(N), kT, 0, e.stream>>>(__VA_ARGS__);                    \
+      } else {                                                                       \
+        if (f32) K<3, float><<<(N), kT, 0, e.stream>>>(__VA_ARGS__);                 \
+        else K<3, double><<<(N), kT, 0, e.stream>>>(__VA_ARGS__);                    \
+      }                                                                              \
+    }                                                                                \
   } while (0)
 
 inline unsigned per_box_blocks(const EnsEngine& e) { return (unsigned)((e.nbox + kT - 1) / kT); }
@@ -214,7 +230,7 @@ void queue_cycle(EnsEngine& e, bool checks) {
   for (int stage = 0; stage < e.nstages; stage++) {
     const int save = (e.nstages > 1 && stage == 0);
     IDFX_ENS_D(ke_fill_faces, e.fill.n, e.d_boxes, e.fill.items, save);
-    IDFX_ENS_D(ke_stage_begin, e.begin.n, e.d_boxes, e.begin.items,
+    IDFX_ENS_DE(ke_stage_begin, e.begin.n, e.d_boxes, e.begin.items,
                kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
     // shock flags: the stage-begin table covers (n + 2)^D cells of every box
     if (e.shock) IDFX_ENS_D(ke_find_shock, e.begin.n, e.d_boxes, e.begin.items);
@@ -222,8 +238,8 @@ void queue_cycle(EnsEngine& e, bool checks) {
       launch_sweep(e, d, e.sweep[d], stage == 0 ? (d == 0 ? 1 : 2) : 0, stage == 0 && d == e.D - 1);
     const int combine = stage > 0;
     const double wc = combine ? e.wc[stage - 1] : 1.0, w0 = combine ? e.w0[stage - 1] : 0.0;
-    IDFX_ENS_D(ke_ct_corner, e.edges.n, e.d_boxes, e.edges.items);
-    IDFX_ENS_D(ke_ct_faces, e.edges.n, e.d_boxes, e.edges.items, combine, wc, w0, np);
+    IDFX_ENS_DE(ke_ct_corner, e.edges.n, e.d_boxes, e.edges.items);
+    IDFX_ENS_DE(ke_ct_faces, e.edges.n, e.d_boxes, e.edges.items, combine, wc, w0, np);
     if (np > 0) {
       ke_reset_nan<<<per_box_blocks(e), kT, 0, e.stream>>>(e.d_boxes, e.nbox, np);
       IDFX_ENS_D(ke_nan_count, e.edges.n, e.d_boxes, e.edges.items, np);

@@ -13,6 +13,7 @@
 #pragma once
 #include <cstdint>
 
+#include "fpconv.cuh"
 #include "mhd_math.cuh"
 
 namespace idfx {
@@ -59,6 +60,9 @@ struct Ctl {
   int status;  // Status
 };
 
+// The EMF buffers (face EMFs ezi..eyk, upwind weights sv*, cell EMFs Ex*,
+// corner EMFs ex/ey/ez, uct_hll(d) weights aL..dR) hold FP64 values on the
+// FP64 path and FP32 values on the mixed path, in the same storage (emf<E>).
 struct Fields {
   double *Vc, *Uc, *Uc0, *Vs, *Vs0, *InvDt;
   double *ezi, *ezj, *exj, *exk, *eyi, *eyk;
@@ -70,6 +74,33 @@ struct Fields {
   float* Vc32;  // FP32 copy of Vc read by the mixed-precision sweeps (else null)
   unsigned char* shock;  // FlagShock per cell when shock flattening is on (else null)
 };
+
+// an EMF buffer in the arithmetic type of its producer
+template <typename E>
+__device__ __forceinline__ E* emf(double* p) {
+  return reinterpret_cast<E*>(p);
+}
+template <typename E>
+__device__ __forceinline__ const E* emf(const double* p) {
+  return reinterpret_cast<const E*>(p);
+}
+// FP32 <-> FP64 on the integer pipe (fpconv.cuh); identity for doubles
+template <typename T>
+__device__ __forceinline__ double to_f64(T x) {
+  if constexpr (sizeof(T) == 4) {
+    return f2d_exact(x);
+  } else {
+    return x;
+  }
+}
+template <typename T>
+__device__ __forceinline__ T from_f64(double x) {
+  if constexpr (sizeof(T) == 4) {
+    return d2f_rn(x);
+  } else {
+    return x;
+  }
+}
 
 __device__ __forceinline__ long long cidx(const Geo& g, int k, int j, int i) {
   return ((long long)k * g.nt[1] + j) * g.nt[0] + i;
@@ -141,7 +172,9 @@ __global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
 // ---------------------------------------------------------------------------
 enum { kSbCons = 1, kSbSaveBegin = 2, kSbCellEmf = 4 };
 
-template <int D>
+// E: type of the EMF buffers (float on the mixed path: the cell EMF is then
+// computed in FP32 from the FP32 primitives that the sweeps read)
+template <int D, typename E = double>
 __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, const Ctl* ctl, int flags, dim3 bid) {
   if (ctl->done) return;
   using v = Var<D>;
@@ -188,25 +221,29 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
       for (int n = 0; n < NV; n++) f.Uc0[n * g.ncell + c] = U[n];
     }
   }
+  // the primitives in the EMF type (the FP32 copy on the mixed path)
+  E W[NV];
+#pragma unroll
+  for (int n = 0; n < NV; n++) W[n] = from_f64<E>(V[n]);
   if (flags & kSbCellEmf) {
-    const double vx1 = V[v::MX1], vx2 = V[v::MX2];
-    const double Bx1 = V[v::BX1], Bx2 = V[v::BX2];
+    const E vx1 = W[v::MX1], vx2 = W[v::MX2];
+    const E Bx1 = W[v::BX1], Bx2 = W[v::BX2];
     if constexpr (D == 3) {
-      const double vx3 = V[v::MX3], Bx3 = V[v::BX3];
-      f.Ex1[c] = (vx3 * Bx2 - vx2 * Bx3);
-      f.Ex2[c] = (vx1 * Bx3 - vx3 * Bx1);
+      const E vx3 = W[v::MX3], Bx3 = W[v::BX3];
+      emf<E>(f.Ex1)[c] = (vx3 * Bx2 - vx2 * Bx3);
+      emf<E>(f.Ex2)[c] = (vx1 * Bx3 - vx3 * Bx1);
     }
-    f.Ex3[c] = (vx2 * Bx1 - vx1 * Bx2);
+    emf<E>(f.Ex3)[c] = (vx2 * Bx1 - vx1 * Bx2);
   }
   if (f.Vc32) {  // mixed precision: the sweeps read the primitives in FP32
 #pragma unroll
-    for (int n = 0; n < NV; n++) f.Vc32[n * g.ncell + c] = (float)V[n];
+    for (int n = 0; n < NV; n++) f.Vc32[n * g.ncell + c] = (sizeof(E) == 4) ? (float)W[n] : d2f_rn(V[n]);
   }
 }
 
-template <int D>
+template <int D, typename E = double>
 __global__ void k_stage_begin(Geo g, Fields f, const Ctl* ctl, int flags) {
-  d_stage_begin<D>(g, f, ctl, flags, blockIdx);
+  d_stage_begin<D, E>(g, f, ctl, flags, blockIdx);
 }
 
 // ---------------------------------------------------------------------------
@@ -418,42 +455,43 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
                                           const RiemannOut<D, T>& r, const T* vL, const T* vR) {
   using d = Dir<D, DIR>;
   using vv = Var<D>;
+  // the EMF buffers take the arithmetic type T of the sweep
   T st, sb;
-  double *Et, *Eb, *SV;
+  T *Et, *Eb, *SV;
   if constexpr (DIR == 0) {
-    st = T(-1); sb = T(+1); Et = f.ezi; Eb = f.eyi; SV = f.svx;
+    st = T(-1); sb = T(+1); Et = emf<T>(f.ezi); Eb = emf<T>(f.eyi); SV = emf<T>(f.svx);
   } else if constexpr (DIR == 1) {
-    st = T(+1); sb = T(-1); Et = f.ezj; Eb = f.exj; SV = f.svy;
+    st = T(+1); sb = T(-1); Et = emf<T>(f.ezj); Eb = emf<T>(f.exj); SV = emf<T>(f.svy);
   } else {
-    st = T(-1); sb = T(+1); Et = f.eyk; Eb = f.exk; SV = f.svz;
+    st = T(-1); sb = T(+1); Et = emf<T>(f.eyk); Eb = emf<T>(f.exk); SV = emf<T>(f.svz);
   }
   if (g.emf == kEmfContact || g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
-    Et[c] = (double)(st * r.F[d::BXt]);
-    if constexpr (D == 3) Eb[c] = (double)(sb * r.F[d::BXb]);
+    Et[c] = st * r.F[d::BXt];
+    if constexpr (D == 3) Eb[c] = sb * r.F[d::BXb];
     if (g.emf == kEmfContact) {
-      double s = 0.5;
-      if (r.F[vv::RHO] > T(kEpsUctContact)) s = 1.0;
-      if (r.F[vv::RHO] < T(-kEpsUctContact)) s = 0.0;
+      T s = T(0.5);
+      if (r.F[vv::RHO] > T(kEpsUctContact)) s = T(1);
+      if (r.F[vv::RHO] < T(-kEpsUctContact)) s = T(0);
       SV[c] = s;
     }
     return;
   }
-  double* aL = f.aL[DIR];
-  double* aR = f.aR[DIR];
-  double* dL = f.dL[DIR];
-  double* dR = f.dR[DIR];
+  T* aL = emf<T>(f.aL[DIR]);
+  T* aR = emf<T>(f.aR[DIR]);
+  T* dL = emf<T>(f.dL[DIR]);
+  T* dR = emf<T>(f.dR[DIR]);
   const T sl = r.sl, sr = r.sr;
   if (g.emf == kEmfUctHll) {
     const T ar = fmax(T(0), sr);
     const T al = fmin(T(0), sl);
     const T scrh = dv(T(1), ar - al);
-    Et[c] = (double)(-st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh);
-    if constexpr (D == 3) Eb[c] = (double)(-sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh);
-    aL[c] = (double)(ar * scrh);
-    aR[c] = (double)(-al * scrh);
+    Et[c] = -st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh;
+    if constexpr (D == 3) Eb[c] = -sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh;
+    aL[c] = ar * scrh;
+    aR[c] = -al * scrh;
     const T dr = -al * ar * scrh;
-    dR[c] = (double)dr;
-    dL[c] = (double)dr;
+    dR[c] = dr;
+    dL[c] = dr;
     return;
   }
   // uct_hlld (K_StoreHLLD, energy branch)
@@ -501,12 +539,12 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
     d_r = -al * ar * scrh;
     d_l = d_r;
   }
-  aL[c] = (double)a_l;
-  aR[c] = (double)a_r;
-  dL[c] = (double)d_l;
-  dR[c] = (double)d_r;
-  Et[c] = (double)(-st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh);
-  if constexpr (D == 3) Eb[c] = (double)(-sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh);
+  aL[c] = a_l;
+  aR[c] = a_r;
+  dL[c] = d_l;
+  dR[c] = d_r;
+  Et[c] = -st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh;
+  if constexpr (D == 3) Eb[c] = -sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh;
 }
 
 // ---------------------------------------------------------------------------
@@ -655,10 +693,10 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
       }
       T bn;
       if constexpr (PF) {
-        bn = (T)nbn;
+        bn = from_f64<T>(nbn);
         if (more) nbn = vs[f0 + (long long)(c + 1 - m0) * fsd];
       } else {
-        bn = (T)vs[f0 + (long long)(c - m0) * fsd];
+        bn = from_f64<T>(vs[f0 + (long long)(c - m0) * fsd]);
       }
       vL[dd::BXn] = bn;
       vR[dd::BXn] = bn;
@@ -678,7 +716,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
           for (int n = 0; n < v::BX1; n++) {
             const T rhs = -dtdVT * (FA[n] - Fp[n]);
             const double u = PF ? curU[n] : f.Uc[n * g.ncell + cu];
-            f.Uc[n * g.ncell + cu] = u + (double)rhs;
+            f.Uc[n * g.ncell + cu] = u + to_f64(rhs);
           }
           if (invdt) {
             const double prev = (invdt == 1) ? 0.0 : (PF ? curI : f.InvDt[cu]);
@@ -686,7 +724,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
             if constexpr (sizeof(T) == 8) {
               inv = prev + 0.5 * (r.cmax + cp) / (g.dx[DIR]);
             } else {
-              inv = prev + (double)(T(0.5) * (r.cmax + cp) * invdxT);
+              inv = prev + to_f64(T(0.5) * (r.cmax + cp) * invdxT);
             }
             f.InvDt[cu] = inv;
             if (inv > run_max) run_max = inv;  // NaN never compares greater
@@ -820,7 +858,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
 #pragma unroll
     for (int n = 0; n < v::BX1; n++) FA[n] = T(0);
     if (face) {
-      const T bn = (T)vs[frow + i];
+      const T bn = from_f64<T>(vs[frow + i]);
       vL[dd::BXn] = bn;
       vR[dd::BXn] = bn;
       RiemannOut<D, T> r;
@@ -844,7 +882,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
 #pragma unroll
       for (int n = 0; n < v::BX1; n++) {
         const T rhs = -dtdVT * (FA[n] - FAp[n]);
-        f.Uc[n * g.ncell + cu] = f.Uc[n * g.ncell + cu] + (double)rhs;
+        f.Uc[n * g.ncell + cu] = f.Uc[n * g.ncell + cu] + to_f64(rhs);
       }
       if (invdt) {
         const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
@@ -852,7 +890,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
         if constexpr (sizeof(T) == 8) {
           inv = prev + 0.5 * (cm + cp) / (g.dx[0]);
         } else {
-          inv = prev + (double)(T(0.5) * (cm + cp) * invdxT);
+          inv = prev + to_f64(T(0.5) * (cm + cp) * invdxT);
         }
         f.InvDt[cu] = inv;
         if (inv > run_max) run_max = inv;
@@ -889,36 +927,41 @@ __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl*
 // uct_hll / uct_hlld: calcRiemannEmf.hpp).  One thread per edge position
 // (k,j,i) in [beg, end]^D; writes ez (and ex, ey in 3-D).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double riemann_edge(int order, const double* q, long long fq, long long fs,
-                                               const double* e, long long c, long long s,
-                                               const double* AL, const double* AR, const double* DL,
-                                               const double* DR, long long sp, double& phi) {
-  const double aL = 0.5 * (AL[c - sp] + AL[c]);
-  const double aR = 0.5 * (AR[c - sp] + AR[c]);
-  const double dL = 0.5 * (DL[c - sp] + DL[c]);
-  const double dR = 0.5 * (DR[c - sp] + DR[c]);
-  double bL, bR, vLv, vRv, db, dv;
+// E: type of the EMF buffers and of the averaging (the face field q is
+// FP64 and is read in E)
+template <typename E>
+__device__ __forceinline__ E riemann_edge(int order, const double* q, long long fq, long long fs,
+                                          const E* e, long long c, long long s,
+                                          const E* AL, const E* AR, const E* DL,
+                                          const E* DR, long long sp, E& phi) {
+  const E h = E(0.5);
+  const E aL = h * (AL[c - sp] + AL[c]);
+  const E aR = h * (AR[c - sp] + AR[c]);
+  const E dL = h * (DL[c - sp] + DL[c]);
+  const E dR = h * (DR[c - sp] + DR[c]);
+  E bL, bR, vLv, vRv, db, dv;
   const long long fm = fq - fs, m = c - s;
+  auto Q = [&](long long x) { return from_f64<E>(q[x]); };
   if (order == 4) {
-    ppm_states(q[fm - 2 * fs], q[fm - fs], q[fm], q[fm + fs], q[fm + 2 * fs], db, bL);
-    ppm_states(q[fq - 2 * fs], q[fq - fs], q[fq], q[fq + fs], q[fq + 2 * fs], bR, db);
+    ppm_states(Q(fm - 2 * fs), Q(fm - fs), Q(fm), Q(fm + fs), Q(fm + 2 * fs), db, bL);
+    ppm_states(Q(fq - 2 * fs), Q(fq - fs), Q(fq), Q(fq + fs), Q(fq + 2 * fs), bR, db);
     ppm_states(e[m - 2 * s], e[m - s], e[m], e[m + s], e[m + 2 * s], dv, vLv);
     ppm_states(e[c - 2 * s], e[c - s], e[c], e[c + s], e[c + 2 * s], vRv, dv);
   } else {
-    db = lim_mc(q[fm + fs] - q[fm], q[fm] - q[fm - fs]);
-    bL = q[fm] + 0.5 * db;
-    db = lim_mc(q[fq + fs] - q[fq], q[fq] - q[fq - fs]);
-    bR = q[fq] - 0.5 * db;
+    db = lim_mc(Q(fm + fs) - Q(fm), Q(fm) - Q(fm - fs));
+    bL = Q(fm) + h * db;
+    db = lim_mc(Q(fq + fs) - Q(fq), Q(fq) - Q(fq - fs));
+    bR = Q(fq) - h * db;
     dv = lim_mc(e[m + s] - e[m], e[m] - e[m - s]);
-    vLv = e[m] + 0.5 * dv;
+    vLv = e[m] + h * dv;
     dv = lim_mc(e[c + s] - e[c], e[c] - e[c - s]);
-    vRv = e[c] - 0.5 * dv;
+    vRv = e[c] - h * dv;
   }
   phi = dR * bR - dL * bL;
   return aL * vLv * bL + aR * vRv * bR;
 }
 
-template <int D>
+template <int D, typename E = double>
 __device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const Ctl* ctl, dim3 bid) {
   if (ctl->done) return;
   const int nx = g.n[0] + 1, ny = g.n[1] + 1;
@@ -931,92 +974,100 @@ __device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const
   const int k = (D == 3) ? g.beg[2] + (int)(r / ny) : 0;
   const long long c = cidx(g, k, j, i);
   const long long si = 1, sj = g.s[1], sk = g.s[2];
-  const double* ezi = f.ezi;
-  const double* ezj = f.ezj;
+  const E* ezi = emf<E>(f.ezi);
+  const E* ezj = emf<E>(f.ezj);
+  const E *exj = emf<E>(f.exj), *exk = emf<E>(f.exk), *eyi = emf<E>(f.eyi), *eyk = emf<E>(f.eyk);
+  E* ex = emf<E>(f.ex);
+  E* ey = emf<E>(f.ey);
+  E* ez = emf<E>(f.ez);
   if (g.emf == kEmfUctHll || g.emf == kEmfUctHlld) {
     const long long fc = fidx(g, k, j, i);
     const double* Vs1 = f.Vs;
     const double* Vs2 = f.Vs + g.nface;
-    double phi, X, ezv;
-    X = riemann_edge(g.order, Vs2, fc, 1, ezj, c, si, f.aL[0], f.aR[0], f.dL[0], f.dR[0], sj, phi);
+    const E *aL0 = emf<E>(f.aL[0]), *aR0 = emf<E>(f.aR[0]), *dL0 = emf<E>(f.dL[0]), *dR0 = emf<E>(f.dR[0]);
+    const E *aL1 = emf<E>(f.aL[1]), *aR1 = emf<E>(f.aR[1]), *dL1 = emf<E>(f.dL[1]), *dR1 = emf<E>(f.dR[1]);
+    E phi, X, ezv;
+    X = riemann_edge<E>(g.order, Vs2, fc, 1, ezj, c, si, aL0, aR0, dL0, dR0, sj, phi);
     ezv = X + phi;
     if constexpr (D == 3) {
       const double* Vs3 = f.Vs + 2 * g.nface;
-      double eyv, exv;
-      X = riemann_edge(g.order, Vs3, fc, 1, f.eyk, c, si, f.aL[0], f.aR[0], f.dL[0], f.dR[0], sk, phi);
+      const E *aL2 = emf<E>(f.aL[2]), *aR2 = emf<E>(f.aR[2]), *dL2 = emf<E>(f.dL[2]), *dR2 = emf<E>(f.dR[2]);
+      E eyv, exv;
+      X = riemann_edge<E>(g.order, Vs3, fc, 1, eyk, c, si, aL0, aR0, dL0, dR0, sk, phi);
       eyv = X - phi;
-      X = riemann_edge(g.order, Vs3, fc, g.fs[1], f.exk, c, sj, f.aL[1], f.aR[1], f.dL[1], f.dR[1], sk, phi);
+      X = riemann_edge<E>(g.order, Vs3, fc, g.fs[1], exk, c, sj, aL1, aR1, dL1, dR1, sk, phi);
       exv = X + phi;
-      X = riemann_edge(g.order, Vs1, fc, g.fs[1], ezi, c, sj, f.aL[1], f.aR[1], f.dL[1], f.dR[1], si, phi);
+      X = riemann_edge<E>(g.order, Vs1, fc, g.fs[1], ezi, c, sj, aL1, aR1, dL1, dR1, si, phi);
       ezv += X - phi;
-      X = riemann_edge(g.order, Vs1, fc, g.fs[2], f.eyi, c, sk, f.aL[2], f.aR[2], f.dL[2], f.dR[2], si, phi);
+      X = riemann_edge<E>(g.order, Vs1, fc, g.fs[2], eyi, c, sk, aL2, aR2, dL2, dR2, si, phi);
       eyv += X + phi;
-      X = riemann_edge(g.order, Vs2, fc, g.fs[2], f.exj, c, sk, f.aL[2], f.aR[2], f.dL[2], f.dR[2], sj, phi);
+      X = riemann_edge<E>(g.order, Vs2, fc, g.fs[2], exj, c, sk, aL2, aR2, dL2, dR2, sj, phi);
       exv += X - phi;
-      f.ex[c] = exv;
-      f.ey[c] = eyv;
+      ex[c] = exv;
+      ey[c] = eyv;
     } else {
-      X = riemann_edge(g.order, Vs1, fc, g.fs[1], ezi, c, sj, f.aL[1], f.aR[1], f.dL[1], f.dR[1], si, phi);
+      X = riemann_edge<E>(g.order, Vs1, fc, g.fs[1], ezi, c, sj, aL1, aR1, dL1, dR1, si, phi);
       ezv += X - phi;
     }
-    f.ez[c] = ezv;
+    ez[c] = ezv;
     return;
   }
+  const E* Ex1 = emf<E>(f.Ex1);
+  const E* Ex2 = emf<E>(f.Ex2);
+  const E* Ex3 = emf<E>(f.Ex3);
   if (g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
-    const double w = 0.25;
+    const E w = E(0.25);
     if (g.emf == kEmfArithmetic) {
       if constexpr (D == 3) {
-        f.ex[c] = w * (f.exj[c] + f.exj[c - sk] + f.exk[c] + f.exk[c - sj]);
-        f.ey[c] = w * (f.eyi[c] + f.eyi[c - sk] + f.eyk[c] + f.eyk[c - si]);
+        ex[c] = w * (exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
+        ey[c] = w * (eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
       }
-      f.ez[c] = w * (ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
+      ez[c] = w * (ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
     } else {
       // CalcUCT0Average: face EMFs become 2 e - (cell EMF average), computed
       // here for the four faces around the edge (calcCornerEmf.hpp:150-190)
-      auto mz_i = [&](long long q) { double a = ezi[q] * 2.0; return a - 0.5 * (f.Ex3[q - si] + f.Ex3[q]); };
-      auto mz_j = [&](long long q) { double a = ezj[q] * 2.0; return a - 0.5 * (f.Ex3[q - sj] + f.Ex3[q]); };
+      const E two = E(2), h = E(0.5);
+      auto mz_i = [&](long long q) { E a = ezi[q] * two; return a - h * (Ex3[q - si] + Ex3[q]); };
+      auto mz_j = [&](long long q) { E a = ezj[q] * two; return a - h * (Ex3[q - sj] + Ex3[q]); };
       if constexpr (D == 3) {
-        auto mx_j = [&](long long q) { double a = f.exj[q] * 2.0; return a - 0.5 * (f.Ex1[q - sj] + f.Ex1[q]); };
-        auto mx_k = [&](long long q) { double a = f.exk[q] * 2.0; return a - 0.5 * (f.Ex1[q - sk] + f.Ex1[q]); };
-        auto my_i = [&](long long q) { double a = f.eyi[q] * 2.0; return a - 0.5 * (f.Ex2[q - si] + f.Ex2[q]); };
-        auto my_k = [&](long long q) { double a = f.eyk[q] * 2.0; return a - 0.5 * (f.Ex2[q - sk] + f.Ex2[q]); };
-        f.ex[c] = w * (mx_j(c) + mx_j(c - sk) + mx_k(c) + mx_k(c - sj));
-        f.ey[c] = w * (my_i(c) + my_i(c - sk) + my_k(c) + my_k(c - si));
+        auto mx_j = [&](long long q) { E a = exj[q] * two; return a - h * (Ex1[q - sj] + Ex1[q]); };
+        auto mx_k = [&](long long q) { E a = exk[q] * two; return a - h * (Ex1[q - sk] + Ex1[q]); };
+        auto my_i = [&](long long q) { E a = eyi[q] * two; return a - h * (Ex2[q - si] + Ex2[q]); };
+        auto my_k = [&](long long q) { E a = eyk[q] * two; return a - h * (Ex2[q - sk] + Ex2[q]); };
+        ex[c] = w * (mx_j(c) + mx_j(c - sk) + mx_k(c) + mx_k(c - sj));
+        ey[c] = w * (my_i(c) + my_i(c - sk) + my_k(c) + my_k(c - si));
       }
-      f.ez[c] = w * (mz_i(c) + mz_i(c - sj) + mz_j(c) + mz_j(c - si));
+      ez[c] = w * (mz_i(c) + mz_i(c - sj) + mz_j(c) + mz_j(c - si));
     }
     return;
   }
   // uct_contact (calcCornerEmf.hpp:224-282)
-  const double* wsx = f.svx;
-  const double* wsy = f.svy;
-  const double* Ex3 = f.Ex3;
-  const double ez_l2 = (1 - wsx[c - sj]) * (ezj[c] - Ex3[c - sj]) + (wsx[c - sj]) * (ezj[c - si] - Ex3[c - sj - si]);
-  const double ez_r2 = (1 - wsx[c]) * (ezj[c] - Ex3[c]) + (wsx[c]) * (ezj[c - si] - Ex3[c - si]);
-  const double ez_l1 = (1 - wsy[c - si]) * (ezi[c] - Ex3[c - si]) + (wsy[c - si]) * (ezi[c - sj] - Ex3[c - sj - si]);
-  const double ez_r1 = (1 - wsy[c]) * (ezi[c] - Ex3[c]) + (wsy[c]) * (ezi[c - sj] - Ex3[c - sj]);
-  f.ez[c] = 0.25 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
+  const E* wsx = emf<E>(f.svx);
+  const E* wsy = emf<E>(f.svy);
+  const E one = E(1), q4 = E(0.25);
+  const E ez_l2 = (one - wsx[c - sj]) * (ezj[c] - Ex3[c - sj]) + (wsx[c - sj]) * (ezj[c - si] - Ex3[c - sj - si]);
+  const E ez_r2 = (one - wsx[c]) * (ezj[c] - Ex3[c]) + (wsx[c]) * (ezj[c - si] - Ex3[c - si]);
+  const E ez_l1 = (one - wsy[c - si]) * (ezi[c] - Ex3[c - si]) + (wsy[c - si]) * (ezi[c - sj] - Ex3[c - sj - si]);
+  const E ez_r1 = (one - wsy[c]) * (ezi[c] - Ex3[c]) + (wsy[c]) * (ezi[c - sj] - Ex3[c - sj]);
+  ez[c] = q4 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
   if constexpr (D == 3) {
-    const double* wsz = f.svz;
-    const double* Ex1 = f.Ex1;
-    const double* Ex2 = f.Ex2;
-    const double *exj = f.exj, *exk = f.exk, *eyi = f.eyi, *eyk = f.eyk;
-    const double ex_l3 = (1 - wsy[c - sk]) * (exk[c] - Ex1[c - sk]) + (wsy[c - sk]) * (exk[c - sj] - Ex1[c - sk - sj]);
-    const double ex_r3 = (1 - wsy[c]) * (exk[c] - Ex1[c]) + (wsy[c]) * (exk[c - sj] - Ex1[c - sj]);
-    const double ex_l2 = (1 - wsz[c - sj]) * (exj[c] - Ex1[c - sj]) + (wsz[c - sj]) * (exj[c - sk] - Ex1[c - sk - sj]);
-    const double ex_r2 = (1 - wsz[c]) * (exj[c] - Ex1[c]) + (wsz[c]) * (exj[c - sk] - Ex1[c - sk]);
-    f.ex[c] = 0.25 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
-    const double ey_l3 = (1 - wsx[c - sk]) * (eyk[c] - Ex2[c - sk]) + (wsx[c - sk]) * (eyk[c - si] - Ex2[c - sk - si]);
-    const double ey_r3 = (1 - wsx[c]) * (eyk[c] - Ex2[c]) + (wsx[c]) * (eyk[c - si] - Ex2[c - si]);
-    const double ey_l1 = (1 - wsz[c - si]) * (eyi[c] - Ex2[c - si]) + (wsz[c - si]) * (eyi[c - sk] - Ex2[c - sk - si]);
-    const double ey_r1 = (1 - wsz[c]) * (eyi[c] - Ex2[c]) + (wsz[c]) * (eyi[c - sk] - Ex2[c - sk]);
-    f.ey[c] = 0.25 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
+    const E* wsz = emf<E>(f.svz);
+    const E ex_l3 = (one - wsy[c - sk]) * (exk[c] - Ex1[c - sk]) + (wsy[c - sk]) * (exk[c - sj] - Ex1[c - sk - sj]);
+    const E ex_r3 = (one - wsy[c]) * (exk[c] - Ex1[c]) + (wsy[c]) * (exk[c - sj] - Ex1[c - sj]);
+    const E ex_l2 = (one - wsz[c - sj]) * (exj[c] - Ex1[c - sj]) + (wsz[c - sj]) * (exj[c - sk] - Ex1[c - sk - sj]);
+    const E ex_r2 = (one - wsz[c]) * (exj[c] - Ex1[c]) + (wsz[c]) * (exj[c - sk] - Ex1[c - sk]);
+    ex[c] = q4 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
+    const E ey_l3 = (one - wsx[c - sk]) * (eyk[c] - Ex2[c - sk]) + (wsx[c - sk]) * (eyk[c - si] - Ex2[c - sk - si]);
+    const E ey_r3 = (one - wsx[c]) * (eyk[c] - Ex2[c]) + (wsx[c]) * (eyk[c - si] - Ex2[c - si]);
+    const E ey_l1 = (one - wsz[c - si]) * (eyi[c] - Ex2[c - si]) + (wsz[c - si]) * (eyi[c - sk] - Ex2[c - sk - si]);
+    const E ey_r1 = (one - wsz[c]) * (eyi[c] - Ex2[c]) + (wsz[c]) * (eyi[c - sk] - Ex2[c - sk]);
+    ey[c] = q4 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
   }
 }
 
-template <int D>
+template <int D, typename E = double>
 __global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
-  d_ct_corner<D>(g, f, ctl, blockIdx);
+  d_ct_corner<D, E>(g, f, ctl, blockIdx);
 }
 
 // ---------------------------------------------------------------------------
@@ -1024,7 +1075,9 @@ __global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
 // then the Runge-Kutta combination of the faces (AddAndStore).  Only faces
 // that the next boundary pass does not overwrite are touched.
 // ---------------------------------------------------------------------------
-template <int D>
+// E: type of the corner EMFs; they are widened exactly to FP64 and the curl
+// and the face update are FP64 on both paths (div B stays at FP64 round-off)
+template <int D, typename E = double>
 __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc, double w0, dim3 bid) {
   if (ctl->done) return;
   const int nx = g.n[0] + 1, ny = g.n[1] + 1;
@@ -1038,18 +1091,21 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
   const long long c = cidx(g, k, j, i);
   const long long fc = fidx(g, k, j, i);
   const long long si = 1, sj = g.s[1], sk = g.s[2];
-  const double* Ex1 = f.ex;
-  const double* Ex2 = f.ey;
-  const double* Ex3 = f.ez;
+  const E* e1 = emf<E>(f.ex);
+  const E* e2 = emf<E>(f.ey);
+  const E* e3 = emf<E>(f.ez);
+  auto Ex1 = [&](long long q) { return to_f64(e1[q]); };
+  auto Ex2 = [&](long long q) { return to_f64(e2[q]); };
+  auto Ex3 = [&](long long q) { return to_f64(e3[q]); };
   const double dtdx1 = ctl->dtdx[0], dtdx2 = ctl->dtdx[1], dtdx3 = ctl->dtdx[2];
   const bool in_i = i < g.end[0], in_j = j < g.end[1], in_k = (D == 2) || k < g.end[2];
   // BX1s: faces i in [beg, end], j, k active
   if (in_j && in_k) {
     double rhs;
     if constexpr (D == 2) {
-      rhs = 0.0 - dtdx2 * (Ex3[c + sj] - Ex3[c]);
+      rhs = 0.0 - dtdx2 * (Ex3(c + sj) - Ex3(c));
     } else {
-      rhs = 0.0 - dtdx2 * (Ex3[c + sj] - Ex3[c]) + dtdx3 * (Ex2[c + sk] - Ex2[c]);
+      rhs = 0.0 - dtdx2 * (Ex3(c + sj) - Ex3(c)) + dtdx3 * (Ex2(c + sk) - Ex2(c));
     }
     double* vs = f.Vs;
     double b = vs[fc] + rhs;
@@ -1059,9 +1115,9 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
   if (in_i && in_k) {
     double rhs;
     if constexpr (D == 2) {
-      rhs = dtdx1 * (Ex3[c + si] - Ex3[c]);
+      rhs = dtdx1 * (Ex3(c + si) - Ex3(c));
     } else {
-      rhs = dtdx1 * (Ex3[c + si] - Ex3[c]) - dtdx3 * (Ex1[c + sk] - Ex1[c]);
+      rhs = dtdx1 * (Ex3(c + si) - Ex3(c)) - dtdx3 * (Ex1(c + sk) - Ex1(c));
     }
     double* vs = f.Vs + g.nface;
     double b = vs[fc] + rhs;
@@ -1070,7 +1126,7 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
   }
   if constexpr (D == 3) {
     if (in_i && in_j) {
-      const double rhs = -dtdx1 * (Ex2[c + si] - Ex2[c]) + dtdx2 * (Ex1[c + sj] - Ex1[c]);
+      const double rhs = -dtdx1 * (Ex2(c + si) - Ex2(c)) + dtdx2 * (Ex1(c + sj) - Ex1(c));
       double* vs = f.Vs + 2 * g.nface;
       double b = vs[fc] + rhs;
       if (combine) b = wc * b + w0 * f.Vs0[2 * g.nface + fc];
@@ -1079,9 +1135,9 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
   }
 }
 
-template <int D>
+template <int D, typename E = double>
 __global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
-  d_ct_faces<D>(g, f, ctl, combine, wc, w0, blockIdx);
+  d_ct_faces<D, E>(g, f, ctl, combine, wc, w0, blockIdx);
 }
 
 // ---------------------------------------------------------------------------

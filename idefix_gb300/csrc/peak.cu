@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/idefix_gb300.h"
+#include "fpconv.cuh"
 #include "intdiv.cuh"
 
 namespace {
@@ -56,7 +57,44 @@ __global__ void k_check_division(long long n, unsigned long long seed, unsigned 
   if (__double_as_longlong(r0) != __double_as_longlong(r1)) atomicAdd(bad, 1ull);
 }
 
+// f2d_exact on a stride of all binary32 patterns, d2f_rn on random binary64
+// values (any pattern, the binary32 range and its edges, rounding ties)
+__global__ void k_check_conversions(long long n, unsigned long long seed, unsigned long long* bad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const unsigned long long h1 = mix(seed ^ (2 * i)), h2 = mix(seed ^ (2 * i + 1));
+  const float f = __uint_as_float((unsigned)h1);
+  const double a0 = (double)f, a1 = idfx::f2d_exact(f);
+  if (__double_as_longlong(a0) != __double_as_longlong(a1) && !(a0 != a0 && a1 != a1)) atomicAdd(bad, 1ull);
+  unsigned long long u;
+  switch (h2 % 3) {
+    case 0: u = h1 ^ h2; break;
+    case 1: u = (h2 & (1ull << 63)) | ((860 + (h1 >> 40) % 330) << 52) | (h2 & ((1ull << 52) - 1)); break;
+    default: {
+      const unsigned long long m = ((h1 & ((1ull << 23) - 1)) << 29) + (1ull << 28) + (h2 >> 61) - 2;
+      u = (h2 & (1ull << 63)) | ((897 + (h1 >> 40) % 254) << 52) | (m & ((1ull << 52) - 1));
+    }
+  }
+  const double x = __longlong_as_double((long long)u);
+  const float b0 = __double2float_rn(x), b1 = idfx::d2f_rn(x);
+  if (__float_as_uint(b0) != __float_as_uint(b1) && !(b0 != b0 && b1 != b1)) atomicAdd(bad, 1ull);
+}
+
 }  // namespace
+
+extern "C" int idfx_check_conversions(long long n, unsigned long long seed, long long* mismatches) {
+  if (!mismatches || n < 0) return IDFX_ERR_STATE;
+  unsigned long long* bad = nullptr;
+  if (cudaMalloc(&bad, sizeof(*bad)) != cudaSuccess) return IDFX_ERR_CUDA;
+  cudaMemset(bad, 0, sizeof(*bad));
+  if (n > 0) k_check_conversions<<<(unsigned)((n + 255) / 256), 256>>>(n, seed, bad);
+  unsigned long long h = 0;
+  const cudaError_t rc = cudaMemcpy(&h, bad, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(bad);
+  if (rc != cudaSuccess || cudaGetLastError() != cudaSuccess) return IDFX_ERR_CUDA;
+  *mismatches = (long long)h;
+  return IDFX_OK;
+}
 
 extern "C" int idfx_check_division(long long n, unsigned long long seed, long long* mismatches) {
   if (!mismatches || n < 0) return IDFX_ERR_STATE;

@@ -168,6 +168,10 @@ int idfx_measure_fp64_peak(double* gops, void* stream);
  * (used by the whole-array cons <-> prim passes): n random operand pairs
  * compared bit for bit with the hardware division */
 int idfx_check_division(long long n, unsigned long long seed, long long* mismatches);
+/* self-check of the FP32 <-> FP64 conversions computed on the integer pipe
+ * (mixed-precision path): n random values each way, bit for bit against the
+ * hardware conversions */
+int idfx_check_conversions(long long n, unsigned long long seed, long long* mismatches);
 
 /* Allocation-free Fluid::EvolveStage — no counterpart in the reference.
  * For callers that may not allocate GPU memory while they step (state held
