@@ -259,7 +259,11 @@ void queue_cycle(Engine& e, int use_tstop) {
     const int save = (e.nstages > 1 && stage == 0);
     launch_boundaries(e);
     launch_fill_faces(e, save);
-    launch_stage_begin(e, kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
+    // mixed path: Uc carried over from the previous stage end when it is
+    // still the state Vc came from (Ctl::uc_fresh); the FP64 path rebuilds it
+    // as the reference does
+    const int cons = kSbCons | (e.precision == IDFX_MIXED ? kSbKeepCons : 0);
+    launch_stage_begin(e, cons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
     if (e.f.shock) launch_find_shock(e);  // RiemannSolver::CalcFlux (calcFlux.hpp:33)
     if (g.order == IDFX_LEARNED) launch_learned_recon(e);
     launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
@@ -655,6 +659,7 @@ static int copy_state(idfx_gpu* h, const double* Vc, const double* Vs, cudaMemcp
   const size_t bc = sizeof(double) * (2 * e.g.D + 2) * e.g.ncell;
   const size_t bs = sizeof(double) * e.g.D * e.g.nface;
   if (up) {
+    IDFX_CK(cudaMemsetAsync(&e.ctl->uc_fresh, 0, sizeof(int), e.stream));  // Uc no longer Vc's
     if (Vc) IDFX_CK(cudaMemcpyAsync(e.f.Vc, Vc, bc, kind, e.stream));
     if (Vs) IDFX_CK(cudaMemcpyAsync(e.f.Vs, Vs, bs, kind, e.stream));
   } else {
@@ -758,8 +763,12 @@ int idfx_gpu_run(idfx_gpu* h, double tstop, long long max_cycles) {
 // ---------------------------------------------------------------------------
 // building blocks
 // ---------------------------------------------------------------------------
-// the building blocks run whatever the time-integrator control says
-static void clear_done(Engine& e) { cudaMemsetAsync(&e.ctl->done, 0, sizeof(int), e.stream); }
+// the building blocks run whatever the time-integrator control says; after
+// any of them the next cycle rebuilds the conserved state from Vc
+static void clear_done(Engine& e) {
+  cudaMemsetAsync(&e.ctl->uc_fresh, 0, sizeof(int), e.stream);
+  cudaMemsetAsync(&e.ctl->done, 0, sizeof(int), e.stream);
+}
 
 static int sync_status(Engine& e) {
   IDFX_CK(cudaGetLastError());

@@ -231,7 +231,8 @@ void queue_cycle(EnsEngine& e, bool checks) {
     const int save = (e.nstages > 1 && stage == 0);
     IDFX_ENS_D(ke_fill_faces, e.fill.n, e.d_boxes, e.fill.items, save);
     IDFX_ENS_DE(ke_stage_begin, e.begin.n, e.d_boxes, e.begin.items,
-               kSbCons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
+               kSbCons | (e.precision == IDFX_MIXED ? kSbKeepCons : 0) | (save ? kSbSaveBegin : 0) |
+                   (cell_emf ? kSbCellEmf : 0));
     // shock flags: the stage-begin table covers (n + 2)^D cells of every box
     if (e.shock) IDFX_ENS_D(ke_find_shock, e.begin.n, e.d_boxes, e.begin.items);
     for (int d = 0; d < e.D; d++)
@@ -626,6 +627,7 @@ static int ens_copy(idfx_ens* h, int box, const double* Vc, const double* Vs, bo
   const size_t bs = sizeof(double) * B.g.D * B.g.nface;
   cudaError_t rc = cudaSuccess;
   if (up) {
+    rc = cudaMemsetAsync(&B.ctl->uc_fresh, 0, sizeof(int), e.stream);  // Uc no longer Vc's
     if (Vc && rc == cudaSuccess) rc = cudaMemcpyAsync(B.f.Vc, Vc, bc, cudaMemcpyHostToDevice, e.stream);
     if (Vs && rc == cudaSuccess) rc = cudaMemcpyAsync(B.f.Vs, Vs, bs, cudaMemcpyHostToDevice, e.stream);
   } else {

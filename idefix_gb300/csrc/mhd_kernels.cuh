@@ -58,6 +58,8 @@ struct Ctl {
   long long ncycles;
   int done;    // 1: every kernel returns at entry
   int status;  // Status
+  int uc_fresh;  // 1: Uc (active cells) is the state the last stage end left
+                 // and Vc was derived from it; 0 after any write from outside
 };
 
 // The EMF buffers (face EMFs ezi..eyk, upwind weights sv*, cell EMFs Ex*,
@@ -170,7 +172,11 @@ __global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
 // the active cells (ConvertPrimToCons), RK begin copy, and the cell-centred
 // EMF E = -v x B used by uct_contact / uct0 (calcCornerEmf.hpp:84-126).
 // ---------------------------------------------------------------------------
-enum { kSbCons = 1, kSbSaveBegin = 2, kSbCellEmf = 4 };
+// kSbKeepCons (mixed path): while Ctl::uc_fresh says that the conserved
+// state of the active cells is the one the previous stage end left (Vc was
+// derived from it), it is kept instead of being rebuilt from Vc; with
+// kSbSaveBegin it is copied to Uc0.
+enum { kSbCons = 1, kSbSaveBegin = 2, kSbCellEmf = 4, kSbKeepCons = 8 };
 
 // E: type of the EMF buffers (float on the mixed path: the cell EMF is then
 // computed in FP32 from the FP32 primitives that the sweeps read)
@@ -211,7 +217,8 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
   }
 #pragma unroll
   for (int d = 0; d < D; d++) f.Vc[(v::BX1 + d) * g.ncell + c] = V[v::BX1 + d];
-  if (!ghost && (flags & kSbCons)) {
+  const bool keep = (flags & kSbKeepCons) && ctl->uc_fresh;
+  if (!ghost && !keep && (flags & kSbCons)) {
     double U[NV];
     prim_to_cons<D, true>(g.gm1, U, V);
 #pragma unroll
@@ -220,6 +227,10 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
 #pragma unroll
       for (int n = 0; n < NV; n++) f.Uc0[n * g.ncell + c] = U[n];
     }
+  } else if (!ghost && keep && (flags & kSbSaveBegin)) {
+    // the Runge-Kutta combination reads the non-field variables of Uc0
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) f.Uc0[n * g.ncell + c] = f.Uc[n * g.ncell + c];
   }
   // the primitives in the EMF type (the FP32 copy on the mixed path)
   E W[NV];
@@ -1159,6 +1170,7 @@ __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const
   const int k = (D == 3) ? g.beg[2] + (int)(r / g.n[1]) : 0;
   const long long c = cidx(g, k, j, i);
   const long long fc = fidx(g, k, j, i);
+  if (tid == 0) ((Ctl*)ctl)->uc_fresh = 1;  // read by the next stage begin
   double U[NV], V[NV];
 #pragma unroll
   for (int n = 0; n < v::BX1; n++) {
