@@ -327,6 +327,8 @@ bool box_geometry(const idfx_gpu_config* cfg, Geo& g) {
   }
   g.gamma = cfg->gamma;
   g.gm1 = cfg->gamma - 1.0;
+  g.rgm1 = 1.0 / g.gm1;  // correctly rounded reciprocals (Markstein quotients)
+  for (int d = 0; d < 3; d++) g.rdx[d] = 1.0 / g.dx[d];
   g.ext = 1;
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
   g.shock_smoothing = cfg->shock_smoothing;

@@ -42,6 +42,8 @@ struct Geo {
   double gamma, gm1;
   int ext;  // perpendicular extension of the flux sweeps for CT
   double shock_smoothing;  // [Hydro] shockFlattening value (flags in Fields::shock)
+  double rgm1;    // RN(1 / gm1), for the FP64 Riemann solvers
+  double rdx[3];  // RN(1 / dx[d]), for the InvDt quotient
   int bc[3][2];  // boundary type per direction and side (IDFX_BC_*: 0 periodic)
   int nonper;    // some direction is not periodic: ghosts filled by k_bc_* first
 };
@@ -712,7 +714,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
       vL[dd::BXn] = bn;
       vR[dd::BXn] = bn;
       RiemannOut<D, T> r;
-      riemann<D, DIR, SOLVER>(gam, vL, vR, r);
+      riemann<D, DIR, SOLVER>(gam, (T)g.rgm1, vL, vR, r);
       store_emf<D, DIR>(g, f, cc, r, vL, vR);
       if (active_col) {
         // flux x area and the flux difference in the arithmetic type T; the
@@ -733,7 +735,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
             const double prev = (invdt == 1) ? 0.0 : (PF ? curI : f.InvDt[cu]);
             double inv;
             if constexpr (sizeof(T) == 8) {
-              inv = prev + 0.5 * (r.cmax + cp) / (g.dx[DIR]);
+              inv = prev + div_r(0.5 * (r.cmax + cp), Recip{g.dx[DIR], g.rdx[DIR]});
             } else {
               inv = prev + to_f64(T(0.5) * (r.cmax + cp) * invdxT);
             }
@@ -873,7 +875,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
       vL[dd::BXn] = bn;
       vR[dd::BXn] = bn;
       RiemannOut<D, T> r;
-      riemann<D, 0, SOLVER>(gam, vL, vR, r);
+      riemann<D, 0, SOLVER>(gam, (T)g.rgm1, vL, vR, r);
       store_emf<D, 0>(g, f, cc, r, vL, vR);
 #pragma unroll
       for (int n = 0; n < v::BX1; n++) FA[n] = r.F[n] * areaT;
@@ -899,7 +901,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
         const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
         double inv;
         if constexpr (sizeof(T) == 8) {
-          inv = prev + 0.5 * (cm + cp) / (g.dx[0]);
+          inv = prev + div_r(0.5 * (cm + cp), Recip{g.dx[0], g.rdx[0]});
         } else {
           inv = prev + to_f64(T(0.5) * (cm + cp) * invdxT);
         }

@@ -16,6 +16,7 @@
 #include <cstdint>
 
 #include "intdiv.cuh"
+#include "rdiv.cuh"
 
 namespace idfx {
 
@@ -73,9 +74,12 @@ __device__ __forceinline__ T sumsq(T a, T b, T c) {
 // cons <-> prim (convertConsToPrim.hpp:15-100; eos_adiabatic.hpp:38-45)
 // gm1 = gamma - 1.0, evaluated once on the host
 // ---------------------------------------------------------------------------
-// INTDIV: quotients on the integer pipe (whole-array kernels)
-template <int D, bool INTDIV = false, typename T>
-__device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V) {
+// QUOT: how p / gm1 is formed - 0 the hardware division, 1 on the integer
+// pipe (whole-array kernels), 2 from rgm1 = RN(1 / gm1) formed once on the
+// host (Riemann solvers, FP64: Markstein's correction, rdiv.cuh); all three
+// give the correctly rounded quotient
+template <int D, int QUOT = 0, typename T>
+__device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V, T rgm1 = T(0)) {
   using v = Var<D>;
   U[v::RHO] = V[v::RHO];
   U[v::MX1] = V[v::MX1] * V[v::RHO];
@@ -93,7 +97,16 @@ __device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V) {
     kin = sumsq<2>(V[v::MX1], V[v::MX2], z);
     mag = sumsq<2>(U[v::BX1], U[v::BX2], z);
   }
-  U[v::ENG] = (INTDIV ? dvi(V[v::PRS], gm1) : dv(V[v::PRS], gm1)) + T(0.5) * V[v::RHO] * kin + T(0.5) * mag;
+  T pq;
+  if constexpr (QUOT == 1) {
+    pq = dvi(V[v::PRS], gm1);
+  } else if constexpr (QUOT == 2 && sizeof(T) == 8) {
+    pq = div_r(V[v::PRS], Recip{gm1, rgm1});
+  } else {
+    (void)rgm1;
+    pq = dv(V[v::PRS], gm1);
+  }
+  U[v::ENG] = pq + T(0.5) * V[v::RHO] * kin + T(0.5) * mag;
 }
 
 template <int D, bool INTDIV = false, typename T>
@@ -324,6 +337,26 @@ struct RiemannOut {
   T cmax, sl, sr;
 };
 
+// a / b where several quotients share b: on the FP64 path with the
+// reciprocal R = recip(b) formed once (Markstein, rdiv.cuh), bit-identical to
+// a / b; the FP32 path divides
+template <typename T>
+__device__ __forceinline__ T shared_div(T a, T b, const Recip& R) {
+  if constexpr (sizeof(T) == 8) {
+    return div_r(a, R);
+  } else {
+    return dv(a, b);
+  }
+}
+template <typename T>
+__device__ __forceinline__ Recip shared_recip(T b) {
+  if constexpr (sizeof(T) == 8) {
+    return recip(b);
+  } else {
+    return Recip{0.0, 0.0};
+  }
+}
+
 // fast magnetosonic speed of one face state (hlldMHD.hpp:205-238)
 template <int D, int DIR, typename T>
 __device__ __forceinline__ T fast_speed(T gamma, const T* v) {
@@ -352,7 +385,7 @@ __device__ __forceinline__ T half_b2(const T* v) {
 // HLLD (Miyoshi & Kusano 2005) with the reference's HLLC fall-back near
 // degeneracy (hlldMHD.hpp:147-457, energy equation branch)
 template <int D, int DIR, typename T>
-__device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
+__device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
@@ -371,8 +404,8 @@ __device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, 
   r.sr = sr;
   r.cmax = fmax(fabs(sl), fabs(sr));
   const T gm1 = gamma - T(1);
-  prim_to_cons<D>(gm1, uL, vL);
-  prim_to_cons<D>(gm1, uR, vR);
+  prim_to_cons<D, 2>(gm1, uL, vL, rgm1);
+  prim_to_cons<D, 2>(gm1, uR, vR, rgm1);
   phys_flux<D, DIR>(fluxL, vL, uL);
   phys_flux<D, DIR>(fluxR, vR, uR);
   const T ptL = vL[v::PRS] + half_b2<D>(vL);
@@ -401,8 +434,10 @@ __device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, 
   const T SM = (duR * uR[Xn] - duL * uL[Xn] - ptR + ptL) * scrh;
   T pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR + vL[RHO] * vR[RHO] * duR * duL * (vR[Xn] - vL[Xn]);
   pts *= scrh;
-  usL[RHO] = dv(uL[RHO] * duL, sl - SM);
-  usR[RHO] = dv(uR[RHO] * duR, sr - SM);
+  // (sl - SM) and (sr - SM) divide the star density and the star energy
+  const Recip RsL = shared_recip(sl - SM), RsR = shared_recip(sr - SM);
+  usL[RHO] = shared_div(uL[RHO] * duL, sl - SM, RsL);
+  usR[RHO] = shared_div(uR[RHO] * duR, sr - SM, RsR);
   const T sqrL = sqrt(usL[RHO]);
   const T sqrR = sqrt(usR[RHO]);
   T S1L = SM - dv(fabs(Bx), sqrL);
@@ -456,7 +491,7 @@ __device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, 
     scrhL -= b;
   }
   usL[ENG] = duL * uL[ENG] - ptL * vL[Xn] + pts * SM + Bx * scrhL;
-  usL[ENG] = dv(usL[ENG], sl - SM);
+  usL[ENG] = shared_div(usL[ENG], sl - SM, RsL);
   {
     T a = vR[Xn] * Bx + vR[Xt] * uR[BXt];
     if constexpr (D == 3) a = a + vR[Xb] * uR[BXb];
@@ -466,7 +501,7 @@ __device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, 
     scrhR -= b;
   }
   usR[ENG] = duR * uR[ENG] - ptR * vR[Xn] + pts * SM + Bx * scrhR;
-  usR[ENG] = dv(usR[ENG], sr - SM);
+  usR[ENG] = shared_div(usR[ENG], sr - SM, RsR);
 
   if (S1L >= T(0)) {
 #pragma unroll
@@ -479,11 +514,13 @@ __device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, 
     T ussl[NV], ussr[NV];
     ussl[RHO] = usL[RHO];
     ussr[RHO] = usR[RHO];
+    // (sqrL + sqrR) divides the four double-star velocity and field values
+    const Recip Rq = shared_recip(sqrL + sqrR);
     vss = sqrL * vsL + sqrR * vsR + (usR[BXt] - usL[BXt]) * sBx;
-    vss = dv(vss, sqrL + sqrR);
+    vss = shared_div(vss, sqrL + sqrR, Rq);
     if constexpr (D == 3) {
       wss = sqrL * wsL + sqrR * wsR + (usR[BXb] - usL[BXb]) * sBx;
-      wss = dv(wss, sqrL + sqrR);
+      wss = shared_div(wss, sqrL + sqrR, Rq);
     }
     ussl[Xn] = ussl[RHO] * SM;
     ussr[Xn] = ussr[RHO] * SM;
@@ -495,11 +532,11 @@ __device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, 
     }
     ussl[BXn] = ussr[BXn] = Bx;
     ussl[BXt] = sqrL * usR[BXt] + sqrR * usL[BXt] + sqrL * sqrR * (vsR - vsL) * sBx;
-    ussl[BXt] = dv(ussl[BXt], sqrL + sqrR);
+    ussl[BXt] = shared_div(ussl[BXt], sqrL + sqrR, Rq);
     ussr[BXt] = ussl[BXt];
     if constexpr (D == 3) {
       ussl[BXb] = sqrL * usR[BXb] + sqrR * usL[BXb] + sqrL * sqrR * (wsR - wsL) * sBx;
-      ussl[BXb] = dv(ussl[BXb], sqrL + sqrR);
+      ussl[BXb] = shared_div(ussl[BXb], sqrL + sqrR, Rq);
       ussr[BXb] = ussl[BXb];
     }
     {
@@ -530,7 +567,7 @@ __device__ __forceinline__ void riemann_hlld(T gamma, const T* vL, const T* vR, 
 
 // HLL (hllMHD.hpp:154-453; the Hall whistler term is not part of ideal MHD)
 template <int D, int DIR, typename T>
-__device__ __forceinline__ void riemann_hll(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
+__device__ __forceinline__ void riemann_hll(T gamma, T rgm1, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
@@ -547,8 +584,8 @@ __device__ __forceinline__ void riemann_hll(T gamma, const T* vL, const T* vR, R
   r.sr = sr;
   r.cmax = fmax(fabs(sl), fabs(sr));
   const T gm1 = gamma - T(1);
-  prim_to_cons<D>(gm1, uL, vL);
-  prim_to_cons<D>(gm1, uR, vR);
+  prim_to_cons<D, 2>(gm1, uL, vL, rgm1);
+  prim_to_cons<D, 2>(gm1, uR, vR, rgm1);
   phys_flux<D, DIR>(fluxL, vL, uL);
   phys_flux<D, DIR>(fluxR, vR, uR);
   T* F = r.F;
@@ -584,7 +621,7 @@ __device__ __forceinline__ void riemann_hll(T gamma, const T* vL, const T* vR, R
 
 // TVDLF / Rusanov (tvdlfMHD.hpp:140-232)
 template <int D, int DIR, typename T>
-__device__ __forceinline__ void riemann_tvdlf(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
+__device__ __forceinline__ void riemann_tvdlf(T gamma, T rgm1, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
@@ -604,8 +641,8 @@ __device__ __forceinline__ void riemann_tvdlf(T gamma, const T* vL, const T* vR,
   r.cmax = cmax;
   T fluxL[NV], fluxR[NV];
   const T gm1 = gamma - T(1);
-  prim_to_cons<D>(gm1, r.uL, vL);
-  prim_to_cons<D>(gm1, r.uR, vR);
+  prim_to_cons<D, 2>(gm1, r.uL, vL, rgm1);
+  prim_to_cons<D, 2>(gm1, r.uR, vR, rgm1);
   phys_flux<D, DIR>(fluxL, vL, r.uL);
   phys_flux<D, DIR>(fluxR, vR, r.uR);
 #pragma unroll
@@ -614,7 +651,7 @@ __device__ __forceinline__ void riemann_tvdlf(T gamma, const T* vL, const T* vR,
 
 // Roe with the entropy fix (roeMHD.hpp:175-650, energy equation branch)
 template <int D, int DIR, typename T>
-__device__ __forceinline__ void riemann_roe(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
+__device__ __forceinline__ void riemann_roe(T gamma, T rgm1, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
   using d = Dir<D, DIR>;
   constexpr int NV = v::NV;
@@ -630,8 +667,8 @@ __device__ __forceinline__ void riemann_roe(T gamma, const T* vL, const T* vR, R
 #pragma unroll
   for (int n = 0; n < NV; n++) dV[n] = vR[n] - vL[n];
   const T gm1 = gamma - T(1);
-  prim_to_cons<D>(gm1, uL, vL);
-  prim_to_cons<D>(gm1, uR, vR);
+  prim_to_cons<D, 2>(gm1, uL, vL, rgm1);
+  prim_to_cons<D, 2>(gm1, uR, vR, rgm1);
 #pragma unroll
   for (int n = 0; n < NV; n++) dU[n] = uR[n] - uL[n];
   phys_flux<D, DIR>(fluxL, vL, uL);
@@ -842,12 +879,13 @@ __device__ __forceinline__ void riemann_roe(T gamma, const T* vL, const T* vR, R
   }
 }
 
+// rgm1 = RN(1 / (gamma - 1)), used by the FP64 path
 template <int D, int DIR, int SOLVER, typename T>
-__device__ __forceinline__ void riemann(T gamma, const T* vL, const T* vR, RiemannOut<D, T>& r) {
-  if constexpr (SOLVER == kHLLD) riemann_hlld<D, DIR>(gamma, vL, vR, r);
-  if constexpr (SOLVER == kHLL) riemann_hll<D, DIR>(gamma, vL, vR, r);
-  if constexpr (SOLVER == kROE) riemann_roe<D, DIR>(gamma, vL, vR, r);
-  if constexpr (SOLVER == kTVDLF) riemann_tvdlf<D, DIR>(gamma, vL, vR, r);
+__device__ __forceinline__ void riemann(T gamma, T rgm1, const T* vL, const T* vR, RiemannOut<D, T>& r) {
+  if constexpr (SOLVER == kHLLD) riemann_hlld<D, DIR>(gamma, rgm1, vL, vR, r);
+  if constexpr (SOLVER == kHLL) riemann_hll<D, DIR>(gamma, rgm1, vL, vR, r);
+  if constexpr (SOLVER == kROE) riemann_roe<D, DIR>(gamma, rgm1, vL, vR, r);
+  if constexpr (SOLVER == kTVDLF) riemann_tvdlf<D, DIR>(gamma, rgm1, vL, vR, r);
 }
 
 }  // namespace idfx

@@ -6,6 +6,7 @@
 #include "../../include/idefix_gb300.h"
 #include "fpconv.cuh"
 #include "intdiv.cuh"
+#include "rdiv.cuh"
 
 namespace {
 
@@ -55,6 +56,9 @@ __global__ void k_check_division(long long n, unsigned long long seed, unsigned 
   const double b = __longlong_as_double((long long)(((h2 & (1ull << 63))) | (eb << 52) | mb));
   const double r0 = a / b, r1 = idfx::div_rn(a, b);
   if (__double_as_longlong(r0) != __double_as_longlong(r1)) atomicAdd(bad, 1ull);
+  // the reciprocal form of the flux sweeps (rdiv.cuh)
+  const double r2 = idfx::div_r(a, idfx::recip(b));
+  if (__double_as_longlong(r0) != __double_as_longlong(r2)) atomicAdd(bad, 1ull);
 }
 
 // f2d_exact on a stride of all binary32 patterns, d2f_rn on random binary64

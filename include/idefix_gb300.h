@@ -164,9 +164,10 @@ int idfx_gpu_set_segments(idfx_gpu* h, const int* seg);  /* 1..1024 cells per th
 /* measured FP64 FMA throughput of the current device (thread operations
  * per second / 1e9), the roof of the FP64-bound sweeps; stream may be NULL */
 int idfx_measure_fp64_peak(double* gops, void* stream);
-/* self-check of the library's FP64 division computed on the integer pipe
- * (used by the whole-array cons <-> prim passes): n random operand pairs
- * compared bit for bit with the hardware division */
+/* self-check of the library's two FP64 division forms - on the integer pipe
+ * (whole-array cons <-> prim passes) and from a correctly rounded reciprocal
+ * with Markstein's correction (flux sweeps): n random operand pairs compared
+ * bit for bit with the hardware division */
 int idfx_check_division(long long n, unsigned long long seed, long long* mismatches);
 /* self-check of the FP32 <-> FP64 conversions computed on the integer pipe
  * (mixed-precision path): n random values each way, bit for bit against the

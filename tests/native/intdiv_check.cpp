@@ -9,6 +9,7 @@
 #include <random>
 
 #include "../../idefix_gb300/csrc/intdiv.cuh"
+#include "../../idefix_gb300/csrc/rdiv.cuh"
 
 static uint64_t mism = 0, total = 0;
 
@@ -19,6 +20,14 @@ static void check(double a, double b) {
   if (!same) {
     if (mism < 10)
       std::printf("mismatch a=%a b=%a ieee=%a int=%a\n", a, b, r0, r1);
+    mism++;
+  }
+  // the reciprocal form with Markstein's correction (rdiv.cuh)
+  const double r2 = idfx::div_r(a, idfx::recip(b));
+  total++;
+  if (!((std::isnan(r0) && std::isnan(r2)) || idfx::dbits(r0) == idfx::dbits(r2))) {
+    if (mism < 10)
+      std::printf("mismatch a=%a b=%a ieee=%a rcp=%a\n", a, b, r0, r2);
     mism++;
   }
 }
