@@ -36,8 +36,8 @@ BYTES_PER_ZONE_CYCLE = 320.0  # 8 FP64 state values x 5 transfers per RK2 cycle
 # active cell of one sweep launch: ncu on the 128^3 case of this workload
 # (stage 0; profiles/sweep_fp64_hlld_plm_turb3d_128.md).  Both scale with the
 # cells processed; at 256^3 the CT-extension columns add 1.6 % instead of 3.1 %.
-FP64_INST_PER_CELL = {"sweep_x": 640.0, "sweep_y": 638.0, "sweep_z": 633.0}
-DRAM_BYTES_PER_CELL = {"sweep_x": 193.1, "sweep_y": 173.2, "sweep_z": 171.6}
+FP64_INST_PER_CELL = {"sweep_x": 608.0, "sweep_y": 606.5, "sweep_z": 601.5}
+DRAM_BYTES_PER_CELL = {"sweep_x": 193.3, "sweep_y": 172.6, "sweep_z": 171.5}
 
 
 def parse():

@@ -419,7 +419,12 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   g.gamma = cfg->gamma;
   g.gm1 = cfg->gamma - 1.0;
   g.rgm1 = 1.0 / g.gm1;  // correctly rounded reciprocals (Markstein quotients)
-  for (int d = 0; d < 3; d++) g.rdx[d] = 1.0 / g.dx[d];
+  for (int d = 0; d < 3; d++) {
+    g.rdx[d] = 1.0 / g.dx[d];
+    const double e = 0.1 * g.dx[d];  // LimO3's r dx, squared as the limiter does
+    g.l3b[d] = e * e;
+    g.l3y[d] = 1.0 / g.l3b[d];
+  }
   g.ext = 1;  // hlldMHD.hpp:30-49: uct_hll(d) with HLLD/HLL needs nghost cells
   if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
   g.shock_smoothing = cfg->shock_smoothing;

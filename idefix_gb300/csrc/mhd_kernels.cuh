@@ -44,6 +44,7 @@ struct Geo {
   double shock_smoothing;  // [Hydro] shockFlattening value (flags in Fields::shock)
   double rgm1;    // RN(1 / gm1), for the FP64 Riemann solvers
   double rdx[3];  // RN(1 / dx[d]), for the InvDt quotient
+  double l3b[3], l3y[3];  // LimO3: (0.1 dx[d])^2 and RN(1 / that)
   int bc[3][2];  // boundary type per direction and side (IDFX_BC_*: 0 periodic)
   int nonper;    // some direction is not periodic: ghosts filled by k_bc_* first
 };
@@ -497,7 +498,7 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
   if (g.emf == kEmfUctHll) {
     const T ar = fmax(T(0), sr);
     const T al = fmin(T(0), sl);
-    const T scrh = dv(T(1), ar - al);
+    const T scrh = rcp(ar - al);
     Et[c] = -st * (ar * vL[d::Xt] - al * vR[d::Xt]) * scrh;
     if constexpr (D == 3) Eb[c] = -sb * (ar * vL[d::Xb] - al * vR[d::Xb]) * scrh;
     aL[c] = ar * scrh;
@@ -516,7 +517,7 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
   const T Bn = dv(sr * vR[d::BXn] - sl * vL[d::BXn], sr - sl);
   const T duL = sl - vL[d::Xn];
   const T duR = sr - vR[d::Xn];
-  T scrh = dv(T(1), duR * uR[vv::RHO] - duL * uL[vv::RHO]);
+  T scrh = rcp(duR * uR[vv::RHO] - duL * uL[vv::RHO]);
   const T Sc = (duR * uR[d::Xn] - duL * uL[d::Xn] - ptR + ptL) * scrh;
   const T usLRHO = dv(uL[vv::RHO] * duL, sl - Sc);
   const T usRRHO = dv(uR[vv::RHO] * duR, sr - Sc);
@@ -545,7 +546,7 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
   }
   const T ar = fmax(T(0), sr);
   const T al = fmin(T(0), sl);
-  scrh = dv(T(1), ar - al);
+  scrh = rcp(ar - al);
   if (revert_to_hll) {
     a_l = ar * scrh;
     a_r = -al * scrh;
@@ -615,6 +616,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
   const long long f0 = fidx(g, idx[2], idx[1], idx[0]);
   const double* vs = f.Vs + DIR * g.nface;
   const T dxd = (T)g.dx[DIR];
+  const Recip l3{g.l3b[DIR], g.l3y[DIR]};
   const T gam = (T)g.gamma;
   T w[NV][W];
   T vrp[NV];            // right-face state of the previous cell
@@ -693,7 +695,7 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
         vl[n] = (T)f.ls[((long long)DIR * 16 + n) * g.ncell + cc];
         vr[n] = (T)f.ls[((long long)DIR * 16 + 8 + n) * g.ncell + cc];
       } else {
-        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk);
+        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk, l3);
       }
     }
     if (c >= m0) {
@@ -812,6 +814,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
   const int base = beg - 1;  // first cell reconstructed (left state of face beg)
   const T gam = (T)g.gamma;
   const T dxd = (T)g.dx[0];
+  const Recip l3{g.l3b[0], g.l3y[0]};
   const T dtdVT = (T)ctl->dtdV;
   const T areaT = (T)g.A[0];
   const T invdxT = T(1) / (T)g.dx[0];
@@ -853,7 +856,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
           w[H + m] = lane_from(cur[n], nxt[n], src, src > 31);
         }
       }
-      Recon<ORDER>::cell(w, dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk);
+      Recon<ORDER>::cell(w, dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk, l3);
     }
     // face on the left of cell i: left state = right state of cell i-1
     T vL[NV], vR[NV];

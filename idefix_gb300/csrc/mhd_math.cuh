@@ -49,6 +49,17 @@ __device__ __forceinline__ T dv(T a, T b) {
   return a / b;
 }
 
+// 1 / b: the correctly rounded reciprocal (FP64: __drcp_rn, one instruction
+// sequence shorter than a general division), equal to 1 / b
+template <typename T>
+__device__ __forceinline__ T rcp(T b) {
+  if constexpr (sizeof(T) == 8) {
+    return rcp_rn(b);
+  } else {
+    return T(1) / b;
+  }
+}
+
 // the same quotient computed on the integer pipe for FP64 (intdiv.cuh): used
 // by the memory-bound whole-array kernels (cons <-> prim), where it takes the
 // division off the FP64 pipe; the sweeps keep the hardware sequence, whose
@@ -191,18 +202,31 @@ __device__ __forceinline__ T lim_mc(T dvp, T dvm) {  // :68-76
   return dq;
 }
 
+// e2: (r dx)^2 and its correctly rounded reciprocal, formed on the host; the
+// FP64 path divides by it and by 3 with Markstein's correction (rdiv.cuh),
+// bit-identical to the divisions
 template <typename T>
-__device__ __forceinline__ T lim_limo3(T dvp, T dvm, T dx) {  // :25-52
+__device__ __forceinline__ T lim_limo3(T dvp, T dvm, T dx, const Recip& e2) {  // :25-52
   const T r = T(0.1), eps = T(1.e-12);
   T th = dv(dvm, dvp + T(1.e-16));
-  T q = dv(T(2) + th, T(3));
+  T q;
+  if constexpr (sizeof(T) == 8) {
+    q = div_r(T(2) + th, Recip{3.0, 1.0 / 3.0});
+  } else {
+    q = dv(T(2) + th, T(3));
+  }
   T a = fmin(T(1.5), T(2) * th);
   a = fmin(q, a);
   T b = fmax(T(-0.5) * th, a);
   T c = fmin(q, b);
   T psi = fmax(T(0), c);
   T eta = r * dx;
-  eta = dv(dvm * dvm + dvp * dvp, eta * eta);
+  if constexpr (sizeof(T) == 8) {
+    eta = div_r(dvm * dvm + dvp * dvp, e2);
+  } else {
+    (void)e2;
+    eta = dv(dvm * dvm + dvp * dvp, eta * eta);
+  }
   T lim;
   if (eta <= T(1) - eps) {
     lim = q;
@@ -232,7 +256,13 @@ __device__ __forceinline__ void ppm_limit_face(T vm1, T v0, T vp1, T vp2, T& vph
       delta = C * fmin(fabs(deltaL), fabs(deltaR));
       delta = sgn(deltaC) * fmin(delta, fabs(deltaC));
     }
-    vph = T(0.5) * (v0 + vp1) - dv(delta, T(6));
+    T d6;
+    if constexpr (sizeof(T) == 8) {
+      d6 = div_r(delta, Recip{6.0, 1.0 / 6.0});
+    } else {
+      d6 = dv(delta, T(6));
+    }
+    vph = T(0.5) * (v0 + vp1) - d6;
   }
 }
 
@@ -285,7 +315,9 @@ struct Recon {
   // shock: the cell is flagged by shock flattening (minmod slope, PLM and
   // LimO3 only, extrapolateToFaces.hpp:96-218)
   template <typename T>
-  __device__ __forceinline__ static void cell(const T* w, T dx, bool pos, T& vl, T& vr, bool shock = false) {
+  // e2: (0.1 dx)^2 and its reciprocal (LimO3, FP64 path; Geo::l3b, l3y)
+  __device__ __forceinline__ static void cell(const T* w, T dx, bool pos, T& vl, T& vr, bool shock = false,
+                                              const Recip& e2 = Recip{0.0, 0.0}) {
     if constexpr (ORDER == 1) {
       vl = w[0];
       vr = w[0];
@@ -298,13 +330,13 @@ struct Recon {
     } else if constexpr (ORDER == 3) {
       const T dm = w[1] - w[0];
       const T dp = w[2] - w[1];
-      T d = shock ? lim_minmod(dp, dm) : dp * lim_limo3(dp, dm, dx);
+      T d = shock ? lim_minmod(dp, dm) : dp * lim_limo3(dp, dm, dx, e2);
       vr = w[1] + T(0.5) * d;
       if (pos && vr <= T(0)) {
         d = lim_minmod(dp, dm);
         vr = w[1] + T(0.5) * d;
       }
-      d = shock ? lim_minmod(dp, dm) : dm * lim_limo3(dm, dp, dx);
+      d = shock ? lim_minmod(dp, dm) : dm * lim_limo3(dm, dp, dx, e2);
       vl = w[1] - T(0.5) * d;
       if (pos && vl <= T(0)) {
         d = lim_minmod(dp, dm);
@@ -425,12 +457,12 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   T scrh, scrhL, scrhR;
   T vsL = T(0), vsR = T(0), wsL = T(0), wsR = T(0);
   int revert_to_hllc = 0;
-  scrh = dv(T(1), sr - sl);
+  scrh = rcp(sr - sl);
   const T Bx = (sr * vR[BXn] - sl * vL[BXn]) * scrh;
   const T sBx = (Bx > T(0) ? T(1) : T(-1));
   const T duL = sl - vL[Xn];
   const T duR = sr - vR[Xn];
-  scrh = dv(T(1), duR * uR[RHO] - duL * uL[RHO]);
+  scrh = rcp(duR * uR[RHO] - duL * uL[RHO]);
   const T SM = (duR * uR[Xn] - duL * uL[Xn] - ptR + ptL) * scrh;
   T pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR + vL[RHO] * vR[RHO] * duR * duL * (vR[Xn] - vL[Xn]);
   pts *= scrh;
@@ -445,7 +477,7 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   if ((S1L - sl) < T(1.e-4) * (SM - sl)) revert_to_hllc = 1;
   if ((S1R - sr) > T(-1.e-4) * (sr - SM)) revert_to_hllc = 1;
   if (revert_to_hllc) {
-    scrh = dv(T(1), sr - sl);
+    scrh = rcp(sr - sl);
     T Uhll[NV];
 #pragma unroll
     for (int n = 0; n < NV; n++) {
@@ -612,10 +644,10 @@ __device__ __forceinline__ void riemann_hll(T gamma, T rgm1, const T* vL, const 
 #pragma unroll
     for (int n = v::BX1; n < v::BX1 + D; n++) {
       F[n] = sl * sr * uR[n] - sl * sr * uL[n] + sr * fluxL[n] - sl * fluxR[n];
-      F[n] *= dv(T(1), sr - sl);
+      F[n] *= rcp(sr - sl);
     }
     F[v::ENG] = sl * sr * uR[v::ENG] - sl * sr * uL[v::ENG] + sr * fluxL[v::ENG] - sl * fluxR[v::ENG];
-    F[v::ENG] *= dv(T(1), sr - sl);
+    F[v::ENG] *= rcp(sr - sl);
   }
 }
 
@@ -744,7 +776,7 @@ __device__ __forceinline__ void riemann_roe(T gamma, T rgm1, const T* vL, const 
     alpha_f = T(1);
     alpha_s = T(0);
   } else {
-    scrh = dv(T(1), cf2 - cs2);
+    scrh = rcp(cf2 - cs2);
     alpha_f = (a2 - cs2) * scrh;
     alpha_s = (cf2 - a2) * scrh;
     alpha_f = fmax(T(0), alpha_f);

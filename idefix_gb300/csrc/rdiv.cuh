@@ -49,13 +49,17 @@ IDFX_HD double fma_rn(double a, double b, double c) {
 
 // a / R.b, correctly rounded
 IDFX_HD double div_r(double a, const Recip& R) {
-  const uint32_t ea = (uint32_t)(dbits(a) >> 52) & 0x7ffu;
-  const uint32_t eb = (uint32_t)(dbits(R.b) >> 52) & 0x7ffu;
-  // |a|, |b| and |a / b| within 2^-959 .. 2^959 (biased exponents 64..1983)
-  if (ea - 64u < 1920u && eb - 64u < 1920u && (ea + 1023u - eb) - 64u < 1920u) {
-    const double q = a * R.y;
-    const double r = fma_rn(-q, R.b, a);
-    return fma_rn(r, R.y, q);
+  const uint64_t A = dbits(a), B = dbits(R.b);
+  const uint32_t ea = (uint32_t)(A >> 52) & 0x7ffu;
+  const uint32_t eb = (uint32_t)(B >> 52) & 0x7ffu;
+  if (eb - 64u < 1920u) {
+    // |a|, |b| and |a / b| within 2^-959 .. 2^959 (biased exponents 64..1983)
+    if (ea - 64u < 1920u && (ea + 1023u - eb) - 64u < 1920u) {
+      const double q = a * R.y;
+      const double r = fma_rn(-q, R.b, a);
+      return fma_rn(r, R.y, q);
+    }
+    if ((A << 1) == 0ull) return dfrom((A ^ B) & (1ull << 63));  // +-0 / b
   }
   return a / R.b;
 }
