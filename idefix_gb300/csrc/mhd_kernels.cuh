@@ -836,8 +836,27 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
   for (int n = 0; n < v::BX1; n++) cFA[n] = T(0);
   const int nchunks = (end - base + 1 + 31) / 32;  // cells base .. end
   double run_max = 0.0;
+  // conserved state (and InvDt) of the cell this lane updates in a chunk,
+  // loaded one chunk ahead: the update is the chunk's last step and its
+  // loads would otherwise wait on memory right at the point of use
+  auto upd = [&](int kk) { return base + 32 * kk + lane - 1; };  // cell updated in chunk kk
+  auto upd_ok = [&](int kk) { const int u = upd(kk); return active_col && u >= beg && u < end; };
+  double nU[v::BX1], nI = 0.0;
+  if (upd_ok(0)) {
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) nU[n] = f.Uc[n * g.ncell + row + upd(0)];
+    if (invdt == 2) nI = f.InvDt[row + upd(0)];
+  }
   for (int k = 0; k < nchunks; k++) {
     const int i = base + 32 * k + lane;  // this lane's cell
+    double cU[v::BX1], cI = nI;
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) cU[n] = nU[n];
+    if (upd_ok(k + 1)) {
+#pragma unroll
+      for (int n = 0; n < v::BX1; n++) nU[n] = f.Uc[n * g.ncell + row + upd(k + 1)];
+      if (invdt == 2) nI = f.InvDt[row + upd(k + 1)];
+    }
     // reconstruction of cell i from the lanes around it
     T vl[NV], vr[NV];
     const bool shk = f.shock && i >= 0 && i < nx && f.shock[row + i];
@@ -898,10 +917,10 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
 #pragma unroll
       for (int n = 0; n < v::BX1; n++) {
         const T rhs = -dtdVT * (FA[n] - FAp[n]);
-        f.Uc[n * g.ncell + cu] = f.Uc[n * g.ncell + cu] + to_f64(rhs);
+        f.Uc[n * g.ncell + cu] = cU[n] + to_f64(rhs);
       }
       if (invdt) {
-        const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
+        const double prev = (invdt == 1) ? 0.0 : cI;
         double inv;
         if constexpr (sizeof(T) == 8) {
           inv = prev + div_r(0.5 * (cm + cp), Recip{g.dx[0], g.rdx[0]});
@@ -929,7 +948,7 @@ __device__ __forceinline__ void d_sweep_xwarp(const Geo& g, const Fields& f, con
 }
 
 template <int D, int ORDER, int SOLVER, typename T>
-__global__ void __launch_bounds__(32 * kXW) k_sweep_xwarp(Geo g, Fields f, const Ctl* ctl, int invdt, int last_dir) {
+__global__ void __launch_bounds__(32 * kXW, 5) k_sweep_xwarp(Geo g, Fields f, const Ctl* ctl, int invdt, int last_dir) {
   d_sweep_xwarp<D, ORDER, SOLVER, T>(g, f, ctl, invdt, last_dir, blockIdx);
 }
 
