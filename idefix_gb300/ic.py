@@ -128,6 +128,54 @@ def shock_tube_domain(nx=800, ny=4):
 ROTOR_DOMAIN = ((-0.5, -0.5, 0.0), (0.5, 0.5, 1.0))  # (xbeg, xend) of rotor_2d
 
 
+FIELD_LOOP_DOMAIN = ((-1.0, -1.0, -1.0), (1.0, 1.0, 1.0))  # (xbeg, xend) of field_loop_3d
+
+
+def field_loop_3d(nx=128, ny=2, nz=128, nghost=2):
+    """Advection of a weak field loop (test/MHD/FieldLoop/setup.cpp:17-56,
+    idefix.ini: [-1,1]^3, HLLD, CFL 0.2, t_stop 2, periodic): rho = p = 1,
+    v = (1, 0, 1), and the face field of the vector potential
+    A_y = A0 (R0 - r) for r = sqrt(x^2 + z^2) <= R0 (A0 = 1e-3, R0 = 0.3),
+    evaluated at the cell centres of every cell index, through
+    DataBlockHost::MakeVsFromAmag's Cartesian differences
+    (dataBlockHost.cpp: Bx = -(A_y(k+1) - A_y(k)) / dz, Bz = (A_y(i+1) -
+    A_y(i)) / dx, By = 0), so the discrete div B vanishes.  The reference
+    runs it with one cell in y; here the y extent holds ny cells of the same
+    state (uniform in y)."""
+    dims = 3
+    n = (nx, ny, nz)
+    nvar, nt, ntv = grid_shapes(dims, n, nghost)
+    xb, xe = FIELD_LOOP_DOMAIN
+    xc, _ = _coords(dims, n, nghost, xb, xe)
+    dx = [(xe[d] - xb[d]) / n[d] for d in range(3)]
+    A0, R0 = 1.0e-3, 0.3
+    x = xc[0][None, :]
+    z = xc[2][:, None]
+    r = np.sqrt(x * x + z * z)
+    Ay2 = A0 * (R0 - r) * (r <= R0)                     # [nt2][nt0], the same for every j
+    Vc = np.zeros((nvar, nt[2], nt[1], nt[0]))
+    Vs = np.zeros((dims, ntv[2], ntv[1], ntv[0]))
+    Vc[0] = 1.0
+    Vc[1] = 1.0
+    Vc[3] = 1.0
+    Vc[4] = 1.0
+    g = nghost
+    # active faces (and the extra right one in every direction), as the
+    # reference's loop over [beg, end + 1)
+    ks, js, is_ = slice(g, g + nz + 1), slice(g, g + ny + 1), slice(g, g + nx + 1)
+    k = np.arange(g, g + nz + 1)
+    i = np.arange(g, g + nx + 1)
+    kk = np.minimum(k + 1, nt[2] - 1)
+    ii = np.minimum(i + 1, nt[0] - 1)
+    dAz = Ay2[kk][:, i] - Ay2[k][:, i]                  # A_y(k+1) - A_y(k)
+    dAx = Ay2[k][:, ii] - Ay2[k][:, i]                  # A_y(i+1) - A_y(i)
+    bx = (0.0 + 1.0 / dx[1] * 0.0) - 1.0 / dx[2] * dAz
+    bz = 1.0 / dx[0] * dAx - 1.0 / dx[1] * 0.0
+    Vs[0, ks, js, is_] = bx[:, None, :]
+    Vs[2, ks, js, is_] = bz[:, None, :]
+    return Vc, Vs
+
+
 def orszag_tang_like_2d(n, mach=1.0, beta=10.0 / 3.0, nghost=2, gamma=5.0 / 3.0):
     """Orszag-Tang vortex with a chosen sonic Mach number and plasma beta.
 

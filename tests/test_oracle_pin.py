@@ -253,3 +253,18 @@ def test_oracle_matches_reference_on_boundary_problems(oracle_lib, reference_lib
     assert port[0] == ref[0] == 0
     assert _same(port[1], ref[1])
     assert port[2] == ref[2]
+
+
+def test_oracle_matches_reference_on_field_loop(oracle_lib, reference_libs):
+    # test/MHD/FieldLoop (HLLD, CFL 0.2, periodic; face field from a vector
+    # potential), y-uniform with two cells
+    n = (24, 2, 24)
+    state = extract(3, n, 2, *ic.field_loop_3d(*n))
+    xb, xe = ic.FIELD_LOOP_DOMAIN
+    P.LIB_REF = os.path.join(reference_libs, "libofx_ref_d3_o2.so")
+    scheme = dict(cfl=0.2, xbeg=xb, xend=xe)
+    port = _run("port", 3, n, state, 25, **scheme)
+    ref = _run("ref", 3, n, state, 25, **scheme)
+    assert port[0] == ref[0] == 0
+    assert _same(port[1], ref[1])
+    assert port[2] == ref[2]
