@@ -521,8 +521,8 @@ __device__ __forceinline__ void store_emf(const Geo& g, const Fields& f, long lo
   const T Sc = (duR * uR[d::Xn] - duL * uL[d::Xn] - ptR + ptL) * scrh;
   const T usLRHO = dv(uL[vv::RHO] * duL, sl - Sc);
   const T usRRHO = dv(uR[vv::RHO] * duR, sr - Sc);
-  const T sqrL = sqrt(usLRHO);
-  const T sqrR = sqrt(usRRHO);
+  const T sqrL = sqr(usLRHO);
+  const T sqrR = sqr(usRRHO);
   const T SaL = Sc - dv(fabs(Bn), sqrL);
   const T SaR = Sc + dv(fabs(Bn), sqrR);
   if ((SaL - sl) < T(1e-4) * (Sc - sl)) revert_to_hll = 1;

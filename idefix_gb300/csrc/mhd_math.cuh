@@ -43,20 +43,38 @@ struct Dir {
 constexpr double kSmallPressureFix = 1.0e-5;  // fluid_defs.hpp:23
 constexpr double kEpsUctContact = 1.0e-6;     // fluid_defs.hpp:24
 
-// division: IEEE correctly rounded in both precisions
+// division: FP64 IEEE correctly rounded (the bit-identical path); FP32 (the
+// mixed path, whose arithmetic is FP32-accurate, not bit-matched) the fast
+// reciprocal-multiply form, within 2 ulp for divisors below 2^126 in
+// magnitude - far beyond any state or wave speed of these flows
 template <typename T>
 __device__ __forceinline__ T dv(T a, T b) {
-  return a / b;
+  if constexpr (sizeof(T) == 4) {
+    return __fdividef(a, b);
+  } else {
+    return a / b;
+  }
 }
 
-// 1 / b: the correctly rounded reciprocal (FP64: __drcp_rn, one instruction
-// sequence shorter than a general division), equal to 1 / b
+// square root: FP64 IEEE (the bit-identical path); FP32 x * rsqrt(x), within
+// 2 ulp (the tiny offset keeps sqr(0) = 0; negative arguments stay NaN)
+template <typename T>
+__device__ __forceinline__ T sqr(T x) {
+  if constexpr (sizeof(T) == 4) {
+    return x * rsqrtf(x + 1.2e-38f);
+  } else {
+    return sqrt(x);
+  }
+}
+
+// 1 / b: FP64 the correctly rounded reciprocal (__drcp_rn, one instruction
+// sequence shorter than a general division, equal to 1 / b); FP32 as dv
 template <typename T>
 __device__ __forceinline__ T rcp(T b) {
   if constexpr (sizeof(T) == 8) {
     return rcp_rn(b);
   } else {
-    return T(1) / b;
+    return __fdividef(T(1), b);
   }
 }
 
@@ -402,8 +420,8 @@ __device__ __forceinline__ T fast_speed(T gamma, const T* v) {
   const T Btmag2 = b2 * b2 + b3 * b3;
   const T Bmag2 = b1 * b1 + Btmag2;
   T c = gpr - Bmag2;
-  c = gpr + Bmag2 + sqrt(c * c + T(4) * gpr * Btmag2);
-  c = sqrt(dv(T(0.5) * c, v[vv::RHO]));
+  c = gpr + Bmag2 + sqr(c * c + T(4) * gpr * Btmag2);
+  c = sqr(dv(T(0.5) * c, v[vv::RHO]));
   return c;
 }
 
@@ -470,8 +488,8 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   const Recip RsL = shared_recip(sl - SM), RsR = shared_recip(sr - SM);
   usL[RHO] = shared_div(uL[RHO] * duL, sl - SM, RsL);
   usR[RHO] = shared_div(uR[RHO] * duR, sr - SM, RsR);
-  const T sqrL = sqrt(usL[RHO]);
-  const T sqrR = sqrt(usR[RHO]);
+  const T sqrL = sqr(usL[RHO]);
+  const T sqrR = sqr(usR[RHO]);
   T S1L = SM - dv(fabs(Bx), sqrL);
   T S1R = SM + dv(fabs(Bx), sqrR);
   if ((S1L - sl) < T(1.e-4) * (SM - sl)) revert_to_hllc = 1;
@@ -665,8 +683,8 @@ __device__ __forceinline__ void riemann_tvdlf(T gamma, T rgm1, const T* vL, cons
   if constexpr (D == 3) Bt2 = Bt2 + vv[d::BXb] * vv[d::BXb];
   const T B2 = Bt2 + vv[d::BXn] * vv[d::BXn];
   T cRL = gpr - B2;
-  cRL = cRL + B2 + sqrt(cRL * cRL + T(4) * gpr * Bt2);
-  cRL = sqrt(dv(T(0.5) * cRL, vv[v::RHO]));
+  cRL = cRL + B2 + sqr(cRL * cRL + T(4) * gpr * Bt2);
+  cRL = sqr(dv(T(0.5) * cRL, vv[v::RHO]));
   const T cmax = fmax(fabs(vv[d::Xn] + cRL), fabs(vv[d::Xn] - cRL));
   r.sl = -cmax;
   r.sr = cmax;
@@ -709,12 +727,12 @@ __device__ __forceinline__ void riemann_roe(T gamma, T rgm1, const T* vL, const 
   for (int a = 0; a < NV; a++)
 #pragma unroll
     for (int b = 0; b < NV; b++) Rc[a][b] = T(0);
-  const T sqr_rho_L = sqrt(vL[RHO]);
-  const T sqr_rho_R = sqrt(vR[RHO]);
+  const T sqr_rho_L = sqr(vL[RHO]);
+  const T sqr_rho_R = sqr(vR[RHO]);
   const T sl = dv(sqr_rho_L, sqr_rho_L + sqr_rho_R);
   const T sr = dv(sqr_rho_R, sqr_rho_L + sqr_rho_R);
   const T rho = sr * vL[RHO] + sl * vR[RHO];
-  const T sqrt_rho = sqrt(rho);
+  const T sqrt_rho = sqr(rho);
   T w = T(0), Bz = T(0), bz = T(0);
   const T u = sl * vL[Xn] + sr * vR[Xn];
   const T vv = sl * vL[Xt] + sr * vR[Xt];
@@ -729,7 +747,7 @@ __device__ __forceinline__ void riemann_roe(T gamma, T rgm1, const T* vL, const 
   T bt2 = T(0) + by * by;
   if constexpr (D == 3) bt2 = bt2 + bz * bz;
   const T b2 = bx * bx + bt2;
-  const T Btmag = sqrt(bt2 * rho);
+  const T Btmag = sqr(bt2 * rho);
   T X = dV[BXn] * dV[BXn] + dV[BXt] * dV[BXt];
   if constexpr (D == 3) X = X + dV[BXb] * dV[BXb];
   X = dv(X, (sqr_rho_L + sqr_rho_R) * (sqr_rho_L + sqr_rho_R) * T(2));
@@ -758,13 +776,13 @@ __device__ __forceinline__ void riemann_roe(T gamma, T rgm1, const T* vL, const 
   T scrh = a2 - b2;
   const T ca2 = bx * bx;
   scrh = scrh * scrh + T(4) * bt2 * a2;
-  scrh = sqrt(scrh);
+  scrh = sqr(scrh);
   const T cf2 = T(0.5) * (a2 + b2 + scrh);
   const T cs2 = dv(a2 * ca2, cf2);
-  const T cf = sqrt(cf2);
-  const T cs = sqrt(cs2);
-  const T ca = sqrt(ca2);
-  const T a = sqrt(a2);
+  const T cf = sqr(cf2);
+  const T cs = sqr(cs2);
+  const T ca = sqr(ca2);
+  const T a = sqr(a2);
   T alpha_f, alpha_s;
   if (cf == cs) {
     alpha_f = T(1);
@@ -781,8 +799,8 @@ __device__ __forceinline__ void riemann_roe(T gamma, T rgm1, const T* vL, const 
     alpha_s = (cf2 - a2) * scrh;
     alpha_f = fmax(T(0), alpha_f);
     alpha_s = fmax(T(0), alpha_s);
-    alpha_f = sqrt(alpha_f);
-    alpha_s = sqrt(alpha_s);
+    alpha_f = sqr(alpha_f);
+    alpha_s = sqr(alpha_s);
   }
   T beta_y, beta_z = T(0);
   if constexpr (D == 2) {
