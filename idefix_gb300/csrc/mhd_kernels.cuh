@@ -952,6 +952,244 @@ __global__ void __launch_bounds__(32 * kXW, 5) k_sweep_xwarp(Geo g, Fields f, co
   d_sweep_xwarp<D, ORDER, SOLVER, T>(g, f, ctl, invdt, last_dir, blockIdx);
 }
 
+// ---------------------------------------------------------------------------
+// x sweep by warp chunks with bulk-copy staging (FP32 path).  The same
+// arithmetic as d_sweep_xwarp, lane for lane; only the data movement
+// differs: each warp keeps a ring of kXB chunk slots in shared memory and
+// its lane 0 fetches whole chunks - the 32 FP32 primitives of every
+// variable and the 32 FP64 conserved values of every hydro variable, each a
+// contiguous row piece - with the bulk-copy engine (cp.async.bulk, tracked
+// by one mbarrier per slot), kXB - 2 chunks ahead of the stencil.  Lanes read
+// their stencil and their conserved state straight from the ring (no
+// register window, no shuffles for the stencil).  Needs 16-byte aligned rows
+// and arrays (nt0 a multiple of 4); the host falls back to d_sweep_xwarp
+// otherwise.  Every wait is bounded: on a timeout the kernel records a CUDA
+// error status, stops the cycle, waits (bounded) for its copies in flight
+// and returns.
+// ---------------------------------------------------------------------------
+constexpr int kXB = 4;                                        // ring slots per warp
+// shared memory per warp: FP32 primitives (nv), FP64 hydro state (nu),
+// mbarriers; a multiple of 128 bytes so that every warp's ring (the bulk
+// copies' destinations) stays 16-byte aligned
+__host__ __device__ constexpr int xb_warp_bytes(int nv, int nu) {
+  return (kXB * 32 * (nv * 4 + nu * 8) + kXB * 8 + 127) / 128 * 128;
+}
+static_assert(xb_warp_bytes(6, 4) % 128 == 0 && xb_warp_bytes(8, 5) % 128 == 0, "ring alignment");
+static_assert((32 * 4) % 16 == 0 && (32 * 8) % 16 == 0, "slot alignment");
+constexpr long long kXBSpin = 1ll << 22;                      // try_wait attempts before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  uint64_t gsrc;
+  asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(gsrc) : "l"(src));
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_done(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (long long it = 0; it < kXBSpin; it++)
+    if (mbar_done(bar, parity)) return true;
+  return false;
+}
+
+template <int D, int ORDER, int SOLVER, typename T>
+__device__ __forceinline__ void d_sweep_xbulk(const Geo& g, const Fields& f, const Ctl* ctl, int invdt, int last_dir,
+                                              dim3 bid, unsigned char* smem) {
+  if (ctl->done) return;
+  static_assert(sizeof(T) == 4, "bulk-staged x sweep: FP32 path");
+  using v = Var<D>;
+  using dd = Dir<D, 0>;
+  constexpr int NV = v::NV;
+  constexpr int NU = v::BX1;  // hydro variables updated by the sweep
+  constexpr int H = Recon<ORDER>::H;
+  constexpr int RING = 32 * kXB;
+  static_assert(ORDER >= 1 && ORDER <= 4, "bulk-staged x sweep: reconstruction orders 1-4");
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int nA = g.n[1] + 2 * g.ext;
+  const int nB = (D == 3) ? g.n[2] + 2 * g.ext : 1;
+  const long long col = (long long)bid.x * kXW + w;
+  if (col >= (long long)nA * nB) return;  // whole warp
+  // this warp's ring: float vr[NV][RING], double ur[NU][RING], mbarriers[kXB]
+  unsigned char* base_w = smem + (size_t)w * xb_warp_bytes(NV, NU);
+  double* ur = reinterpret_cast<double*>(base_w);
+  float* vr = reinterpret_cast<float*>(base_w + (size_t)NU * RING * 8);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base_w + (size_t)NU * RING * 8 + (size_t)NV * RING * 4);
+  const int ca = g.beg[1] - g.ext + (int)(col % nA);
+  const int cb = (D == 3) ? g.beg[2] - g.ext + (int)(col / nA) : 0;
+  bool active_col = (ca >= g.beg[1] && ca < g.end[1]);
+  if constexpr (D == 3) active_col = active_col && cb >= g.beg[2] && cb < g.end[2];
+  const long long row = cidx(g, cb, ca, 0);
+  const long long frow = fidx(g, cb, ca, 0);
+  const double* vs = f.Vs;
+  const float* vc = f.Vc32;
+  const int nx = g.nt[0];
+  const int beg = g.beg[0], end = g.end[0];
+  const T gam = (T)g.gamma;
+  const T dxd = (T)g.dx[0];
+  const Recip l3{g.l3b[0], g.l3y[0]};
+  const T dtdVT = (T)ctl->dtdV;
+  const T areaT = (T)g.A[0];
+  const T invdxT = T(1) / (T)g.dx[0];
+  const int nchunks = (end + 1 + 31) / 32;        // chunks of cells 0 .. end
+  const int last = min(nchunks, (nx - 1) / 32);    // last chunk with data the stencil may read
+  // lane 0 fetches chunk c into slot c % kXB
+  // bulk copies need 16-byte aligned addresses and sizes: with nt0 a
+  // multiple of 4 (so ncell and every row start are) and 16-byte aligned
+  // Vc32 and Uc, checked by the host before it launches this kernel, every
+  // chunk's source is; the ring's slots are by construction (xb_warp_bytes)
+  auto fetch = [&](int c) {
+    uint64_t* b = bar + (c % kXB);
+    const int ne = min(32, nx - 32 * c);          // a multiple of 4 (nt0 is)
+    const int s = (c % kXB) * 32;
+    mbar_expect(b, (uint32_t)ne * (NV * 4 + NU * 8));
+#pragma unroll
+    for (int n = 0; n < NV; n++)
+      bulk_to_smem(vr + (size_t)n * RING + s, vc + n * g.ncell + row + 32 * c, (uint32_t)ne * 4, b);
+#pragma unroll
+    for (int n = 0; n < NU; n++)
+      bulk_to_smem(ur + (size_t)n * RING + s, f.Uc + n * g.ncell + row + 32 * c, (uint32_t)ne * 8, b);
+  };
+  if (lane == 0) {
+    for (int s = 0; s < kXB; s++) mbar_init(bar + s);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int c = 0; c <= min(last, kXB - 1); c++) fetch(c);
+  }
+  __syncwarp();
+  int fetched = min(last, kXB - 1);  // chunks 0 .. fetched are issued
+  int waited = -1;                   // chunks 0 .. waited have landed
+  bool ok = true;
+  auto wait_upto = [&](int c) {
+    c = min(c, last);
+    while (ok && waited < c) {
+      const int q = waited + 1;
+      ok = mbar_wait(bar + (q % kXB), (uint32_t)((q / kXB) & 1));
+      if (ok) waited = q;
+    }
+  };
+  auto V = [&](int n, int i) -> T { return vr[(size_t)n * RING + ((i + RING) % RING)]; };
+  auto U = [&](int n, int i) -> double { return ur[(size_t)n * RING + ((i + RING) % RING)]; };
+  T cvr[NV];
+  T cFA[NU];
+  T ccp = T(0);
+#pragma unroll
+  for (int n = 0; n < NV; n++) cvr[n] = T(0);
+#pragma unroll
+  for (int n = 0; n < NU; n++) cFA[n] = T(0);
+  double run_max = 0.0;
+  for (int k = 0; k < nchunks; k++) {
+    wait_upto(k + 1);
+    ok = __all_sync(0xffffffffu, ok);  // the warp stops together
+    if (!ok) break;
+    const int i = 32 * k + lane;  // this lane's cell
+    T vl[NV], vrr[NV];
+    const bool shk = f.shock && i < nx && f.shock[row + i];
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      if (n == dd::BXn) continue;
+      T wv[2 * H + 1];
+#pragma unroll
+      for (int m = -H; m <= H; m++) wv[H + m] = (i + m >= 0 && i + m < nx) ? V(n, i + m) : T(0);
+      Recon<ORDER>::cell(wv, dxd, n == v::RHO || n == v::PRS, vl[n], vrr[n], shk, l3);
+    }
+    T vL[NV], vR[NV];
+#pragma unroll
+    for (int n = 0; n < NV; n++) {
+      if (n == dd::BXn) continue;
+      const T up = __shfl_up_sync(0xffffffffu, vrr[n], 1);
+      vL[n] = lane == 0 ? cvr[n] : up;
+      vR[n] = vl[n];
+    }
+    const bool face = (i >= beg && i <= end);
+    const long long cc = row + i;
+    T FA[NU];
+    T cm = T(0);
+#pragma unroll
+    for (int n = 0; n < NU; n++) FA[n] = T(0);
+    if (face) {
+      const T bn = from_f64<T>(vs[frow + i]);
+      vL[dd::BXn] = bn;
+      vR[dd::BXn] = bn;
+      RiemannOut<D, T> r;
+      riemann<D, 0, SOLVER>(gam, (T)g.rgm1, vL, vR, r);
+      store_emf<D, 0>(g, f, cc, r, vL, vR);
+#pragma unroll
+      for (int n = 0; n < NU; n++) FA[n] = r.F[n] * areaT;
+      cm = r.cmax;
+    }
+    T FAp[NU];
+#pragma unroll
+    for (int n = 0; n < NU; n++) {
+      const T up = __shfl_up_sync(0xffffffffu, FA[n], 1);
+      FAp[n] = lane == 0 ? cFA[n] : up;
+    }
+    const T cpu = __shfl_up_sync(0xffffffffu, cm, 1);
+    const T cp = lane == 0 ? ccp : cpu;
+    if (active_col && face && i - 1 >= beg) {
+      const long long cu = cc - 1;
+#pragma unroll
+      for (int n = 0; n < NU; n++) {
+        const T rhs = -dtdVT * (FA[n] - FAp[n]);
+        f.Uc[n * g.ncell + cu] = U(n, i - 1) + to_f64(rhs);
+      }
+      if (invdt) {
+        const double prev = (invdt == 1) ? 0.0 : f.InvDt[cu];
+        const double inv = prev + to_f64(T(0.5) * (cm + cp) * invdxT);
+        f.InvDt[cu] = inv;
+        if (inv > run_max) run_max = inv;
+      }
+    }
+#pragma unroll
+    for (int n = 0; n < NV; n++) cvr[n] = __shfl_sync(0xffffffffu, vrr[n], 31);
+#pragma unroll
+    for (int n = 0; n < NU; n++) cFA[n] = __shfl_sync(0xffffffffu, FA[n], 31);
+    ccp = __shfl_sync(0xffffffffu, cm, 31);
+    // chunk k-1 is no longer read: its slot takes chunk k-1+kXB
+    __syncwarp();
+    if (k >= 1 && k - 1 + kXB <= last) {
+      if (lane == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fetch(k - 1 + kXB);
+      }
+      fetched = k - 1 + kXB;
+    }
+  }
+  if (!ok) {  // a copy did not land: stop the cycle, drain what is in flight
+    if (lane == 0) {
+      ((Ctl*)ctl)->status = kErrCuda;
+      ((Ctl*)ctl)->done = 1;
+    }
+  }
+  // every issued copy lands before the warp's shared memory is released
+  for (int q = waited + 1; q <= fetched; q++) mbar_wait(bar + (q % kXB), (uint32_t)((q / kXB) & 1));
+  __syncwarp();
+  if (ok && last_dir && invdt && active_col)
+    atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, run_max);
+}
+
+template <int D, int ORDER, int SOLVER, typename T>
+__global__ void __launch_bounds__(32 * kXW) k_sweep_xbulk(Geo g, Fields f, const Ctl* ctl, int invdt, int last_dir) {
+  extern __shared__ __align__(16) unsigned char xb_smem[];
+  d_sweep_xbulk<D, ORDER, SOLVER, T>(g, f, ctl, invdt, last_dir, blockIdx, xb_smem);
+}
+
 template <int D, int DIR, int ORDER, int SOLVER, typename T>
 __global__ void __launch_bounds__(kTM) k_sweep_march(Geo g, Fields f, const Ctl* ctl, int invdt, int last_dir, int seg) {
   d_sweep_march<D, DIR, ORDER, SOLVER, T>(g, f, ctl, invdt, last_dir, seg, blockIdx);

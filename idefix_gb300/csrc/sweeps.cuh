@@ -15,9 +15,17 @@ void launch_dir(Engine& e, int invdt, int last) {
   const long long cols = (long long)(g.n[A] + 2 * g.ext) * (D == 3 ? g.n[B] + 2 * g.ext : 1);
   mark_begin(e, kKSweepX + DIR);
   if constexpr (DIR == 0 && sizeof(T) == 4 && ORDER <= 4) {
-    // FP32 x sweep: warp chunks along each row (coalesced)
-    k_sweep_xwarp<D, ORDER, SOLVER, T><<<(unsigned)((cols + kXW - 1) / kXW), 32 * kXW, 0, e.stream>>>(
-        g, e.f, e.ctl, invdt, last);
+    // FP32 x sweep: warp chunks along each row (coalesced); staged by bulk
+    // copies when rows and arrays are 16-byte aligned
+    const unsigned blocks = (unsigned)((cols + kXW - 1) / kXW);
+    const bool aligned = g.nt[0] % 4 == 0 && (reinterpret_cast<uintptr_t>(e.f.Vc32) & 15) == 0 &&
+                         (reinterpret_cast<uintptr_t>(e.f.Uc) & 15) == 0;
+    if (aligned && e.xbulk) {
+      const size_t smem = (size_t)kXW * xb_warp_bytes(Var<D>::NV, Var<D>::BX1);
+      k_sweep_xbulk<D, ORDER, SOLVER, T><<<blocks, 32 * kXW, smem, e.stream>>>(g, e.f, e.ctl, invdt, last);
+    } else {
+      k_sweep_xwarp<D, ORDER, SOLVER, T><<<blocks, 32 * kXW, 0, e.stream>>>(g, e.f, e.ctl, invdt, last);
+    }
   } else {
     dim3 grid((unsigned)((cols + kTM - 1) / kTM), nseg, 1);
     k_sweep_march<D, DIR, ORDER, SOLVER, T><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt, last, e.seg[DIR]);
