@@ -151,12 +151,13 @@ __global__ void k_set_stage_dt(Geo g, Ctl* ctl, double dt) {
   for (int d = 0; d < 3; d++) ctl->dtdx[d] = dt / g.dx[d];
 }
 
+template <typename E>
 __global__ void k_faces_combine(Geo g, Fields f, Ctl* ctl, double wc, double w0) {
   if (ctl->done) return;
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long tot = g.nface * g.D;
   if (tid >= tot) return;
-  f.Vs[tid] = wc * f.Vs[tid] + w0 * f.Vs0[tid];
+  f.Vs[tid] = rk_combine<E>(f.Vs[tid], f.Vs0[tid], wc, w0);  // as k_ct_faces combines
 }
 
 // ---------------------------------------------------------------------------
@@ -272,12 +273,17 @@ void queue_cycle(Engine& e, int use_tstop) {
     if (nan_check) {
       launch_ct(e, 0, 1.0, 0.0);
       launch_nan_check(e);
-      if (combine) k_faces_combine<<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
+      if (combine) {
+        if (e.precision == IDFX_MIXED)
+          k_faces_combine<float><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
+        else
+          k_faces_combine<double><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
+      }
     } else {
       launch_ct(e, combine, wc, w0);
     }
     mark_begin(e, kKStageEnd);
-    IDFX_DISPATCH_D(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0);
+    IDFX_DISPATCH_DE(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0);
     mark_end(e);
   }
   k_cycle_end<<<1, 1, 0, e.stream>>>(e.ctl);

@@ -63,11 +63,11 @@ __global__ void ke_ct_faces(const EnsBox* boxes, const int4* items, int combine,
   const int cmb = combine && !due(B.ctl, nan_period);
   d_ct_faces<D, E>(B.g, B.f, B.ctl, cmb, cmb ? wc : 1.0, cmb ? w0 : 0.0, dim3(it.y, it.z, it.w));
 }
-template <int D>
+template <int D, typename E>
 __global__ void ke_stage_end(const EnsBox* boxes, const int4* items, int combine, double wc, double w0) {
   const int4 it = items[blockIdx.x];
   const EnsBox& B = boxes[it.x];
-  d_stage_end<D>(B.g, B.f, B.ctl, combine, wc, w0, dim3(it.y, it.z, it.w));
+  d_stage_end<D, E>(B.g, B.f, B.ctl, combine, wc, w0, dim3(it.y, it.z, it.w));
 }
 template <int D>
 __global__ void ke_divb(const EnsBox* boxes, const int4* items, int period) {
@@ -84,6 +84,7 @@ __global__ void ke_nan_count(const EnsBox* boxes, const int4* items, int period)
   d_nan_count<D>(B.g, B.f, B.ctl, dim3(it.y, it.z, it.w));
 }
 // RK combination of the faces of the boxes that ran a NaN check this stage
+template <typename E>
 __global__ void ke_faces_combine(const EnsBox* boxes, const int4* items, double wc, double w0, int period) {
   const int4 it = items[blockIdx.x];
   const EnsBox& B = boxes[it.x];
@@ -91,7 +92,7 @@ __global__ void ke_faces_combine(const EnsBox* boxes, const int4* items, double 
   const long long tid = (long long)it.y * blockDim.x + threadIdx.x;  // fill-table layout
   if (tid >= B.g.nface) return;
   const long long q = (long long)it.z * B.g.nface + tid;
-  B.f.Vs[q] = wc * B.f.Vs[q] + w0 * B.f.Vs0[q];
+  B.f.Vs[q] = rk_combine<E>(B.f.Vs[q], B.f.Vs0[q], wc, w0);  // as d_ct_faces combines
 }
 // per-box control: one thread per box
 __global__ void ke_cycle_begin(const EnsBox* boxes, int nbox) {
@@ -246,9 +247,12 @@ void queue_cycle(EnsEngine& e, bool checks) {
       IDFX_ENS_D(ke_nan_count, e.edges.n, e.d_boxes, e.edges.items, np);
       ke_check_nan<<<per_box_blocks(e), kT, 0, e.stream>>>(e.d_boxes, e.nbox, np);
       if (combine && e.fill.n)
-        ke_faces_combine<<<e.fill.n, kT, 0, e.stream>>>(e.d_boxes, e.fill.items, wc, w0, np);
+        if (e.precision == IDFX_MIXED)
+          ke_faces_combine<float><<<e.fill.n, kT, 0, e.stream>>>(e.d_boxes, e.fill.items, wc, w0, np);
+        else
+          ke_faces_combine<double><<<e.fill.n, kT, 0, e.stream>>>(e.d_boxes, e.fill.items, wc, w0, np);
     }
-    IDFX_ENS_D(ke_stage_end, e.active.n, e.d_boxes, e.active.items, combine, wc, w0);
+    IDFX_ENS_DE(ke_stage_end, e.active.n, e.d_boxes, e.active.items, combine, wc, w0);
   }
   ke_cycle_end<<<per_box_blocks(e), kT, 0, e.stream>>>(e.d_boxes, e.nbox);
 }

@@ -1348,6 +1348,17 @@ __global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
 // then the Runge-Kutta combination of the faces (AddAndStore).  Only faces
 // that the next boundary pass does not overwrite are touched.
 // ---------------------------------------------------------------------------
+// Runge-Kutta combination wc u + w0 u0 (stateContainer AddAndStore).  The
+// FP64 path keeps the reference's expression; the mixed path (FP32 EMF
+// type) writes equal weights (RK2: 1/2, 1/2) as one product of the sum.
+template <typename E>
+__device__ __forceinline__ double rk_combine(double u, double u0, double wc, double w0) {
+  if constexpr (sizeof(E) == 4) {
+    if (wc == w0) return wc * (u + u0);
+  }
+  return wc * u + w0 * u0;
+}
+
 // E: type of the corner EMFs; they are widened exactly to FP64 and the curl
 // and the face update are FP64 on both paths (div B stays at FP64 round-off)
 template <int D, typename E = double>
@@ -1375,14 +1386,16 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
   // BX1s: faces i in [beg, end], j, k active
   if (in_j && in_k) {
     double rhs;
+    // (0.0 - x: the reference's expression; the mixed path negates)
+    const double z = (sizeof(E) == 4) ? -0.0 : 0.0;
     if constexpr (D == 2) {
-      rhs = 0.0 - dtdx2 * (Ex3(c + sj) - Ex3(c));
+      rhs = z - dtdx2 * (Ex3(c + sj) - Ex3(c));
     } else {
-      rhs = 0.0 - dtdx2 * (Ex3(c + sj) - Ex3(c)) + dtdx3 * (Ex2(c + sk) - Ex2(c));
+      rhs = z - dtdx2 * (Ex3(c + sj) - Ex3(c)) + dtdx3 * (Ex2(c + sk) - Ex2(c));
     }
     double* vs = f.Vs;
     double b = vs[fc] + rhs;
-    if (combine) b = wc * b + w0 * f.Vs0[fc];
+    if (combine) b = rk_combine<E>(b, f.Vs0[fc], wc, w0);
     vs[fc] = b;
   }
   if (in_i && in_k) {
@@ -1394,7 +1407,7 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
     }
     double* vs = f.Vs + g.nface;
     double b = vs[fc] + rhs;
-    if (combine) b = wc * b + w0 * f.Vs0[g.nface + fc];
+    if (combine) b = rk_combine<E>(b, f.Vs0[g.nface + fc], wc, w0);
     vs[fc] = b;
   }
   if constexpr (D == 3) {
@@ -1402,7 +1415,7 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
       const double rhs = -dtdx1 * (Ex2(c + si) - Ex2(c)) + dtdx2 * (Ex1(c + sj) - Ex1(c));
       double* vs = f.Vs + 2 * g.nface;
       double b = vs[fc] + rhs;
-      if (combine) b = wc * b + w0 * f.Vs0[2 * g.nface + fc];
+      if (combine) b = rk_combine<E>(b, f.Vs0[2 * g.nface + fc], wc, w0);
       vs[fc] = b;
     }
   }
@@ -1418,7 +1431,8 @@ __global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double 
 // cell-centred field from the faces (ReconstructVcField on Uc), and
 // ConvertConsToPrim.  Writes Uc and Vc.
 // ---------------------------------------------------------------------------
-template <int D>
+// E: EMF type of the path (FP32: mixed path, see rk_combine)
+template <int D, typename E = double>
 __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc, double w0, dim3 bid) {
   if (ctl->done) return;
   using v = Var<D>;
@@ -1437,7 +1451,7 @@ __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const
 #pragma unroll
   for (int n = 0; n < v::BX1; n++) {
     double u = f.Uc[n * g.ncell + c];
-    if (combine) u = wc * u + w0 * f.Uc0[n * g.ncell + c];
+    if (combine) u = rk_combine<E>(u, f.Uc0[n * g.ncell + c], wc, w0);
     U[n] = u;
   }
 #pragma unroll
@@ -1453,9 +1467,9 @@ __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const
   }
 }
 
-template <int D>
+template <int D, typename E = double>
 __global__ void k_stage_end(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
-  d_stage_end<D>(g, f, ctl, combine, wc, w0, blockIdx);
+  d_stage_end<D, E>(g, f, ctl, combine, wc, w0, blockIdx);
 }
 
 // ---------------------------------------------------------------------------
