@@ -695,7 +695,9 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
         vl[n] = (T)f.ls[((long long)DIR * 16 + n) * g.ncell + cc];
         vr[n] = (T)f.ls[((long long)DIR * 16 + 8 + n) * g.ncell + cc];
       } else {
-        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk, l3);
+        // FP64: odd variables' limiter quotient on the integer pipe
+        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk, l3,
+                           sizeof(T) == 8 && (n & 1));
       }
     }
     if (c >= m0) {
