@@ -1236,6 +1236,49 @@ __device__ __forceinline__ E riemann_edge(int order, const double* q, long long 
   return aL * vLv * bL + aR * vRv * bR;
 }
 
+// One upwind term of CalcContactAverage, (1 - w) a + w b with the weight w
+// in {0, 1/2, 1} (storeFlux.hpp:40-43).  The FP64 path forms the two
+// products exactly on the integer pipe - a product by 1 is the value, by 0 a
+// zero of the value's sign, by 1/2 an exponent decrement - and 1 - w from
+// w's bit pattern, so only the sum issues on the FP64 pipe; any other weight,
+// and non-finite or subnormal values, take the FP64 expression.  Every case
+// is bit-identical to the reference's expression.
+__device__ __forceinline__ double zero_times(double x) {  // (+0) x
+  const uint64_t u = dbits(x);
+  if (((u >> 52) & 0x7ffu) != 0x7ffu) return dfrom(u & (1ull << 63));
+  return 0.0 * x;
+}
+__device__ __forceinline__ double half_of(double x) {  // x / 2
+  const uint64_t u = dbits(x);
+  const uint32_t e = (uint32_t)(u >> 52) & 0x7ffu;
+  if (e - 2u < 2045u) return dfrom(u - (1ull << 52));
+  if ((u << 1) == 0ull) return x;
+  return 0.5 * x;
+}
+template <typename E>
+__device__ __forceinline__ E upwind_term(E w, E a, E b) {
+  if constexpr (sizeof(E) == 8) {
+    const uint64_t W = dbits(w);
+    double p, q;
+    if (W == 0ull) {  // (1 - 0) a + 0 b
+      p = a;
+      q = zero_times(b);
+    } else if (W == 0x3FF0000000000000ull) {  // (1 - 1) a + 1 b
+      p = zero_times(a);
+      q = b;
+    } else if (W == 0x3FE0000000000000ull) {  // halves
+      p = half_of(a);
+      q = half_of(b);
+    } else {
+      p = (1.0 - w) * a;
+      q = w * b;
+    }
+    return p + q;
+  } else {
+    return (E(1) - w) * a + w * b;
+  }
+}
+
 template <int D, typename E = double>
 __device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const Ctl* ctl, dim3 bid) {
   if (ctl->done) return;
@@ -1319,23 +1362,23 @@ __device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const
   // uct_contact (calcCornerEmf.hpp:224-282)
   const E* wsx = emf<E>(f.svx);
   const E* wsy = emf<E>(f.svy);
-  const E one = E(1), q4 = E(0.25);
-  const E ez_l2 = (one - wsx[c - sj]) * (ezj[c] - Ex3[c - sj]) + (wsx[c - sj]) * (ezj[c - si] - Ex3[c - sj - si]);
-  const E ez_r2 = (one - wsx[c]) * (ezj[c] - Ex3[c]) + (wsx[c]) * (ezj[c - si] - Ex3[c - si]);
-  const E ez_l1 = (one - wsy[c - si]) * (ezi[c] - Ex3[c - si]) + (wsy[c - si]) * (ezi[c - sj] - Ex3[c - sj - si]);
-  const E ez_r1 = (one - wsy[c]) * (ezi[c] - Ex3[c]) + (wsy[c]) * (ezi[c - sj] - Ex3[c - sj]);
+  const E q4 = E(0.25);
+  const E ez_l2 = upwind_term(wsx[c - sj], ezj[c] - Ex3[c - sj], ezj[c - si] - Ex3[c - sj - si]);
+  const E ez_r2 = upwind_term(wsx[c], ezj[c] - Ex3[c], ezj[c - si] - Ex3[c - si]);
+  const E ez_l1 = upwind_term(wsy[c - si], ezi[c] - Ex3[c - si], ezi[c - sj] - Ex3[c - sj - si]);
+  const E ez_r1 = upwind_term(wsy[c], ezi[c] - Ex3[c], ezi[c - sj] - Ex3[c - sj]);
   ez[c] = q4 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
   if constexpr (D == 3) {
     const E* wsz = emf<E>(f.svz);
-    const E ex_l3 = (one - wsy[c - sk]) * (exk[c] - Ex1[c - sk]) + (wsy[c - sk]) * (exk[c - sj] - Ex1[c - sk - sj]);
-    const E ex_r3 = (one - wsy[c]) * (exk[c] - Ex1[c]) + (wsy[c]) * (exk[c - sj] - Ex1[c - sj]);
-    const E ex_l2 = (one - wsz[c - sj]) * (exj[c] - Ex1[c - sj]) + (wsz[c - sj]) * (exj[c - sk] - Ex1[c - sk - sj]);
-    const E ex_r2 = (one - wsz[c]) * (exj[c] - Ex1[c]) + (wsz[c]) * (exj[c - sk] - Ex1[c - sk]);
+    const E ex_l3 = upwind_term(wsy[c - sk], exk[c] - Ex1[c - sk], exk[c - sj] - Ex1[c - sk - sj]);
+    const E ex_r3 = upwind_term(wsy[c], exk[c] - Ex1[c], exk[c - sj] - Ex1[c - sj]);
+    const E ex_l2 = upwind_term(wsz[c - sj], exj[c] - Ex1[c - sj], exj[c - sk] - Ex1[c - sk - sj]);
+    const E ex_r2 = upwind_term(wsz[c], exj[c] - Ex1[c], exj[c - sk] - Ex1[c - sk]);
     ex[c] = q4 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
-    const E ey_l3 = (one - wsx[c - sk]) * (eyk[c] - Ex2[c - sk]) + (wsx[c - sk]) * (eyk[c - si] - Ex2[c - sk - si]);
-    const E ey_r3 = (one - wsx[c]) * (eyk[c] - Ex2[c]) + (wsx[c]) * (eyk[c - si] - Ex2[c - si]);
-    const E ey_l1 = (one - wsz[c - si]) * (eyi[c] - Ex2[c - si]) + (wsz[c - si]) * (eyi[c - sk] - Ex2[c - sk - si]);
-    const E ey_r1 = (one - wsz[c]) * (eyi[c] - Ex2[c]) + (wsz[c]) * (eyi[c - sk] - Ex2[c - sk]);
+    const E ey_l3 = upwind_term(wsx[c - sk], eyk[c] - Ex2[c - sk], eyk[c - si] - Ex2[c - sk - si]);
+    const E ey_r3 = upwind_term(wsx[c], eyk[c] - Ex2[c], eyk[c - si] - Ex2[c - si]);
+    const E ey_l1 = upwind_term(wsz[c - si], eyi[c] - Ex2[c - si], eyi[c - sk] - Ex2[c - sk - si]);
+    const E ey_r1 = upwind_term(wsz[c], eyi[c] - Ex2[c], eyi[c - sk] - Ex2[c - sk]);
     ey[c] = q4 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
   }
 }
