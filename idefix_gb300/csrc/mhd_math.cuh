@@ -413,6 +413,20 @@ __device__ __forceinline__ Recip shared_recip(T b) {
   }
 }
 
+// x * s for a sign s = +-1 held as its sign bit (sb: 0 or the sign mask):
+// on the FP64 path a sign-bit flip on the integer pipe, equal to the product
+// for every non-NaN x; FP32 the product
+template <typename T>
+__device__ __forceinline__ T times_sign(T x, T s, uint64_t sb) {
+  if constexpr (sizeof(T) == 8) {
+    (void)s;
+    return dfrom(dbits(x) ^ sb);
+  } else {
+    (void)sb;
+    return x * s;
+  }
+}
+
 // fast magnetosonic speed of one face state (hlldMHD.hpp:205-238)
 template <int D, int DIR, typename T>
 __device__ __forceinline__ T fast_speed(T gamma, const T* v) {
@@ -484,6 +498,7 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   scrh = rcp(sr - sl);
   const T Bx = (sr * vR[BXn] - sl * vL[BXn]) * scrh;
   const T sBx = (Bx > T(0) ? T(1) : T(-1));
+  const uint64_t sBxb = (Bx > T(0)) ? 0ull : (1ull << 63);  // its sign bit
   const T duL = sl - vL[Xn];
   const T duR = sr - vR[Xn];
   scrh = rcp(duR * uR[RHO] - duL * uL[RHO]);
@@ -572,10 +587,10 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
     ussr[RHO] = usR[RHO];
     // (sqrL + sqrR) divides the four double-star velocity and field values
     const Recip Rq = shared_recip(sqrL + sqrR);
-    vss = sqrL * vsL + sqrR * vsR + (usR[BXt] - usL[BXt]) * sBx;
+    vss = sqrL * vsL + sqrR * vsR + times_sign(usR[BXt] - usL[BXt], sBx, sBxb);
     vss = shared_div(vss, sqrL + sqrR, Rq);
     if constexpr (D == 3) {
-      wss = sqrL * wsL + sqrR * wsR + (usR[BXb] - usL[BXb]) * sBx;
+      wss = sqrL * wsL + sqrR * wsR + times_sign(usR[BXb] - usL[BXb], sBx, sBxb);
       wss = shared_div(wss, sqrL + sqrR, Rq);
     }
     ussl[Xn] = ussl[RHO] * SM;
@@ -587,11 +602,11 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
       ussr[Xb] = ussr[RHO] * wss;
     }
     ussl[BXn] = ussr[BXn] = Bx;
-    ussl[BXt] = sqrL * usR[BXt] + sqrR * usL[BXt] + sqrL * sqrR * (vsR - vsL) * sBx;
+    ussl[BXt] = sqrL * usR[BXt] + sqrR * usL[BXt] + times_sign(sqrL * sqrR * (vsR - vsL), sBx, sBxb);
     ussl[BXt] = shared_div(ussl[BXt], sqrL + sqrR, Rq);
     ussr[BXt] = ussl[BXt];
     if constexpr (D == 3) {
-      ussl[BXb] = sqrL * usR[BXb] + sqrR * usL[BXb] + sqrL * sqrR * (wsR - wsL) * sBx;
+      ussl[BXb] = sqrL * usR[BXb] + sqrR * usL[BXb] + times_sign(sqrL * sqrR * (wsR - wsL), sBx, sBxb);
       ussl[BXb] = shared_div(ussl[BXb], sqrL + sqrR, Rq);
       ussr[BXb] = ussl[BXb];
     }
@@ -609,8 +624,8 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
       scrhR = a;
       scrhR -= b;
     }
-    ussl[ENG] = usL[ENG] - sqrL * scrhL * sBx;
-    ussr[ENG] = usR[ENG] + sqrR * scrhR * sBx;
+    ussl[ENG] = usL[ENG] - times_sign(sqrL * scrhL, sBx, sBxb);
+    ussr[ENG] = usR[ENG] + times_sign(sqrR * scrhR, sBx, sBxb);
     if (SM >= T(0)) {
 #pragma unroll
       for (int n = 0; n < NV; n++) F[n] = fluxL[n] + S1L * (ussl[n] - usL[n]) + sl * (usL[n] - uL[n]);
