@@ -413,6 +413,44 @@ __device__ __forceinline__ Recip shared_recip(T b) {
   }
 }
 
+// Sign tests against zero from the bit pattern (FP64: integer pipe), equal
+// to the IEEE comparisons for every x: zeros of either sign are neither > 0
+// nor < 0, NaNs compare false.  FP32: the comparisons.
+template <typename T>
+__device__ __forceinline__ bool gt0(T x) {
+  if constexpr (sizeof(T) == 8) {
+    const int64_t b = (int64_t)dbits(x);
+    return b > 0 && b <= 0x7FF0000000000000ll;
+  } else {
+    return x > T(0);
+  }
+}
+template <typename T>
+__device__ __forceinline__ bool lt0(T x) {
+  if constexpr (sizeof(T) == 8) {
+    const uint64_t m = dbits(x) & 0x7FFFFFFFFFFFFFFFull;  // |x|
+    return (dbits(x) >> 63) && m != 0ull && m <= 0x7FF0000000000000ull;
+  } else {
+    return x < T(0);
+  }
+}
+template <typename T>
+__device__ __forceinline__ bool ge0(T x) {  // x >= 0: a zero or > 0
+  if constexpr (sizeof(T) == 8) {
+    return (dbits(x) << 1) == 0ull || gt0(x);
+  } else {
+    return x >= T(0);
+  }
+}
+template <typename T>
+__device__ __forceinline__ bool le0(T x) {
+  if constexpr (sizeof(T) == 8) {
+    return (dbits(x) << 1) == 0ull || lt0(x);
+  } else {
+    return x <= T(0);
+  }
+}
+
 // x * s for a sign s = +-1 held as its sign bit (sb: 0 or the sign mask):
 // on the FP64 path a sign-bit flip on the integer pipe, equal to the product
 // for every non-NaN x; FP32 the product
@@ -481,12 +519,12 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   const T ptL = vL[v::PRS] + half_b2<D>(vL);
   const T ptR = vR[v::PRS] + half_b2<D>(vR);
   T* F = r.F;
-  if (sl > T(0)) {
+  if (gt0(sl)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxL[n];
     return;
   }
-  if (sr < T(0)) {
+  if (lt0(sr)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxR[n];
     return;
@@ -497,8 +535,9 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   int revert_to_hllc = 0;
   scrh = rcp(sr - sl);
   const T Bx = (sr * vR[BXn] - sl * vL[BXn]) * scrh;
-  const T sBx = (Bx > T(0) ? T(1) : T(-1));
-  const uint64_t sBxb = (Bx > T(0)) ? 0ull : (1ull << 63);  // its sign bit
+  const bool bpos = gt0(Bx);
+  const T sBx = (bpos ? T(1) : T(-1));
+  const uint64_t sBxb = bpos ? 0ull : (1ull << 63);  // its sign bit
   const T duL = sl - vL[Xn];
   const T duR = sr - vR[Xn];
   scrh = rcp(duR * uR[RHO] - duL * uL[RHO]);
@@ -574,10 +613,10 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   usR[ENG] = duR * uR[ENG] - ptR * vR[Xn] + pts * SM + Bx * scrhR;
   usR[ENG] = shared_div(usR[ENG], sr - SM, RsR);
 
-  if (S1L >= T(0)) {
+  if (ge0(S1L)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxL[n] + sl * (usL[n] - uL[n]);
-  } else if (S1R <= T(0)) {
+  } else if (le0(S1R)) {
 #pragma unroll
     for (int n = 0; n < NV; n++) F[n] = fluxR[n] + sr * (usR[n] - uR[n]);
   } else {
@@ -626,7 +665,7 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
     }
     ussl[ENG] = usL[ENG] - times_sign(sqrL * scrhL, sBx, sBxb);
     ussr[ENG] = usR[ENG] + times_sign(sqrR * scrhR, sBx, sBxb);
-    if (SM >= T(0)) {
+    if (ge0(SM)) {
 #pragma unroll
       for (int n = 0; n < NV; n++) F[n] = fluxL[n] + S1L * (ussl[n] - usL[n]) + sl * (usL[n] - uL[n]);
     } else {
