@@ -125,6 +125,25 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(values, world, device="cuda"):
+    """element-wise maximum of per-rank timings over the process group (the
+    slowest rank sets the whole job's time); identity on one rank"""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def whole_job_rate(cells_per_rank, steps, world, seconds):
+    """zone-cycles/s of the whole job: every rank advances its own box
+    (replicas, weak scaling), timed by the slowest rank"""
+    return cells_per_rank * steps * world / seconds
+
+
 def cpu_baseline(size=128, cycles=12, seed=1):
     """the CPU path (oracle restatement, OpenMP on every host core) on a
     bounded sample: a size^3 box of the same workload for `cycles` cycles"""
@@ -218,12 +237,8 @@ def run_ours(args, world, rank, local):
     e1.record(stream)
     torch.cuda.synchronize()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = cells * args.steps * world / (ms * 1e-3)
+    ms = max_over_ranks([e0.elapsed_time(e1)], world)[0]
+    value = whole_job_rate(cells, args.steps, world, ms * 1e-3)
     ms_step = ms / args.steps
 
     # ---- end to end through the C ABI with host buffers ------------------
@@ -283,12 +298,9 @@ def run_ours(args, world, rank, local):
         blk.download((hVc, hVs))  # device -> host
     torch.cuda.synchronize()
     sync_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s, sync_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s, sync_s = float(t[0].item()), float(t[1].item())
-    e2e_value = cells * e2e_steps * world / e2e_s
-    e2e_sync_value = cells * e2e_steps * world / sync_s
+    e2e_s, sync_s = max_over_ranks([e2e_s, sync_s], world)
+    e2e_value = whole_job_rate(cells, e2e_steps, world, e2e_s)
+    e2e_sync_value = whole_job_rate(cells, e2e_steps, world, sync_s)
     state_bytes = hVc.nbytes + hVs.nbytes
     del h_in, h_out, d_in, d_out
 
@@ -344,8 +356,9 @@ def run_ours(args, world, rank, local):
         mblk.run(max_cycles=args.steps)
         e1.record(stream)
         torch.cuda.synchronize()
-        mms = e0.elapsed_time(e1)
-        mixed = {"value": cells * args.steps * world / (mms * 1e-3), "unit": UNIT, "ms_per_step": mms / args.steps,
+        mms = max_over_ranks([e0.elapsed_time(e1)], world)[0]
+        mixed = {"value": whole_job_rate(cells, args.steps, world, mms * 1e-3), "unit": UNIT,
+                 "ms_per_step": mms / args.steps,
                  "dtype": "f32 recon+Riemann / f64 state", "segments": mblk.segments()}
         mblk.close()
 
