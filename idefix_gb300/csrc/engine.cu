@@ -552,25 +552,35 @@ int idfx_gpu_autotune(idfx_gpu* h, int reps) {
   if (!rc && e.g.order == IDFX_LEARNED) launch_learned_recon(e);
   for (int d = 0; d < e.g.D && !rc; d++) {
     e.only_dir = d;
-    int best = e.seg[d];
-    float best_ms = 1e30f;
-    for (int s = 4; s <= 64 && s <= e.g.n[d]; s *= 2) {
-      e.seg[d] = s;
-      launch_sweeps(e, 2, 0);  // warm-up
-      for (int r = 0; r < reps; r++) {
-        cudaEventRecord(a, e.stream);
-        launch_sweeps(e, 2, 0);
-        cudaEventRecord(b, e.stream);
-        cudaEventSynchronize(b);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, a, b);
-        if (ms < best_ms) {
-          best_ms = ms;
-          best = s;
+    // candidates timed in two passes (ascending, then descending), the best
+    // of every launch kept per candidate, so that a drift of the clocks or
+    // of the cache state during the search favours no candidate
+    int cand[8], nc = 0;
+    float cand_ms[8];
+    for (int s = 4; s <= 64 && s <= e.g.n[d] && nc < 8; s *= 2) {
+      cand[nc] = s;
+      cand_ms[nc++] = 1e30f;
+    }
+    for (int pass = 0; pass < 2; pass++) {
+      for (int q = 0; q < nc; q++) {
+        const int c = pass == 0 ? q : nc - 1 - q;
+        e.seg[d] = cand[c];
+        launch_sweeps(e, 2, 0);  // warm-up
+        for (int r = 0; r < reps; r++) {
+          cudaEventRecord(a, e.stream);
+          launch_sweeps(e, 2, 0);
+          cudaEventRecord(b, e.stream);
+          cudaEventSynchronize(b);
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, a, b);
+          if (ms < cand_ms[c]) cand_ms[c] = ms;
         }
       }
     }
-    e.seg[d] = best;
+    int best = 0;
+    for (int c = 1; c < nc; c++)
+      if (cand_ms[c] < cand_ms[best]) best = c;
+    if (nc > 0) e.seg[d] = cand[best];
   }
   e.only_dir = -1;
   e.profile = prof;

@@ -43,21 +43,40 @@ struct Dir {
 constexpr double kSmallPressureFix = 1.0e-5;  // fluid_defs.hpp:23
 constexpr double kEpsUctContact = 1.0e-6;     // fluid_defs.hpp:24
 
+// FP32 quotient for the mixed path: the approximate reciprocal (MUFU) and
+// one FMA correction of the quotient, q' = q + (a - q b) r with q = a r
+// (the correction step of Markstein's FMA division, P. W. Markstein, IBM J.
+// Res. Dev. 34 (1990)): within about an ulp, at the cost of the bare
+// reciprocal-multiply plus two FMAs; no special-case path (the mixed path
+// divides by nonzero finite values; subnormals flush to zero).  Against IEEE
+// division it leaves the mixed path's errors against FP64 unchanged while
+// the bare reciprocal-multiply (2 ulp) had doubled them.
+__device__ __forceinline__ float rcp_approx(float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  return r;
+}
+__device__ __forceinline__ float fdiv_corrected(float a, float b) {
+  const float r = rcp_approx(b);
+  const float q = a * r;
+  const float e = __fmaf_rn(-q, b, a);
+  return __fmaf_rn(e, r, q);
+}
+
 // division: FP64 IEEE correctly rounded (the bit-identical path); FP32 (the
-// mixed path, whose arithmetic is FP32-accurate, not bit-matched) the fast
-// reciprocal-multiply form, within 2 ulp for divisors below 2^126 in
-// magnitude - far beyond any state or wave speed of these flows
+// mixed path, FP32-accurate rather than bit-matched) fdiv_corrected
 template <typename T>
 __device__ __forceinline__ T dv(T a, T b) {
   if constexpr (sizeof(T) == 4) {
-    return __fdividef(a, b);
+    return fdiv_corrected(a, b);
   } else {
     return a / b;
   }
 }
 
 // square root: FP64 IEEE (the bit-identical path); FP32 x * rsqrt(x), within
-// 2 ulp (the tiny offset keeps sqr(0) = 0; negative arguments stay NaN)
+// 2 ulp (the tiny offset keeps sqrt(0) = 0; negative arguments stay NaN) -
+// measured not to change the mixed path's errors against FP64
 template <typename T>
 __device__ __forceinline__ T sqr(T x) {
   if constexpr (sizeof(T) == 4) {
@@ -74,7 +93,7 @@ __device__ __forceinline__ T rcp(T b) {
   if constexpr (sizeof(T) == 8) {
     return rcp_rn(b);
   } else {
-    return __fdividef(T(1), b);
+    return fdiv_corrected(T(1), b);
   }
 }
 
