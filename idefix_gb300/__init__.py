@@ -3,7 +3,8 @@
 Host-side mirror of the reference interface for this path, over the C ABI
 of ``libidefix_gb300.so`` (declared in include/idefix_gb300.h):
 
-* :class:`GpuBlock` — one periodic Cartesian block on the GPU: state
+* :class:`GpuBlock` — one Cartesian block on the GPU (periodic, reflective
+  or outflow boundaries): state
   upload/download in the reference layout, ``cycle`` / ``run`` with the
   semantics of ``TimeIntegrator::Cycle`` and the main loop, and the
   building blocks (``set_boundaries``, ``prim_to_cons``, ``evolve_stage``,

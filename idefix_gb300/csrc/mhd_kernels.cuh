@@ -1,5 +1,6 @@
 // Kernels of one Runge-Kutta stage of the ideal-MHD Godunov step on a
-// periodic Cartesian block, FP64, bit-identical to the reference.
+// Cartesian block (periodic, reflective or outflow boundaries): FP64,
+// bit-identical to the reference, or mixed precision (T = float).
 //
 // Device state keeps the reference layout (LayoutRight, ghost zones,
 // face arrays padded by one in every active dimension) so that the C-ABI

@@ -1,8 +1,9 @@
 /*
  * idefix_gb300 — C ABI of the GB300 (sm_103a) ideal-MHD Godunov stage.
  *
- * Drop-in for the hot path of Idefix v2.2.02: one periodic Cartesian block
- * (COMPONENTS == DIMENSIONS in {2, 3}), advanced by the reference's
+ * Drop-in for the hot path of Idefix v2.2.02: one Cartesian block with
+ * periodic, reflective or outflow boundaries (COMPONENTS == DIMENSIONS in
+ * {2, 3}), advanced by the reference's
  * TimeIntegrator::Cycle semantics with PLM / LimO3 / PPM reconstruction,
  * HLLD / HLL / Roe / TVDLF fluxes and constrained transport.  In FP64 mode
  * the results are bit-identical to the reference built without FMA
