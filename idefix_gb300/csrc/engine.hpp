@@ -36,7 +36,6 @@ struct Engine {
   std::vector<Mark> marks;
   std::vector<cudaEvent_t> free_events;
   void* learned = nullptr;   // network of the learned reconstruction (ORDER 5)
-  bool xbulk = true;         // FP32 x sweep staged by bulk copies when aligned
 };
 
 // kernel classes reported by the per-kernel timing

@@ -20,7 +20,7 @@ void launch_dir(Engine& e, int invdt, int last) {
     const unsigned blocks = (unsigned)((cols + kXW - 1) / kXW);
     const bool aligned = g.nt[0] % 4 == 0 && (reinterpret_cast<uintptr_t>(e.f.Vc32) & 15) == 0 &&
                          (reinterpret_cast<uintptr_t>(e.f.Uc) & 15) == 0;
-    if (aligned && e.xbulk) {
+    if (aligned) {
       const size_t smem = (size_t)kXW * xb_warp_bytes(Var<D>::NV, Var<D>::BX1);
       k_sweep_xbulk<D, ORDER, SOLVER, T><<<blocks, 32 * kXW, smem, e.stream>>>(g, e.f, e.ctl, invdt, last);
     } else {
