@@ -1237,49 +1237,6 @@ __device__ __forceinline__ E riemann_edge(int order, const double* q, long long 
   return aL * vLv * bL + aR * vRv * bR;
 }
 
-// One upwind term of CalcContactAverage, (1 - w) a + w b with the weight w
-// in {0, 1/2, 1} (storeFlux.hpp:40-43).  The FP64 path forms the two
-// products exactly on the integer pipe - a product by 1 is the value, by 0 a
-// zero of the value's sign, by 1/2 an exponent decrement - and 1 - w from
-// w's bit pattern, so only the sum issues on the FP64 pipe; any other weight,
-// and non-finite or subnormal values, take the FP64 expression.  Every case
-// is bit-identical to the reference's expression.
-__device__ __forceinline__ double zero_times(double x) {  // (+0) x
-  const uint64_t u = dbits(x);
-  if (((u >> 52) & 0x7ffu) != 0x7ffu) return dfrom(u & (1ull << 63));
-  return 0.0 * x;
-}
-__device__ __forceinline__ double half_of(double x) {  // x / 2
-  const uint64_t u = dbits(x);
-  const uint32_t e = (uint32_t)(u >> 52) & 0x7ffu;
-  if (e - 2u < 2045u) return dfrom(u - (1ull << 52));
-  if ((u << 1) == 0ull) return x;
-  return 0.5 * x;
-}
-template <typename E>
-__device__ __forceinline__ E upwind_term(E w, E a, E b) {
-  if constexpr (sizeof(E) == 8) {
-    const uint64_t W = dbits(w);
-    double p, q;
-    if (W == 0ull) {  // (1 - 0) a + 0 b
-      p = a;
-      q = zero_times(b);
-    } else if (W == 0x3FF0000000000000ull) {  // (1 - 1) a + 1 b
-      p = zero_times(a);
-      q = b;
-    } else if (W == 0x3FE0000000000000ull) {  // halves
-      p = half_of(a);
-      q = half_of(b);
-    } else {
-      p = (1.0 - w) * a;
-      q = w * b;
-    }
-    return p + q;
-  } else {
-    return (E(1) - w) * a + w * b;
-  }
-}
-
 template <int D, typename E = double>
 __device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const Ctl* ctl, dim3 bid) {
   if (ctl->done) return;

@@ -15,6 +15,7 @@
 #pragma once
 #include <cstdint>
 
+#include "exact_ops.cuh"
 #include "intdiv.cuh"
 #include "rdiv.cuh"
 
@@ -429,58 +430,6 @@ __device__ __forceinline__ Recip shared_recip(T b) {
     return recip(b);
   } else {
     return Recip{0.0, 0.0};
-  }
-}
-
-// Sign tests against zero from the bit pattern (FP64: integer pipe), equal
-// to the IEEE comparisons for every x: zeros of either sign are neither > 0
-// nor < 0, NaNs compare false.  FP32: the comparisons.
-template <typename T>
-__device__ __forceinline__ bool gt0(T x) {
-  if constexpr (sizeof(T) == 8) {
-    const int64_t b = (int64_t)dbits(x);
-    return b > 0 && b <= 0x7FF0000000000000ll;
-  } else {
-    return x > T(0);
-  }
-}
-template <typename T>
-__device__ __forceinline__ bool lt0(T x) {
-  if constexpr (sizeof(T) == 8) {
-    const uint64_t m = dbits(x) & 0x7FFFFFFFFFFFFFFFull;  // |x|
-    return (dbits(x) >> 63) && m != 0ull && m <= 0x7FF0000000000000ull;
-  } else {
-    return x < T(0);
-  }
-}
-template <typename T>
-__device__ __forceinline__ bool ge0(T x) {  // x >= 0: a zero or > 0
-  if constexpr (sizeof(T) == 8) {
-    return (dbits(x) << 1) == 0ull || gt0(x);
-  } else {
-    return x >= T(0);
-  }
-}
-template <typename T>
-__device__ __forceinline__ bool le0(T x) {
-  if constexpr (sizeof(T) == 8) {
-    return (dbits(x) << 1) == 0ull || lt0(x);
-  } else {
-    return x <= T(0);
-  }
-}
-
-// x * s for a sign s = +-1 held as its sign bit (sb: 0 or the sign mask):
-// on the FP64 path a sign-bit flip on the integer pipe, equal to the product
-// for every non-NaN x; FP32 the product
-template <typename T>
-__device__ __forceinline__ T times_sign(T x, T s, uint64_t sb) {
-  if constexpr (sizeof(T) == 8) {
-    (void)s;
-    return dfrom(dbits(x) ^ sb);
-  } else {
-    (void)sb;
-    return x * s;
   }
 }
 
