@@ -228,3 +228,38 @@ def test_gpu_shock_tube_to_t10_bit_identical_and_uniform():
     assert rho[0] == 1.0 and rho[-1] == 0.125
     assert 0.1 < rho.min() and rho.max() < 1.1
     blk.close()
+
+
+COMBOS = [
+    (2, dict(order="plm", solver="hlld", shock_flattening=0.5, bc=(R, O))),
+    (3, dict(order="limo3", solver="hll", emf="uct_hll", bc=(O, O, O))),
+    (2, dict(order="ppm", solver="roe", nstages=3, bc=(R, PER))),
+    (3, dict(order="plm", solver="tvdlf", emf="arithmetic", bc=(R, O, PER))),
+    (3, dict(order="ppm", solver="hlld", emf="uct_hlld", shock_flattening=0.0, bc=(O, PER, RO))),
+]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,scheme", COMBOS)
+def test_gpu_combined_options_match_oracle(dims, scheme):
+    """boundaries together with shock flattening, RK3 and the other solvers /
+    EMF averages (each combination pinned to the reference harness on the
+    CPU): bit-identical to the oracle"""
+    from oracle.pyofx import Oracle
+
+    n, state = _state(dims)
+    kw = dict(scheme, cfl=0.6 if dims == 2 else 0.4, first_dt=1e-4)
+    cycles = 25 if dims == 2 else 8
+    o = Oracle(dims, n, threads=os.cpu_count() or 1, **kw)
+    o.set_prim(*embed(dims, n, o.ng, *state))
+    assert o.run(max_cycles=cycles) == 0
+    ref = extract(dims, n, o.ng, *o.get_prim())
+    blk = ig.GpuBlock(dims, n, **kw)
+    blk.upload(*embed(dims, n, blk.ng, *state))
+    blk.run(max_cycles=cycles)
+    out = extract(dims, n, blk.ng, *blk.download())
+    assert np.array_equal(out[0], ref[0]), np.nanmax(np.abs(out[0] - ref[0]))
+    for c in range(dims):
+        assert np.array_equal(out[1][c], ref[1][c])
+    assert blk.get_time()[:2] == o.get_time()[:2]
+    blk.close()

@@ -268,3 +268,35 @@ def test_oracle_matches_reference_on_field_loop(oracle_lib, reference_libs):
     assert port[0] == ref[0] == 0
     assert _same(port[1], ref[1])
     assert port[2] == ref[2]
+
+
+COMBO_CASES = [
+    (2, dict(order="plm", solver="hlld", shock_flattening=0.5, bc=(R, O))),
+    (3, dict(order="limo3", solver="hll", emf="uct_hll", bc=(O, O, O))),
+    (2, dict(order="ppm", solver="roe", nstages=3, bc=(R, PER))),
+    (3, dict(order="plm", solver="tvdlf", emf="arithmetic", bc=(R, O, PER))),
+    (3, dict(order="ppm", solver="hlld", emf="uct_hlld", shock_flattening=0.0, bc=(O, PER, RO))),
+]
+
+
+@pytest.mark.parametrize("dims,scheme", COMBO_CASES)
+def test_oracle_matches_reference_on_combined_options(oracle_lib, reference_libs, dims, scheme):
+    # boundaries together with shock flattening, RK3 and the other solvers /
+    # EMF averages, against the reference harness
+    if dims == 2:
+        n = (32, 24)
+        Vc, Vs = ic.orszag_tang_2d(32, nghost=2)
+        state = extract(dims, (32, 32), 2, Vc, Vs)
+        state = (state[0][:, :, :24, :], [st[:, :24 + (c == 1), :] for c, st in enumerate(state[1])])
+    else:
+        n = (10, 10, 10)
+        Vc, Vs = ic.turbulence_3d(n[0], seed=9, nghost=2, kmax=4)
+        state = extract(dims, n, 2, Vc, Vs)
+    P.LIB_REF = os.path.join(reference_libs, f"libofx_ref_d{dims}_o{P.ORDER[scheme['order']]}.so")
+    kw = dict(scheme, cfl=0.6 if dims == 2 else 0.4)
+    cycles = 20 if dims == 2 else 6
+    port = _run("port", dims, n, state, cycles, **kw)
+    ref = _run("ref", dims, n, state, cycles, **kw)
+    assert port[0] == ref[0] == 0
+    assert _same(port[1], ref[1])
+    assert port[2] == ref[2]
