@@ -38,6 +38,26 @@ BYTES_PER_ZONE_CYCLE = 320.0  # 8 FP64 state values x 5 transfers per RK2 cycle
 # cells processed; at 256^3 the CT-extension columns add 1.6 % instead of 3.1 %.
 FP64_INST_PER_CELL = {"sweep_x": 578.6, "sweep_y": 567.9, "sweep_z": 572.2}
 DRAM_BYTES_PER_CELL = {"sweep_x": 193.3, "sweep_y": 172.7, "sweep_z": 171.7}
+# FP64 operations per active zone and RK2 cycle of the reference algorithm on
+# this workload at 256^3, each add/sub, mul, div and sqrt counted once
+# (1465.5 + 1662.8 + 215.5 + 35.8): the operation-counting build of the CPU
+# oracle, `python -m oracle.opcount --n 256`.
+FP64_FLOP_PER_ZONE_CYCLE = 3379.6
+
+
+def fp64_flop_roof(value, peak_gops):
+    """The algorithmic FP64 rate of one GPU running `value` zone-cycles/s,
+    against the FP64 issue rate measured on it (Gop/s), and the zone-cycle
+    rate that issue rate allows if every counted operation took a single FP64
+    instruction (an upper bound: a correctly rounded division or square root
+    takes several)."""
+    if not peak_gops or peak_gops <= 0.0:
+        return None
+    ach = value * FP64_FLOP_PER_ZONE_CYCLE / 1e9
+    return {"flop_per_zone_cycle": FP64_FLOP_PER_ZONE_CYCLE, "achieved": ach, "unit": "G FP64 FLOP/s",
+            "peak": peak_gops, "frac": ach / peak_gops,
+            "ceiling_zone_cycles_per_gpu": peak_gops * 1e9 / FP64_FLOP_PER_ZONE_CYCLE,
+            "count_source": "operation-counting build of the CPU oracle on this workload, 256^3"}
 
 
 def parse():
@@ -395,6 +415,7 @@ def run_ours(args, world, rank, local):
                          "traffic_note": "ncu dram read+write per active cell of the 128^3 sweep x 256^3 cells",
                          "note": "FP64-issue bound (GB300 FP64 ~1.2 TFLOP/s): see fp64_roofline"},
             "fp64_roofline": fp64_roof,
+            "fp64_flop": fp64_flop_roof(value / world, fp64_peak) if args.precision == "fp64" else None,
             "segments": blk.segments(),
             "cycle_hbm": {"achieved": cycle_gbs, "unit": "GB/s", "frac": cycle_gbs / hbm_peak,
                           "bytes_per_zone_cycle": BYTES_PER_ZONE_CYCLE},

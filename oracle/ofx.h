@@ -2,7 +2,8 @@
  * CPU oracle for the ideal-MHD Godunov stage — TEST INFRASTRUCTURE ONLY.
  *
  * This is a plain-C restatement of the reference algorithm (Idefix v2.2.02,
- * Cartesian, uniform grid, periodic boxes, COMPONENTS == DIMENSIONS in {2,3}).
+ * Cartesian, uniform grid, periodic, reflective or outflow boundaries,
+ * COMPONENTS == DIMENSIONS in {2,3}).
  * It is the checker for the CUDA path: only tests/, __graft_entry__.smoke()
  * and bench.py's CPU-baseline leg may load it.  Nothing in the product library
  * links or calls it.

@@ -1,0 +1,90 @@
+"""Floating-point operations per zone-cycle of the reference algorithm -
+TEST INFRASTRUCTURE ONLY.
+
+Runs the counting build of the CPU oracle (``opcount.cpp``, built by
+``make -C oracle count``; results bit-identical to ``libofx.so``) on the 3-D
+decaying-turbulence workload (HLLD + PLM + uct_contact, RK2, periodic) and
+prints one JSON line of operation counts per active zone and cycle, by kind:
+add/sub, mul, div, sqrt, min/max, abs, compare, negate.  ``cycle`` counts a
+whole TimeIntegrator::Cycle (timeIntegrator.cpp:246-414: boundaries,
+cons/prim conversions, the two stages, the RK combination, the dt
+reduction); ``stage`` counts one Fluid::EvolveStage alone (evolveStage.hpp:
+13-90: reconstruction, Riemann fluxes and flux-difference update in three
+directions, the corner EMFs and the face update).  The counts depend on the
+data (HLLD fallbacks, limiter branches), so they are taken on the workload
+itself.
+
+    python -m oracle.opcount --n 256 --cycles 1
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KINDS = ("add", "mul", "div", "sqrt", "minmax", "abs", "cmp", "neg")
+
+
+def _read(lib):
+    c = (ctypes.c_longlong * len(KINDS))()
+    lib.ofx_opcount_read(c, len(KINDS))
+    return np.array(list(c), dtype=np.float64)
+
+
+def _summary(counts, units):
+    per = counts / units
+    d = {k: round(float(v), 2) for k, v in zip(KINDS, per)}
+    # FLOP: each add, mul, div and sqrt counts one
+    d["flop"] = round(float(per[0] + per[1] + per[2] + per[3]), 2)
+    return d
+
+
+def count(n=64, cycles=1, seed=1):
+    sys.path.insert(0, os.path.dirname(HERE))
+    from idefix_gb300 import ic
+    from oracle.pyofx import Oracle
+
+    subprocess.run(["make", "-s", "-C", HERE, "libofx_count.so"], check=True)
+    Vc, Vs = ic.turbulence_3d(n=n, seed=seed)
+    o = Oracle(3, (n, n, n), kind="count")
+    o.set_prim(Vc, Vs)
+    lib = o.lib
+    lib.ofx_opcount_reset()
+    for _ in range(cycles):
+        st = o.cycle()
+        if st != 0:
+            raise RuntimeError(f"oracle cycle failed with status {st}")
+    cyc = _read(lib)
+    # one stage on the current state, its inputs prepared outside the count
+    t, dt, _ = o.get_time()
+    lib.ofx_set_boundaries(o.h)
+    lib.ofx_prim_to_cons(o.h)
+    lib.ofx_reset_stage(o.h)
+    lib.ofx_opcount_reset()
+    lib.ofx_evolve_stage(o.h, t, dt)
+    stage = _read(lib)
+    cells = n**3
+    return {
+        "workload": f"turbulence 3-D {n}^3 FP64, HLLD + PLM + uct_contact, RK2",
+        "cells": cells,
+        "cycles": cycles,
+        "cycle": _summary(cyc, cells * cycles),
+        "stage": _summary(stage, cells),
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--cycles", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=1)
+    a = ap.parse_args()
+    print(json.dumps(count(a.n, a.cycles, a.seed)))
+
+
+if __name__ == "__main__":
+    main()

@@ -2,12 +2,14 @@
 
 Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
 as the checker; the product library never imports this module.
-The same API is served by two shared objects built by oracle/Makefile:
+The same API is served by three shared objects built by oracle/Makefile:
 
 * ``oracle/libofx.so``          - the plain-C restatement (ofx.c)
 * ``oracle/_ref/libofx_ref.so`` - the reference's own hot-path headers
   compiled against a small harness (ref_harness.cpp); only buildable where
   the reference sources are present.
+* ``oracle/libofx_count.so``    - ofx.c with a scalar type that counts its
+  floating-point operations (opcount.cpp; kind="count"); same results.
 """
 import ctypes
 import os
@@ -17,6 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PORT = os.path.join(HERE, "libofx.so")
 LIB_REF = os.path.join(HERE, "_ref", "libofx_ref.so")
+LIB_COUNT = os.path.join(HERE, "libofx_count.so")
 
 ORDER = {"order1": 1, "plm": 2, "limo3": 3, "ppm": 4}
 SOLVER = {"hlld": 0, "hll": 1, "roe": 2, "tvdlf": 3}
@@ -26,7 +29,7 @@ _libs = {}
 
 
 def load(kind="port"):
-    path = LIB_PORT if kind == "port" else LIB_REF
+    path = {"port": LIB_PORT, "count": LIB_COUNT}.get(kind, LIB_REF)
     if path in _libs:
         return _libs[path]
     if not os.path.exists(path):
@@ -66,6 +69,9 @@ def load(kind="port"):
     lib.ofx_cycle.argtypes = [P]
     lib.ofx_run.restype = I
     lib.ofx_run.argtypes = [P, D, L]
+    if kind == "count":
+        lib.ofx_opcount_read.restype = I
+        lib.ofx_opcount_read.argtypes = [ctypes.POINTER(ctypes.c_longlong), I]
     _libs[path] = lib
     return lib
 
