@@ -3,8 +3,9 @@ TEST INFRASTRUCTURE ONLY.
 
 Runs the counting build of the CPU oracle (``opcount.cpp``, built by
 ``make -C oracle count``; results bit-identical to ``libofx.so``) on the 3-D
-decaying-turbulence workload (HLLD + PLM + uct_contact, RK2, periodic) and
-prints one JSON line of operation counts per active zone and cycle, by kind:
+decaying-turbulence workload (HLLD + PLM + uct_contact, RK2, periodic; or,
+with ``--workload lowbeta``, the low-beta workload with LimO3) and prints
+one JSON line of operation counts per active zone and cycle, by kind:
 add/sub, mul, div, sqrt, min/max, abs, compare, negate.  ``cycle`` counts a
 whole TimeIntegrator::Cycle (timeIntegrator.cpp:246-414: boundaries,
 cons/prim conversions, the two stages, the RK combination, the dt
@@ -15,6 +16,7 @@ data (HLLD fallbacks, limiter branches), so they are taken on the workload
 itself.
 
     python -m oracle.opcount --n 256 --cycles 1
+    python -m oracle.opcount --n 256 --workload lowbeta
 """
 import argparse
 import ctypes
@@ -43,14 +45,22 @@ def _summary(counts, units):
     return d
 
 
-def count(n=64, cycles=1, seed=1):
+# initial condition (idefix_gb300.ic), reconstruction, description
+WORKLOADS = {
+    "turbulence": ("turbulence_3d", "plm", "turbulence 3-D {n}^3 FP64, HLLD + PLM + uct_contact, RK2"),
+    "lowbeta": ("low_beta_3d", "limo3", "low-beta 3-D {n}^3 FP64, HLLD + LimO3 + uct_contact, RK2"),
+}
+
+
+def count(n=64, cycles=1, seed=1, workload="turbulence"):
     sys.path.insert(0, os.path.dirname(HERE))
     from idefix_gb300 import ic
     from oracle.pyofx import Oracle
 
     subprocess.run(["make", "-s", "-C", HERE, "libofx_count.so"], check=True)
-    Vc, Vs = ic.turbulence_3d(n=n, seed=seed)
-    o = Oracle(3, (n, n, n), kind="count")
+    make_ic, order, desc = WORKLOADS[workload]
+    Vc, Vs = getattr(ic, make_ic)(n=n, seed=seed)
+    o = Oracle(3, (n, n, n), order=order, kind="count")
     o.set_prim(Vc, Vs)
     lib = o.lib
     lib.ofx_opcount_reset()
@@ -69,7 +79,7 @@ def count(n=64, cycles=1, seed=1):
     stage = _read(lib)
     cells = n**3
     return {
-        "workload": f"turbulence 3-D {n}^3 FP64, HLLD + PLM + uct_contact, RK2",
+        "workload": desc.format(n=n),
         "cells": cells,
         "cycles": cycles,
         "cycle": _summary(cyc, cells * cycles),
@@ -82,8 +92,9 @@ def main():
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--cycles", type=int, default=1)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--workload", default="turbulence", choices=sorted(WORKLOADS))
     a = ap.parse_args()
-    print(json.dumps(count(a.n, a.cycles, a.seed)))
+    print(json.dumps(count(a.n, a.cycles, a.seed, a.workload)))
 
 
 if __name__ == "__main__":

@@ -93,3 +93,14 @@ def test_bench_flop_figure_follows_the_count(count_lib):
     assert roof["frac"] == pytest.approx(1.2e8 / roof["ceiling_zone_cycles_per_gpu"])
     assert roof["achieved"] == pytest.approx(1.2e8 * bench.FP64_FLOP_PER_ZONE_CYCLE / 1e9)
     assert bench.fp64_flop_roof(1.2e8, 0.0) is None
+
+
+def test_limo3_workload_counts_its_limiter(count_lib):
+    """LimO3 (slopeLimiter.hpp:25-52) adds divisions and min/max to every
+    reconstructed value: the low-beta workload counts more of both."""
+    from oracle.opcount import count
+
+    plm = count(n=16, workload="turbulence")["cycle"]
+    limo3 = count(n=16, seed=0, workload="lowbeta")["cycle"]
+    assert limo3["div"] > 1.5 * plm["div"]
+    assert limo3["minmax"] > 10 * plm["minmax"]
