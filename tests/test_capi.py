@@ -99,3 +99,49 @@ def test_missing_library_fails_loudly(tmp_path):
             ig.load_library(str(tmp_path / "absent.so"))
     finally:
         ig._lib = saved
+
+
+def _gxx():
+    import shutil
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no host C++ compiler")
+    return gxx
+
+
+def test_cpp_facade_forwards_and_throws(tmp_path):
+    """include/idefix_gb300.hpp against a scripted fake of the C ABI: the
+    reference-named calls reach the right entry points in order, statuses
+    become idefix_gb300::Error (a std::runtime_error), handles are freed once."""
+    exe = tmp_path / "facade_check"
+    subprocess.run([_gxx(), "-O1", "-std=c++17", "-Wall", "-Werror", "-o", str(exe),
+                    os.path.join(ROOT, "tests", "native", "facade_check.cpp")], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    assert "facade ok" in out.stdout
+
+
+def test_cpp_facade_links_against_the_library(lib, tmp_path):
+    """The facade compiles against include/idefix_gb300.h, links against the
+    built library, and a refused setup arrives as Error(IDFX_ERR_CONFIG)
+    before any CUDA call."""
+    src = tmp_path / "facade_link.cpp"
+    src.write_text(
+        '#include "idefix_gb300.hpp"\n#include <cstdio>\n'
+        "int main() {\n"
+        "  idfx_gpu_config cfg;\n"
+        "  idfx_gpu_default_config(&cfg, 2, 16, 16, 1);\n"
+        "  cfg.nstages = 4;\n"
+        "  try { idefix_gb300::DataBlock data(cfg); return 2; }\n"
+        "  catch (const idefix_gb300::Error& e) {\n"
+        '    std::printf("%d %s\\n", e.status(), e.what());\n'
+        "    return e.status() == IDFX_ERR_CONFIG && !e.numerical() ? 0 : 1;\n"
+        "  }\n}\n")
+    libdir = os.path.join(ROOT, "idefix_gb300")
+    exe = tmp_path / "facade_link"
+    subprocess.run([_gxx(), "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-L", libdir,
+                    "-lidefix_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    assert "invalid setup" in out.stdout
