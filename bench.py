@@ -174,7 +174,7 @@ def cpu_baseline(size=128, cycles=12, seed=1):
     threads = os.cpu_count() or 1
     Vc, Vs = ic.turbulence_3d(size, seed=seed)
     o = Oracle(3, (size,) * 3, order="plm", solver="hlld", emf="uct_contact", cfl=0.6,
-               first_dt=1e-4, threads=threads)
+               first_dt=1e-4, threads=threads, log_period=100, check_nan_period=100)
     o.set_prim(Vc, Vs)
     o.run(max_cycles=1)  # warm-up
     t0 = time.perf_counter()
@@ -185,6 +185,24 @@ def cpu_baseline(size=128, cycles=12, seed=1):
                       f"{el:.2f} s wall on {threads} threads"}
 
 
+def state_bytes_of(size):
+    """bytes of one 256^3-style state in the reference layout: Vc (8 variables,
+    2 ghosts a side) and Vs (3 components, one more face per direction)"""
+    return 8 * (8 * (size + 4) ** 3 + 3 * (size + 5) ** 3)
+
+
+def workload_config(size, precision, state_bytes):
+    """the `config` of both arms' lines: the workload the metric is quoted on"""
+    return {"workload": f"3-D MHD decaying turbulence {size}^3 periodic, HLLD+PLM "
+                        "(van Leer)+CT uct_contact, RK2, CFL 0.6, "
+                        + ("FP64 bit-identical to the reference" if precision == "fp64"
+                           else "mixed precision (FP32 reconstruction, Riemann and EMF averaging, "
+                                "FP64 state, ConsToPrim and face update)"),
+            "cells_per_gpu": size**3,
+            "l2": f"inputs larger than L2 ({state_bytes / 1e9:.2f} GB state), no flush",
+            "ic": "seeded Gaussian k^-2, Mach 1, beta 10"}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
@@ -193,24 +211,23 @@ def run_reference(args, world, rank):
 
     build.build_oracle()
     threads = os.cpu_count() or 1
-    size = 128
+    size = min(args.size, 128)
     Vc, Vs = ic.turbulence_3d(size, seed=1)
     o = Oracle(3, (size,) * 3, order="plm", solver="hlld", emf="uct_contact", cfl=0.6,
-               first_dt=1e-4, threads=threads)
+               first_dt=1e-4, threads=threads, log_period=100, check_nan_period=100)
     o.set_prim(Vc, Vs)
     o.run(max_cycles=args.warmup)
     t0 = time.perf_counter()
     o.run(max_cycles=args.steps)
     el = time.perf_counter() - t0
     value = size**3 * args.steps / el
-    sample = (f"each step = one RK2 cycle of a {size}^3 sample of the 256^3 workload on the host "
+    sample = (f"each step = one RK2 cycle of a {size}^3 sample of the {args.size}^3 workload on the host "
               f"CPU ({threads} threads, CPU restatement pinned bit-for-bit to the reference kernels)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"3-D MHD decaying turbulence {size}^3 sample (of 256^3), HLLD+PLM+CT "
-                                   "uct_contact, RK2, CFL 0.6", "l2": "inputs larger than L2"},
+            "config": workload_config(args.size, "fp64", state_bytes_of(args.size)),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -390,14 +407,7 @@ def run_ours(args, world, rank, local):
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32 recon+Riemann / f64 state", "data": "synthetic",
-            "config": {"workload": f"3-D MHD decaying turbulence {args.size}^3 periodic, HLLD+PLM "
-                                   "(van Leer)+CT uct_contact, RK2, CFL 0.6, "
-                                   + ("FP64 bit-identical to the reference" if args.precision == "fp64"
-                                      else "mixed precision (FP32 reconstruction, Riemann and EMF averaging, "
-                                           "FP64 state, ConsToPrim and face update)"),
-                       "cells_per_gpu": cells,
-                       "l2": f"inputs larger than L2 ({state_bytes / 1e9:.2f} GB state), no flush",
-                       "ic": "seeded Gaussian k^-2, Mach 1, beta 10"},
+            "config": workload_config(args.size, args.precision, state_bytes),
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": state_bytes,
                     "d2h_bytes_per_step": state_bytes, "steps": e2e_steps,

@@ -83,3 +83,32 @@ def test_dist_setup_reads_the_launcher_environment(monkeypatch):
     monkeypatch.setenv("RANK", "1")
     monkeypatch.setenv("LOCAL_RANK", "1")
     assert bench.dist_setup() == (2, 1, 1)
+
+
+def test_reference_arm_line_matches_our_arms_contract():
+    """--impl reference: the same metric, unit, direction and config as our
+    arm's line, a cpu_baseline describing the run and an e2e with no copies"""
+    import json
+
+    class Args:
+        steps, warmup, gpus, size = 1, 1, 1, 24
+
+    buf = io.StringIO()
+    with redirect_stdout(buf):
+        bench.run_reference(Args(), 1, 0)
+    line = json.loads(buf.getvalue().strip().splitlines()[-1])
+    assert line["impl"] == "reference"
+    assert line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is True and line["value"] > 0
+    assert line["config"] == bench.workload_config(24, "fp64", bench.state_bytes_of(24))
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT,
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_state_bytes_formula_matches_the_arrays():
+    from idefix_gb300 import ic
+
+    Vc, Vs = ic.turbulence_3d(16, seed=1)
+    assert bench.state_bytes_of(16) == Vc.nbytes + Vs.nbytes
