@@ -235,7 +235,6 @@ def run_reference(args, world, rank):
 
 
 def run_ours(args, world, rank, local):
-    import numpy as np
     import torch
 
     import idefix_gb300 as ig
