@@ -300,3 +300,29 @@ def test_oracle_matches_reference_on_combined_options(oracle_lib, reference_libs
     assert port[0] == ref[0] == 0
     assert _same(port[1], ref[1])
     assert port[2] == ref[2]
+
+
+NON_CUBIC = [
+    dict(order="plm", solver="hlld", emf="uct_contact"),
+    dict(order="limo3", solver="roe", emf="uct0"),
+    dict(order="ppm", solver="hll", emf="arithmetic"),
+    dict(order="plm", solver="tvdlf", emf="uct_hll", nstages=3),
+]
+
+
+@pytest.mark.parametrize("scheme", NON_CUBIC, ids=lambda s: "_".join(str(v) for v in s.values()))
+def test_oracle_matches_reference_on_a_non_cubic_block(oracle_lib, reference_libs, scheme):
+    """a 12 x 8 x 6 block (every direction its own extent and stride), cut
+    from a periodic 12^3 state, against the reference harness"""
+    n = (12, 8, 6)
+    Vc, Vs = ic.turbulence_3d(12, seed=4, nghost=2, kmax=4)
+    vc, vs = extract(3, (12, 12, 12), 2, Vc, Vs)
+    state = (vc[:, :n[2], :n[1], :n[0]],
+             [st[:n[2] + (c == 2), :n[1] + (c == 1), :n[0] + (c == 0)] for c, st in enumerate(vs)])
+    P.LIB_REF = os.path.join(reference_libs, f"libofx_ref_d3_o{P.ORDER[scheme['order']]}.so")
+    kw = dict(scheme, cfl=0.4)
+    port = _run("port", 3, n, state, 6, **kw)
+    ref = _run("ref", 3, n, state, 6, **kw)
+    assert port[0] == ref[0] == 0
+    assert _same(port[1], ref[1])
+    assert port[2] == ref[2]
