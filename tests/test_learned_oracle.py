@@ -1,12 +1,14 @@
 """CPU checks of the learned-correction oracle (oracle/mlp.py), which the GPU
 tests use as the checker of the tensor-core kernels: its gradient against
-central finite differences, its coarsening against the conservation laws
+central finite differences and, with its Adam step, against torch's
+autograd and optimiser; its coarsening against the conservation laws
 and div B = 0, and its features / PLM states on states with known answers.
 """
 import os
 import sys
 
 import numpy as np
+import pytest
 
 from idefix_gb300 import ic
 from mhd_state import extract
@@ -112,3 +114,35 @@ def test_face_targets_are_exact_for_linear_profiles():
     # r = 1: the cell values themselves
     t1 = mlp.face_layers(fine[:, :3, :3, :3], 1)
     assert np.allclose(t1[0, 0], fine[0, :3, :3, :3].ravel())
+
+
+def test_gradient_and_adam_match_torch_autograd():
+    """the oracle's hand-written backward pass and Adam step against torch's
+    autograd and torch.optim.Adam, float64 on the CPU"""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(6)
+    p = mlp.init_params(3, out_scale=0.5)
+    X = rng.standard_normal((9, mlp.NIN)) * 0.5
+    T = rng.standard_normal((9, mlp.NOUT))
+    P = {k: torch.tensor(v.copy(), dtype=torch.float64, requires_grad=True) for k, v in mlp.unpack(p).items()}
+    names = ("W1", "b1", "W2", "b2", "W3", "b3")
+    opt = torch.optim.Adam([P[k] for k in names], lr=1e-3, betas=(0.9, 0.999), eps=1e-8)
+    Xt, Tt = torch.tensor(X), torch.tensor(T)
+    mask = torch.tensor(mlp.LOSS_MASK)
+    m = np.zeros(mlp.NPARAM)
+    v = np.zeros(mlp.NPARAM)
+    for step in range(1, 4):
+        opt.zero_grad()
+        H1 = torch.nn.functional.silu(Xt @ P["W1"] + P["b1"])
+        H2 = torch.nn.functional.silu(H1 @ P["W2"] + P["b2"])
+        Y = H2 @ P["W3"] + P["b3"]
+        loss = (((Y - Tt) * mask) ** 2).sum() / X.shape[0]
+        loss.backward()
+        ref_g = np.concatenate([P[k].grad.detach().numpy().ravel() for k in names])
+        ours_loss, g = mlp.loss_and_grad(p, X, T)
+        assert abs(ours_loss - loss.item()) <= 1e-12 * abs(loss.item())
+        assert np.max(np.abs(g - ref_g)) <= 1e-12 * max(1.0, np.max(np.abs(ref_g)))
+        opt.step()
+        p, m, v = mlp.adam(p, g, m, v, step, 1e-3)
+        ref_p = np.concatenate([P[k].detach().numpy().ravel() for k in names])
+        assert np.max(np.abs(p - ref_p)) <= 1e-12
