@@ -15,6 +15,15 @@
 #define MX1 1
 #define MX2 2
 
+/* Phases of a cycle for the operation-counting build (opcount.cpp defines
+   OFX_PHASE to switch its counters); no-ops in this build. */
+enum { OFX_PH_OTHER = 0, OFX_PH_SWEEP_X, OFX_PH_SWEEP_Y, OFX_PH_SWEEP_Z, OFX_PH_CT_CORNER,
+       OFX_PH_CT_FACES, OFX_PH_BOUNDARIES, OFX_PH_PRIM2CONS, OFX_PH_RK, OFX_PH_CONS2PRIM,
+       OFX_PH_TIMESTEP, OFX_PH_CHECKS, OFX_NPH };
+#ifndef OFX_PHASE
+#define OFX_PHASE(p) ((void)0)
+#endif
+
 #define OFX_SMALL_PRESSURE_FIX (1.0e-5) /* fluid_defs.hpp:23 */
 #define OFX_EPS_UCT_CONTACT (1.0e-6)    /* fluid_defs.hpp:24 */
 
@@ -560,25 +569,33 @@ int ofx_cycle(ofx* o) {
     wc[1] = 2.0 / 3.0;
     w0[1] = 1.0 / 3.0;
   }
+  OFX_PHASE(OFX_PH_CHECKS);
   if (o->log_period > 0 && o->ncycles % o->log_period == 0) {
     if (ofx_check_divb(o) > o->maxdivb) return OFX_ERR_DIVB;
   }
+  OFX_PHASE(OFX_PH_OTHER);
   const double t0 = o->t;
   double newdt = 0.0;
   ofx_reset_stage(o);
   for (int stage = 0; stage < o->nstages; stage++) {
+    OFX_PHASE(OFX_PH_BOUNDARIES);
     ofx_set_boundaries(o);
+    OFX_PHASE(OFX_PH_PRIM2CONS);
     ofx_prim_to_cons(o);
+    OFX_PHASE(OFX_PH_OTHER);
     if (o->nstages > 1 && stage == 0) {
       memcpy(o->Uc0, o->Uc, sizeof(double) * o->nvar * o->ncell);
       memcpy(o->Vs0, o->Vs, sizeof(double) * o->D * o->nface);
     }
     ofx_evolve_stage(o, o->t, o->dt);
     o->t += o->dt;
+    OFX_PHASE(OFX_PH_CHECKS);
     if (o->check_nan_period > 0 && o->ncycles % o->check_nan_period == 0) {
       if (ofx_check_nan(o) > 0) return OFX_ERR_NAN;
     }
+    OFX_PHASE(OFX_PH_TIMESTEP);
     if (stage == 0) newdt = o->cfl * ofx_compute_timestep(o);
+    OFX_PHASE(OFX_PH_RK);
     if (stage > 0) {
       const double wcs = wc[stage - 1], w0s = w0[stage - 1];
       const size_t nu = (size_t)o->nvar * o->ncell, ns = (size_t)o->D * o->nface;
@@ -588,7 +605,9 @@ int ofx_cycle(ofx* o) {
       for (long a = 0; a < (long)ns; a++) o->Vs[a] = wcs * o->Vs[a] + w0s * o->Vs0[a];
       o->t = wcs * o->t + w0s * t0;
     }
+    OFX_PHASE(OFX_PH_CONS2PRIM);
     ofx_cons_to_prim(o);
+    OFX_PHASE(OFX_PH_OTHER);
   }
   o->t = t0 + o->dt;
   if (newdt > o->cflmax * o->dt) {

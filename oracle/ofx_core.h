@@ -1053,12 +1053,16 @@ static void SFX(evolve_mag_field)(ofx* o, double dt) {
 static void SFX(evolve_stage)(ofx* o, double t, double dt) {
   (void)t;
   for (int dir = 0; dir < OFX_D; dir++) {
+    OFX_PHASE(OFX_PH_SWEEP_X + dir);
     SFX(calc_flux)(o, dir);
     SFX(calc_rhs)(o, dir, dt);
   }
+  OFX_PHASE(OFX_PH_CT_CORNER);
   SFX(corner_emf)(o);
+  OFX_PHASE(OFX_PH_CT_FACES);
   SFX(evolve_mag_field)(o, dt);
   ofx_reconstruct_vc_field(o, o->Uc);
+  OFX_PHASE(OFX_PH_OTHER);
 }
 
 #undef SFX

@@ -9,7 +9,9 @@ one JSON line of operation counts per active zone and cycle, by kind:
 add/sub, mul, div, sqrt, min/max, abs, compare, negate.  ``cycle`` counts a
 whole TimeIntegrator::Cycle (timeIntegrator.cpp:246-414: boundaries,
 cons/prim conversions, the two stages, the RK combination, the dt
-reduction); ``stage`` counts one Fluid::EvolveStage alone (evolveStage.hpp:
+reduction), also split by phase (``cycle_by_phase``: each direction's
+reconstruction + Riemann + flux difference, the corner EMFs, the face
+update, ...); ``stage`` counts one Fluid::EvolveStage alone (evolveStage.hpp:
 13-90: reconstruction, Riemann fluxes and flux-difference update in three
 directions, the corner EMFs and the face update).  The counts depend on the
 data (HLLD fallbacks, limiter branches), so they are taken on the workload
@@ -29,11 +31,20 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 KINDS = ("add", "mul", "div", "sqrt", "minmax", "abs", "cmp", "neg")
+# the OFX_PH_* phases of ofx.c, in order
+PHASES = ("other", "sweep_x", "sweep_y", "sweep_z", "ct_corner", "ct_faces", "boundaries",
+          "prim_to_cons", "rk_combine", "cons_to_prim", "timestep", "checks")
 
 
 def _read(lib):
     c = (ctypes.c_longlong * len(KINDS))()
     lib.ofx_opcount_read(c, len(KINDS))
+    return np.array(list(c), dtype=np.float64)
+
+
+def _read_phase(lib, phase):
+    c = (ctypes.c_longlong * len(KINDS))()
+    assert lib.ofx_opcount_read_phase(phase, c, len(KINDS)) == len(PHASES)
     return np.array(list(c), dtype=np.float64)
 
 
@@ -69,6 +80,7 @@ def count(n=64, cycles=1, seed=1, workload="turbulence"):
         if st != 0:
             raise RuntimeError(f"oracle cycle failed with status {st}")
     cyc = _read(lib)
+    phases = {name: _summary(_read_phase(lib, p), n**3 * cycles) for p, name in enumerate(PHASES)}
     # one stage on the current state, its inputs prepared outside the count
     t, dt, _ = o.get_time()
     lib.ofx_set_boundaries(o.h)
@@ -84,6 +96,7 @@ def count(n=64, cycles=1, seed=1, workload="turbulence"):
         "cycles": cycles,
         "cycle": _summary(cyc, cells * cycles),
         "stage": _summary(stage, cells),
+        "cycle_by_phase": phases,
     }
 
 

@@ -72,6 +72,8 @@ def load(kind="port"):
     if kind == "count":
         lib.ofx_opcount_read.restype = I
         lib.ofx_opcount_read.argtypes = [ctypes.POINTER(ctypes.c_longlong), I]
+        lib.ofx_opcount_read_phase.restype = I
+        lib.ofx_opcount_read_phase.argtypes = [I, ctypes.POINTER(ctypes.c_longlong), I]
     _libs[path] = lib
     return lib
 

@@ -104,3 +104,19 @@ def test_limo3_workload_counts_its_limiter(count_lib):
     limo3 = count(n=16, seed=0, workload="lowbeta")["cycle"]
     assert limo3["div"] > 1.5 * plm["div"]
     assert limo3["minmax"] > 10 * plm["minmax"]
+
+
+def test_phases_add_up_to_the_cycle(count_lib):
+    """the per-phase counters split the cycle without losing or adding work;
+    the three sweeps carry most of it"""
+    from oracle.opcount import PHASES, count
+
+    res = count(n=16, cycles=2)
+    ph = res["cycle_by_phase"]
+    assert tuple(ph) == PHASES
+    for k in ("add", "mul", "div", "sqrt", "flop"):
+        # each figure is rounded to 0.01
+        assert sum(v[k] for v in ph.values()) == pytest.approx(res["cycle"][k], abs=0.01 * len(ph))
+    sweeps = sum(ph[s]["flop"] for s in ("sweep_x", "sweep_y", "sweep_z"))
+    assert 0.8 * res["cycle"]["flop"] < sweeps < res["cycle"]["flop"]
+    assert ph["ct_corner"]["flop"] > 0 and ph["ct_faces"]["flop"] > 0
