@@ -13,8 +13,8 @@ Under torchrun (N > 1) every rank advances its own 256^3 box (replicas: the
 single-GPU path has no data exchange), value = sum over ranks.  The
 reference arm times the CPU implementation of the same path on the host
 cores (the oracle restatement, pinned bit for bit to the reference's own
-kernels; the reference itself needs Kokkos, absent on the GPU host) on a
-bounded 128^3 sample of the same workload.
+kernels; the reference itself needs Kokkos, which its tree does not carry)
+on a bounded 128^3 sample of the same workload.
 """
 import argparse
 import json

@@ -202,7 +202,7 @@ int idfx_dump_read(const char* path, const idfx_gpu_config* cfg, double* Vc, dou
   char header[kHeader + 1];
   std::memset(header, 0, sizeof(header));
   if (std::fread(header, 1, kHeader, f) != (size_t)kHeader) rc = IDFX_ERR_STATE;
-  if (!rc && std::strstr(header, "big endian")) rc = IDFX_ERR_CONFIG;  // this build is little-endian
+  if (!rc && std::strstr(header, "big endian")) rc = IDFX_ERR_CONFIG;  // the library writes little-endian
   if (!rc && std::strncmp(header, "Idefix ", 7) != 0) rc = IDFX_ERR_CONFIG;
   std::string name;
   int type = 0;

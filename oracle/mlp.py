@@ -1,5 +1,5 @@
 """NumPy restatement of the learned interface-state correction — TEST
-INFRASTRUCTURE ONLY (imported by tests/ as the checker of the CUDA kernels;
+INFRASTRUCTURE ONLY (imported by tests/ as the oracle of the CUDA kernels;
 the product library never imports it).
 
 The reference has no learned component; this file is the mathematical

@@ -16,7 +16,7 @@
 #define MX2 2
 
 /* Phases of a cycle for the operation-counting build (opcount.cpp defines
-   OFX_PHASE to switch its counters); no-ops in this build. */
+   OFX_PHASE to switch its counters); no-ops in the plain oracle. */
 enum { OFX_PH_OTHER = 0, OFX_PH_SWEEP_X, OFX_PH_SWEEP_Y, OFX_PH_SWEEP_Z, OFX_PH_CT_CORNER,
        OFX_PH_CT_FACES, OFX_PH_BOUNDARIES, OFX_PH_PRIM2CONS, OFX_PH_RK, OFX_PH_CONS2PRIM,
        OFX_PH_TIMESTEP, OFX_PH_CHECKS, OFX_NPH };

@@ -4,7 +4,7 @@
  * This is a plain-C restatement of the reference algorithm (Idefix v2.2.02,
  * Cartesian, uniform grid, periodic, reflective or outflow boundaries,
  * COMPONENTS == DIMENSIONS in {2,3}).
- * It is the checker for the CUDA path: only tests/, __graft_entry__.smoke()
+ * It is the oracle of the CUDA path: only tests/, __graft_entry__.smoke()
  * and bench.py's CPU-baseline leg may load it.  Nothing in the product library
  * links or calls it.
  *

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle — TEST INFRASTRUCTURE ONLY.
 
 Loaded by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
-as the checker; the product library never imports this module.
+as the oracle; the product library never imports this module.
 The same API is served by three shared objects built by oracle/Makefile:
 
 * ``oracle/libofx.so``          - the plain-C restatement (ofx.c)

@@ -1,8 +1,8 @@
 """Mixed-precision path (FP32 reconstruction + Riemann solve, FP64 conserved
 state, ConsToPrim and CT face update) against the bit-exact FP64 path.
 
-The precision workload of the north-star (low beta = 1e-3, HLLD + LimO3 +
-CT) at reduced size: per-variable L1-relative and Linf errors of the mixed
+The low-beta precision workload (beta = 1e-3, HLLD + LimO3 + CT, 384^3 at
+full size) at reduced size: per-variable L1-relative and Linf errors of the mixed
 run against the FP64 run, and div B, which the FP64 face update keeps at
 round-off whatever the precision of the EMFs.
 """

@@ -1,5 +1,5 @@
 """CPU checks of the learned-correction oracle (oracle/mlp.py), which the GPU
-tests use as the checker of the tensor-core kernels: its gradient against
+tests use as the oracle of the tensor-core kernels: its gradient against
 central finite differences and, with its Adam step, against torch's
 autograd and optimiser; its coarsening against the conservation laws
 and div B = 0, and its features / PLM states on states with known answers.
