@@ -176,6 +176,49 @@ def field_loop_3d(nx=128, ny=2, nz=128, nghost=2):
     return Vc, Vs
 
 
+def orszag_tang_3d(nx=32, ny=64, nz=32, nghost=2):
+    """3-D Orszag-Tang vortex on the periodic unit box (test/MHD/OrszagTang3D:
+    setup.cpp:213-258, idefix.ini: 32 x 64 x 32, HLLD, CFL 0.9, t_stop 0.2;
+    the reference's published GPU benchmark problem at 128^3, run without
+    tracers): rho = 25/(36 pi), p = 5/(12 pi), v = (-sin 2pi y,
+    sin 2pi x + cos 2pi z, cos 2pi x), and the face field of the edge
+    potential A = B0/(2 pi) (cos 2pi y, sin 2pi x, cos 2pi y + cos(4pi x)/2)
+    (B0 = 1/sqrt(4 pi); every component evaluated at the left-edge
+    coordinates of its index) through DataBlockHost::MakeVsFromAmag's
+    Cartesian differences (dataBlockHost.cpp:198-213), on the faces
+    [beg, end + 1) of every direction."""
+    dims = 3
+    n = (nx, ny, nz)
+    nvar, nt, ntv = grid_shapes(dims, n, nghost)
+    xc, xl = _coords(dims, n, nghost, (0.0, 0.0, 0.0), (1.0, 1.0, 1.0))
+    dx = [1.0 / n[d] for d in range(3)]
+    B0 = 1.0 / math.sqrt(4.0 * math.pi)
+    tp = 2.0 * math.pi
+    X, Y, Z = (lambda a: a[None, None, :]), (lambda a: a[None, :, None]), (lambda a: a[:, None, None])
+    shape = (nt[2], nt[1], nt[0])
+    Vc = np.zeros((nvar, nt[2], nt[1], nt[0]))
+    Vc[0] = 25.0 / (36.0 * math.pi)
+    Vc[4] = 5.0 / (12.0 * math.pi)
+    Vc[1] = np.broadcast_to(-np.sin(tp * Y(xc[1])), shape)
+    Vc[2] = np.broadcast_to(np.sin(tp * X(xc[0])) + np.cos(tp * Z(xc[2])), shape)
+    Vc[3] = np.broadcast_to(np.cos(tp * X(xc[0])), shape)
+    # edge potential on the np_tot^3 indices (the reference's extra index
+    # np_tot is never read by the differences below)
+    Ax = np.broadcast_to(B0 / tp * np.cos(tp * Y(xl[1])), shape)
+    Ay = np.broadcast_to(B0 / tp * np.sin(tp * X(xl[0])), shape)
+    Az = np.broadcast_to(B0 / tp * (np.cos(tp * Y(xl[1])) + np.cos(2.0 * tp * X(xl[0])) / 2.0), shape)
+    g = nghost
+    s = np.s_[g:g + nz + 1, g:g + ny + 1, g:g + nx + 1]
+    si = np.s_[g:g + nz + 1, g:g + ny + 1, g + 1:g + nx + 2]
+    sj = np.s_[g:g + nz + 1, g + 1:g + ny + 2, g:g + nx + 1]
+    sk = np.s_[g + 1:g + nz + 2, g:g + ny + 1, g:g + nx + 1]
+    Vs = np.zeros((dims, ntv[2], ntv[1], ntv[0]))
+    Vs[(0,) + s] = (0.0 + 1 / dx[1] * (Az[sj] - Az[s])) - 1 / dx[2] * (Ay[sk] - Ay[s])
+    Vs[(1,) + s] = -1 / dx[0] * (Az[si] - Az[s]) + 1 / dx[2] * (Ax[sk] - Ax[s])
+    Vs[(2,) + s] = 1 / dx[0] * (Ay[si] - Ay[s]) - 1 / dx[1] * (Ax[sj] - Ax[s])
+    return Vc, Vs
+
+
 def orszag_tang_like_2d(n, mach=1.0, beta=10.0 / 3.0, nghost=2, gamma=5.0 / 3.0):
     """Orszag-Tang vortex with a chosen sonic Mach number and plasma beta.
 

@@ -4,7 +4,8 @@ TEST INFRASTRUCTURE ONLY.
 Runs the counting build of the CPU oracle (``opcount.cpp``, built by
 ``make -C oracle count``; results bit-identical to ``libofx.so``) on the 3-D
 decaying-turbulence workload (HLLD + PLM + uct_contact, RK2, periodic; or,
-with ``--workload lowbeta``, the low-beta workload with LimO3) and prints
+with ``--workload lowbeta``, the low-beta workload with LimO3; with
+``--workload ot3d``, the 3-D Orszag-Tang problem) and prints
 one JSON line of operation counts per active zone and cycle, by kind:
 add/sub, mul, div, sqrt, min/max, abs, compare, negate.  ``cycle`` counts a
 whole TimeIntegrator::Cycle (timeIntegrator.cpp:246-414: boundaries,
@@ -56,10 +57,15 @@ def _summary(counts, units):
     return d
 
 
-# initial condition (idefix_gb300.ic), reconstruction, description
+# initial condition (idefix_gb300.ic: name, arguments of (n, seed)),
+# reconstruction, CFL, description
 WORKLOADS = {
-    "turbulence": ("turbulence_3d", "plm", "turbulence 3-D {n}^3 FP64, HLLD + PLM + uct_contact, RK2"),
-    "lowbeta": ("low_beta_3d", "limo3", "low-beta 3-D {n}^3 FP64, HLLD + LimO3 + uct_contact, RK2"),
+    "turbulence": ("turbulence_3d", lambda n, seed: dict(n=n, seed=seed), "plm", 0.6,
+                   "turbulence 3-D {n}^3 FP64, HLLD + PLM + uct_contact, RK2"),
+    "lowbeta": ("low_beta_3d", lambda n, seed: dict(n=n, seed=seed), "limo3", 0.6,
+                "low-beta 3-D {n}^3 FP64, HLLD + LimO3 + uct_contact, RK2"),
+    "ot3d": ("orszag_tang_3d", lambda n, seed: dict(nx=n, ny=n, nz=n), "plm", 0.9,
+             "Orszag-Tang 3-D {n}^3 FP64, HLLD + PLM + uct_contact, RK2, CFL 0.9"),
 }
 
 
@@ -69,9 +75,9 @@ def count(n=64, cycles=1, seed=1, workload="turbulence"):
     from oracle.pyofx import Oracle
 
     subprocess.run(["make", "-s", "-C", HERE, "libofx_count.so"], check=True)
-    make_ic, order, desc = WORKLOADS[workload]
-    Vc, Vs = getattr(ic, make_ic)(n=n, seed=seed)
-    o = Oracle(3, (n, n, n), order=order, kind="count")
+    make_ic, ic_args, order, cfl, desc = WORKLOADS[workload]
+    Vc, Vs = getattr(ic, make_ic)(**ic_args(n, seed))
+    o = Oracle(3, (n, n, n), order=order, cfl=cfl, kind="count")
     o.set_prim(Vc, Vs)
     lib = o.lib
     lib.ofx_opcount_reset()

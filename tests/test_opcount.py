@@ -120,3 +120,13 @@ def test_phases_add_up_to_the_cycle(count_lib):
     sweeps = sum(ph[s]["flop"] for s in ("sweep_x", "sweep_y", "sweep_z"))
     assert 0.8 * res["cycle"]["flop"] < sweeps < res["cycle"]["flop"]
     assert ph["ct_corner"]["flop"] > 0 and ph["ct_faces"]["flop"] > 0
+
+
+def test_orszag_tang_3d_costs_as_much_as_the_turbulence_workload(count_lib):
+    """the reference's benchmark problem (3-D Orszag-Tang) and the bench's
+    turbulence workload cost the same FP64 work per zone-cycle to a few %"""
+    from oracle.opcount import count
+
+    ot = count(n=24, workload="ot3d")["cycle"]["flop"]
+    turb = count(n=24, workload="turbulence")["cycle"]["flop"]
+    assert abs(ot - turb) < 0.05 * turb

@@ -270,6 +270,19 @@ def test_oracle_matches_reference_on_field_loop(oracle_lib, reference_libs):
     assert port[2] == ref[2]
 
 
+def test_oracle_matches_reference_on_orszag_tang_3d(oracle_lib, reference_libs):
+    # test/MHD/OrszagTang3D (32 x 64 x 32, HLLD, CFL 0.9, face field from a
+    # vector potential; without its two passive tracers)
+    n = (32, 64, 32)
+    state = extract(3, n, 2, *ic.orszag_tang_3d(*n))
+    P.LIB_REF = os.path.join(reference_libs, "libofx_ref_d3_o2.so")
+    port = _run("port", 3, n, state, 10, cfl=0.9)
+    ref = _run("ref", 3, n, state, 10, cfl=0.9)
+    assert port[0] == ref[0] == 0
+    assert _same(port[1], ref[1])
+    assert port[2] == ref[2]
+
+
 COMBO_CASES = [
     (2, dict(order="plm", solver="hlld", shock_flattening=0.5, bc=(R, O))),
     (3, dict(order="limo3", solver="hll", emf="uct_hll", bc=(O, O, O))),
