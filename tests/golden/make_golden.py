@@ -65,29 +65,40 @@ def initial(dims, n):
     return extract(dims, n, 2, Vc, Vs)
 
 
+def all_cases():
+    return [c + (dict(),) for c in CASES] + EXTRA_CASES
+
+
+def make_case(case, ref_dir=os.path.join(ROOT, "oracle", "_ref")):
+    """run one case through the reference harness -> (arrays, meta)"""
+    name, dims, n, order, solver, emf, nstages, cfl, cycles, extra = case
+    vc0, vs0 = initial(dims, n)
+    P.LIB_REF = os.path.join(ref_dir, f"libofx_ref_d{dims}_o{P.ORDER[order]}.so")
+    o = P.Oracle(dims, n, order=order, solver=solver, emf=emf, nstages=nstages, cfl=cfl,
+                 kind="ref", bc=extra.get("bc"), shock_flattening=extra.get("shock"))
+    Vc, Vs = embed(dims, n, o.ng, vc0, vs0)
+    o.set_prim(Vc, Vs)
+    st = o.run(max_cycles=cycles)
+    assert st == 0, (name, st)
+    vc1, vs1 = extract(dims, n, o.ng, *o.get_prim())
+    t, dt, nc = o.get_time()
+    arrays = {"vc0": vc0, "vc1": vc1, "t": t, "dt": dt, "ncycles": nc}
+    for c in range(dims):
+        arrays[f"vs0_{c}"] = vs0[c]
+        arrays[f"vs1_{c}"] = vs1[c]
+    meta = dict(dims=dims, n=list(n), order=order, solver=solver, emf=emf, nstages=nstages,
+                cfl=cfl, cycles=cycles, gamma=5.0 / 3.0, first_dt=1e-4, **extra)
+    return arrays, meta
+
+
 def main(force=False):
-    for case in [c + (dict(),) for c in CASES] + EXTRA_CASES:
-        name, dims, n, order, solver, emf, nstages, cfl, cycles, extra = case
+    for case in all_cases():
+        name = case[0]
         if os.path.exists(os.path.join(OUT, name + ".npz")) and not force:
             continue
-        vc0, vs0 = initial(dims, n)
-        P.LIB_REF = os.path.join(ROOT, "oracle", "_ref", f"libofx_ref_d{dims}_o{P.ORDER[order]}.so")
-        o = P.Oracle(dims, n, order=order, solver=solver, emf=emf, nstages=nstages, cfl=cfl,
-                     kind="ref", bc=extra.get("bc"), shock_flattening=extra.get("shock"))
-        Vc, Vs = embed(dims, n, o.ng, vc0, vs0)
-        o.set_prim(Vc, Vs)
-        st = o.run(max_cycles=cycles)
-        assert st == 0, (name, st)
-        vc1, vs1 = extract(dims, n, o.ng, *o.get_prim())
-        t, dt, nc = o.get_time()
-        arrays = {"vc0": vc0, "vc1": vc1, "t": t, "dt": dt, "ncycles": nc}
-        for c in range(dims):
-            arrays[f"vs0_{c}"] = vs0[c]
-            arrays[f"vs1_{c}"] = vs1[c]
-        meta = dict(dims=dims, n=list(n), order=order, solver=solver, emf=emf, nstages=nstages,
-                    cfl=cfl, cycles=cycles, gamma=5.0 / 3.0, first_dt=1e-4, **extra)
+        arrays, meta = make_case(case)
         np.savez_compressed(os.path.join(OUT, name + ".npz"), meta=np.array(repr(meta)), **arrays)
-        print(name, t, dt, nc)
+        print(name, arrays["t"], arrays["dt"], arrays["ncycles"])
 
 
 if __name__ == "__main__":

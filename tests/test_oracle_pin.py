@@ -112,6 +112,29 @@ def test_oracle_matches_golden_fixture(oracle_lib, path):
         assert np.array_equal(out[1][c], z[f"vs1_{c}"])
 
 
+def test_golden_fixtures_regenerate_bit_for_bit(oracle_lib, reference_libs):
+    """every committed fixture is what tests/golden/make_golden.py makes now
+    from the reference harness: same initial state (the initial conditions
+    have not drifted), same scheme, same result"""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    saved = P.LIB_REF
+    try:
+        cases = mg.all_cases()
+        assert sorted(c[0] + ".npz" for c in cases) == sorted(os.path.basename(p) for p in _golden_cases())
+        for case in cases:
+            z = np.load(os.path.join(GOLDEN, case[0] + ".npz"))
+            arrays, meta = mg.make_case(case, reference_libs)
+            assert eval(str(z["meta"])) == meta, case[0]
+            for k, v in arrays.items():
+                assert np.array_equal(np.asarray(v), z[k]), (case[0], k)
+    finally:
+        P.LIB_REF = saved
+
+
 def test_golden_fixtures_present():
     assert len(_golden_cases()) >= 16
 
