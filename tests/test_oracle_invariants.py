@@ -116,3 +116,24 @@ def test_orszag_tang_keeps_its_point_symmetry(oracle_lib):
     for q in range(6):
         scale = np.max(np.abs(V[q][act]))
         assert np.max(np.abs(R[q][act] - V[q][act])) <= 1e-13 * scale, q
+
+
+def test_orszag_tang_3d_keeps_div_b_and_conserves(oracle_lib):
+    """the reference's 3-D benchmark problem (test/MHD/OrszagTang3D), its
+    face field built from an edge potential: div B at round-off from the
+    start, and after 10 cycles; mass, momentum and energy conserved"""
+    n = (16, 32, 16)
+    Vc, Vs = ic.orszag_tang_3d(*n)
+    o = Oracle(3, n, cfl=0.9)
+    o.set_prim(Vc, Vs)
+    o.lib.ofx_set_boundaries(o.h)
+    assert o.check_divb() < 1e-13
+    o.lib.ofx_prim_to_cons(o.h)
+    U0 = o.get_cons()
+    assert o.run(max_cycles=10) == 0
+    assert o.check_divb() < 1e-12
+    U1 = o.get_cons()
+    act = (Ellipsis, slice(NG, NG + n[2]), slice(NG, NG + n[1]), slice(NG, NG + n[0]))
+    for q in range(5):
+        s0, s1 = np.sum(U0[q][act]), np.sum(U1[q][act])
+        assert abs(s1 - s0) <= 1e-13 * np.sum(np.abs(U0[q][act])), (q, s0, s1)
