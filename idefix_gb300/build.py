@@ -70,10 +70,18 @@ def build_library(verbose=False, jobs=None, extra=()):
     return LIB
 
 
+def reference_src():
+    """the reference's src/ tree: $IDEFIX_SRC, else a `reference/` checkout
+    beside this repository; None where neither exists (the reference harness
+    is then not built and the tests that need it skip)"""
+    ref_src = os.environ.get("IDEFIX_SRC") or os.path.join(os.path.dirname(ROOT), "reference", "src")
+    return ref_src if os.path.isdir(ref_src) else None
+
+
 def build_oracle():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "libofx.so"], check=True)
-    ref_src = os.environ.get("IDEFIX_SRC", "/root/reference/src")
-    if os.path.isdir(ref_src):
+    ref_src = reference_src()
+    if ref_src:
         subprocess.run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle"), "ref",
                         f"IDEFIX_SRC={ref_src}"], check=True)
 

@@ -144,6 +144,54 @@ __global__ void k_invdt_max(Geo g, Fields f, Ctl* ctl) {
   atomic_max_pos(&ctl->invdt_max_bits, f.InvDt[cidx(g, k, j, i)]);
 }
 
+// Control-block traffic and device-side state copies by kernels rather
+// than cudaMemcpyAsync / cudaMemsetAsync: those go to the copy engines,
+// where a control read of a few hundred bytes waits behind whatever
+// gigabyte-sized host transfer a caller has queued on another stream (the
+// pipelined loop that overlaps the next step's input and the previous
+// step's result with a cycle).  A kernel writes the pinned host mirror
+// directly, and a Ctl passed by value is taken at launch.
+__global__ void k_ctl_put(Ctl* ctl, Ctl v) { *ctl = v; }
+__global__ void k_ctl_get(const Ctl* ctl, Ctl* host) { *host = *ctl; }
+enum { kClrUcFresh = 1, kClrDone = 2, kClrNan = 4, kClrDivB = 8, kClrInvDt = 16 };
+__global__ void k_ctl_clear(Ctl* ctl, int what) {
+  if (what & kClrUcFresh) ctl->uc_fresh = 0;
+  if (what & kClrDone) ctl->done = 0;
+  if (what & kClrNan) ctl->nan_count = 0ull;
+  if (what & kClrDivB) ctl->divb_bits = 0ull;
+  if (what & kClrInvDt) ctl->invdt_max_bits = 0ull;
+}
+// n doubles from src to dst (device memory), 16-byte vectors where both
+// addresses allow it
+__global__ void k_copy_f64(double* __restrict__ dst, const double* __restrict__ src, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+    const long long n2 = n / 2;
+    double2* d2 = reinterpret_cast<double2*>(dst);
+    const double2* s2 = reinterpret_cast<const double2*>(src);
+    for (long long q = t; q < n2; q += stride) d2[q] = s2[q];
+    if (t == 0 && (n & 1)) dst[n - 1] = src[n - 1];
+  } else {
+    for (long long q = t; q < n; q += stride) dst[q] = src[q];
+  }
+}
+
+// Bounded-wait probe: the wait of the bulk-copy staged sweep (mbar_wait)
+// and its give-up path (report_wait_timeout) on an mbarrier whose phase
+// never completes (mode 0: nothing arrives, as when a copy never lands) or
+// completes at once (mode 1: its one expected arrival is made).
+__global__ void k_wait_probe(Ctl* ctl, int mode, long long limit, int* gave_up) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (mode == 1) mbar_arrive(&bar);
+  const bool ok = mbar_wait(&bar, 0u, limit);
+  *gave_up = ok ? 0 : 1;
+  if (!ok) report_wait_timeout(ctl);
+}
+
 __global__ void k_set_stage_dt(Geo g, Ctl* ctl, double dt) {
   double dV = g.dx[0] * g.dx[1];
   if (g.D == 3) dV = dV * g.dx[2];
@@ -238,13 +286,27 @@ void launch_find_shock(Engine& e) {
   mark_end(e);
 }
 
+void ctl_clear(Engine& e, int what) { k_ctl_clear<<<1, 1, 0, e.stream>>>(e.ctl, what); }
+void ctl_push(Engine& e) { k_ctl_put<<<1, 1, 0, e.stream>>>(e.ctl, *e.ctl_host); }
+
+// device -> device copy of n doubles on the engine's stream (SMs, not a copy engine)
+void copy_f64(Engine& e, double* dst, const double* src, long long n) {
+  if (n <= 0) return;
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (n / 2 + kThreads - 1) / kThreads;
+  const unsigned blocks = (unsigned)(want < (long long)sms * 8 ? (want > 0 ? want : 1) : (long long)sms * 8);
+  k_copy_f64<<<blocks, kThreads, 0, e.stream>>>(dst, src, n);
+}
+
 void launch_nan_check(Engine& e) {
-  cudaMemsetAsync(&e.ctl->nan_count, 0, sizeof(unsigned long long), e.stream);
+  ctl_clear(e, kClrNan);
   IDFX_DISPATCH_D(k_nan_count, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
   k_check_nan<<<1, 1, 0, e.stream>>>(e.ctl);
 }
 void launch_divb_check(Engine& e) {
-  cudaMemsetAsync(&e.ctl->divb_bits, 0, sizeof(unsigned long long), e.stream);
+  ctl_clear(e, kClrDivB);
   IDFX_DISPATCH_D(k_divb, nblocks(n_active(e.g)), kThreads, e.g, e.f, e.ctl);
   k_check_divb<<<1, 1, 0, e.stream>>>(e.ctl);
 }
@@ -291,7 +353,8 @@ void queue_cycle(Engine& e, int use_tstop) {
 }
 
 int read_ctl(Engine& e) {
-  IDFX_CK(cudaMemcpyAsync(e.ctl_host, e.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e.stream));
+  k_ctl_get<<<1, 1, 0, e.stream>>>(e.ctl, e.ctl_host_dev);
+  IDFX_CK(cudaGetLastError());
   IDFX_CK(cudaStreamSynchronize(e.stream));
   return IDFX_OK;
 }
@@ -304,23 +367,6 @@ const char* status_text(int s) {
     case kErrFirstDt: return "Your guessed first_dt is too large. Try to reduce first_dt.";
     default: return "error";
   }
-}
-
-int choose_segments(Engine& e) {
-  // enough marching columns x segments to fill the GPU (>= ~512 threads/SM)
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long want = (long long)sms * 512;
-  for (int d = 0; d < e.g.D; d++) {
-    // marching columns: the two other directions (with the CT extension)
-    const int a = (d == 0) ? 1 : 0, b = (d == 2) ? 1 : 2;
-    const long long cols = (long long)(e.g.n[a] + 2 * e.g.ext) * (e.g.D == 3 ? e.g.n[b] + 2 * e.g.ext : 1);
-    int s = 64;
-    while (s > 2 && cols * ((e.g.n[d] + s - 1) / s) < want) s /= 2;
-    e.seg[d] = s;
-  }
-  return 0;
 }
 
 }  // namespace
@@ -338,38 +384,16 @@ static bool boundaries_valid(const idfx_gpu_config* cfg) {
   return true;
 }
 
-// ===========================================================================
-// C ABI
-// ===========================================================================
-extern "C" {
+namespace idfx {
 
-void idfx_gpu_default_config(idfx_gpu_config* c, int dims, int nx, int ny, int nz) {
-  std::memset(c, 0, sizeof(*c));
-  c->dims = dims;
-  c->n[0] = nx;
-  c->n[1] = ny;
-  c->n[2] = dims == 3 ? nz : 1;
-  for (int d = 0; d < 3; d++) {
-    c->xbeg[d] = 0.0;
-    c->xend[d] = 1.0;
-  }
-  c->order = IDFX_PLM;
-  c->solver = IDFX_HLLD;
-  c->emf = IDFX_EMF_UCT_CONTACT;
-  c->nstages = 2;
-  c->gamma = 5.0 / 3.0;
-  c->cfl = 0.9;
-  c->cfl_max_var = 1.1;   // timeIntegrator.cpp:40
-  c->first_dt = 1.0e-10;  // timeIntegrator.cpp:41
-  c->maxdivb = 1e-6;      // timeIntegrator.cpp:56
-  c->log_period = 100;    // timeIntegrator.cpp:44
-  c->check_nan_period = 100;
-  c->precision = IDFX_FP64;
-}
-
-int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
-  if (!cfg || !out) return IDFX_ERR_STATE;
-  *out = nullptr;
+// Validation of a block configuration and the block's grid and geometry:
+// ghost zones (grid.cpp:60-65), cell widths (gridHost.cpp:80-86), face
+// areas (makeGeometry.cpp:146-147,178-179,201-202), the correctly rounded
+// reciprocals of the exact quotient forms, and the CT extension of the
+// sweeps.  Shared by the handle (idfx_gpu_create) and the allocation-free
+// stage, so that both set up a block identically.
+int block_geometry(const idfx_gpu_config* cfg, Geo& g) {
+  if (!cfg) return IDFX_ERR_STATE;
   if (cfg->dims != 2 && cfg->dims != 3) return IDFX_ERR_CONFIG;
   if (cfg->order < 1 || cfg->order > 5 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
   // the learned reconstruction: 3-D, HLLD, FP64 arithmetic around the network
@@ -384,10 +408,6 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   for (int d = 0; d < cfg->dims; d++)
     if (cfg->n[d] < 2 || !(cfg->xend[d] > cfg->xbeg[d])) return IDFX_ERR_CONFIG;
   if (!boundaries_valid(cfg)) return IDFX_ERR_CONFIG;
-  idfx_gpu* h = new (std::nothrow) idfx_gpu();
-  if (!h) return IDFX_ERR_STATE;
-  Engine& e = h->e;
-  Geo& g = e.g;
   g.D = cfg->dims;
   g.order = cfg->order;
   g.solver = cfg->solver;
@@ -440,6 +460,68 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
     g.bc[d][1] = d < g.D ? cfg->rbound[d] : 0;
     if (g.bc[d][0] || g.bc[d][1]) g.nonper = 1;
   }
+  return IDFX_OK;
+}
+
+// March segment length per direction: enough marching columns x segments to
+// fill the GPU (>= ~512 threads per SM)
+void choose_segments(Engine& e) {
+  int dev = 0, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (long long)sms * 512;
+  for (int d = 0; d < e.g.D; d++) {
+    // marching columns: the two other directions (with the CT extension)
+    const int a = (d == 0) ? 1 : 0, b = (d == 2) ? 1 : 2;
+    const long long cols = (long long)(e.g.n[a] + 2 * e.g.ext) * (e.g.D == 3 ? e.g.n[b] + 2 * e.g.ext : 1);
+    int s = 64;
+    while (s > 2 && cols * ((e.g.n[d] + s - 1) / s) < want) s /= 2;
+    e.seg[d] = s;
+  }
+}
+
+}  // namespace idfx
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+void idfx_gpu_default_config(idfx_gpu_config* c, int dims, int nx, int ny, int nz) {
+  std::memset(c, 0, sizeof(*c));
+  c->dims = dims;
+  c->n[0] = nx;
+  c->n[1] = ny;
+  c->n[2] = dims == 3 ? nz : 1;
+  for (int d = 0; d < 3; d++) {
+    c->xbeg[d] = 0.0;
+    c->xend[d] = 1.0;
+  }
+  c->order = IDFX_PLM;
+  c->solver = IDFX_HLLD;
+  c->emf = IDFX_EMF_UCT_CONTACT;
+  c->nstages = 2;
+  c->gamma = 5.0 / 3.0;
+  c->cfl = 0.9;
+  c->cfl_max_var = 1.1;   // timeIntegrator.cpp:40
+  c->first_dt = 1.0e-10;  // timeIntegrator.cpp:41
+  c->maxdivb = 1e-6;      // timeIntegrator.cpp:56
+  c->log_period = 100;    // timeIntegrator.cpp:44
+  c->check_nan_period = 100;
+  c->precision = IDFX_FP64;
+}
+
+int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
+  if (!cfg || !out) return IDFX_ERR_STATE;
+  *out = nullptr;
+  Geo geo{};
+  const int grc = block_geometry(cfg, geo);
+  if (grc != IDFX_OK) return grc;
+  idfx_gpu* h = new (std::nothrow) idfx_gpu();
+  if (!h) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  Geo& g = e.g;
+  g = geo;
   e.nstages = cfg->nstages;
   e.precision = cfg->precision;
   if (e.nstages == 2) {  // timeIntegrator.cpp:62-71
@@ -476,6 +558,8 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   if (rc == IDFX_OK) rc = cuda_check(e, cudaMemsetAsync(e.pool, 0, len * sizeof(double), e.stream), "cudaMemset");
   if (rc == IDFX_OK) rc = cuda_check(e, cudaMalloc(&e.ctl, sizeof(Ctl)), "cudaMalloc(ctl)");
   if (rc == IDFX_OK) rc = cuda_check(e, cudaMallocHost(&e.ctl_host, sizeof(Ctl)), "cudaMallocHost(ctl)");
+  if (rc == IDFX_OK)
+    rc = cuda_check(e, cudaHostGetDevicePointer((void**)&e.ctl_host_dev, e.ctl_host, 0), "cudaHostGetDevicePointer(ctl)");
   if (rc != IDFX_OK) {
     std::fprintf(stderr, "idfx_gpu_create: %s\n", e.err.c_str());
     idfx_gpu_destroy(h);
@@ -512,7 +596,8 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   c.cflmax = cfg->cfl_max_var;
   c.maxdivb = cfg->maxdivb;
   *e.ctl_host = c;
-  rc = cuda_check(e, cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream), "ctl");
+  ctl_push(e);
+  rc = cuda_check(e, cudaGetLastError(), "ctl");
   if (rc == IDFX_OK) rc = cuda_check(e, cudaStreamSynchronize(e.stream), "sync");
   if (rc != IDFX_OK) {
     idfx_gpu_destroy(h);
@@ -542,7 +627,7 @@ int idfx_gpu_autotune(idfx_gpu* h, int reps) {
                                               cudaMemcpyDeviceToDevice, e.stream), "autotune backup");
   if (!rc) {
     e.ctl_host->done = 0;
-    rc = cuda_check(e, cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream), "ctl");
+    ctl_push(e);
   }
   cudaEvent_t a, b;
   cudaEventCreate(&a);
@@ -589,7 +674,7 @@ int idfx_gpu_autotune(idfx_gpu* h, int reps) {
   if (!rc) rc = cuda_check(e, cudaGetLastError(), "autotune");
   cudaMemcpyAsync(e.pool, backup, e.pool_len * sizeof(double), cudaMemcpyDeviceToDevice, e.stream);
   *e.ctl_host = saved;
-  cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream);
+  ctl_push(e);
   const cudaError_t se = cudaStreamSynchronize(e.stream);
   cudaFree(backup);
   if (!rc) rc = cuda_check(e, se, "autotune restore");
@@ -681,14 +766,24 @@ static int copy_state(idfx_gpu* h, const double* Vc, const double* Vs, cudaMemcp
   Engine& e = h->e;
   const size_t bc = sizeof(double) * (2 * e.g.D + 2) * e.g.ncell;
   const size_t bs = sizeof(double) * e.g.D * e.g.nface;
+  const bool d2d = (kind == cudaMemcpyDeviceToDevice);  // by a kernel (see k_copy_f64)
   if (up) {
-    IDFX_CK(cudaMemsetAsync(&e.ctl->uc_fresh, 0, sizeof(int), e.stream));  // Uc no longer Vc's
-    if (Vc) IDFX_CK(cudaMemcpyAsync(e.f.Vc, Vc, bc, kind, e.stream));
-    if (Vs) IDFX_CK(cudaMemcpyAsync(e.f.Vs, Vs, bs, kind, e.stream));
+    ctl_clear(e, kClrUcFresh);  // Uc no longer Vc's
+    if (d2d) {
+      if (Vc) copy_f64(e, e.f.Vc, Vc, (long long)(bc / sizeof(double)));
+      if (Vs) copy_f64(e, e.f.Vs, Vs, (long long)(bs / sizeof(double)));
+    } else {
+      if (Vc) IDFX_CK(cudaMemcpyAsync(e.f.Vc, Vc, bc, kind, e.stream));
+      if (Vs) IDFX_CK(cudaMemcpyAsync(e.f.Vs, Vs, bs, kind, e.stream));
+    }
+  } else if (d2d) {
+    if (Vc) copy_f64(e, (double*)Vc, e.f.Vc, (long long)(bc / sizeof(double)));
+    if (Vs) copy_f64(e, (double*)Vs, e.f.Vs, (long long)(bs / sizeof(double)));
   } else {
     if (Vc) IDFX_CK(cudaMemcpyAsync((void*)Vc, e.f.Vc, bc, kind, e.stream));
     if (Vs) IDFX_CK(cudaMemcpyAsync((void*)Vs, e.f.Vs, bs, kind, e.stream));
   }
+  IDFX_CK(cudaGetLastError());
   IDFX_CK(cudaStreamSynchronize(e.stream));
   return IDFX_OK;
 }
@@ -725,7 +820,8 @@ int idfx_gpu_set_time(idfx_gpu* h, double t, double dt, long long ncycles) {
   e.ctl_host->done = 0;
   e.ctl_host->status = 0;
   e.ncycles = ncycles;
-  IDFX_CK(cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream));
+  ctl_push(e);
+  IDFX_CK(cudaGetLastError());
   IDFX_CK(cudaStreamSynchronize(e.stream));
   return IDFX_OK;
 }
@@ -752,7 +848,7 @@ static int run_cycles(idfx_gpu* h, double tstop, long long max_cycles) {
   e.ctl_host->done = 0;
   e.ctl_host->status = 0;
   e.ncycles = e.ctl_host->ncycles;
-  IDFX_CK(cudaMemcpyAsync(e.ctl, e.ctl_host, sizeof(Ctl), cudaMemcpyHostToDevice, e.stream));
+  ctl_push(e);
   const int use_tstop = tstop >= 0.0;
   long long done = 0;
   const long long chunk = 64;  // host polls t / status every chunk of queued cycles
@@ -788,10 +884,7 @@ int idfx_gpu_run(idfx_gpu* h, double tstop, long long max_cycles) {
 // ---------------------------------------------------------------------------
 // the building blocks run whatever the time-integrator control says; after
 // any of them the next cycle rebuilds the conserved state from Vc
-static void clear_done(Engine& e) {
-  cudaMemsetAsync(&e.ctl->uc_fresh, 0, sizeof(int), e.stream);
-  cudaMemsetAsync(&e.ctl->done, 0, sizeof(int), e.stream);
-}
+static void clear_done(Engine& e) { ctl_clear(e, kClrUcFresh | kClrDone); }
 
 static int sync_status(Engine& e) {
   IDFX_CK(cudaGetLastError());
@@ -854,7 +947,7 @@ int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt) {
 int idfx_gpu_compute_timestep(idfx_gpu* h, double* dt) {
   if (!h || !dt) return IDFX_ERR_STATE;
   Engine& e = h->e;
-  IDFX_CK(cudaMemsetAsync(&e.ctl->invdt_max_bits, 0, sizeof(unsigned long long), e.stream));
+  ctl_clear(e, kClrInvDt);
   IDFX_DISPATCH_D(k_invdt_max, nblocks(n_active(e.g)), kThreads, e.g, e.f, e.ctl);
   int rc = sync_status(e);
   if (rc) return rc;
@@ -870,7 +963,7 @@ int idfx_gpu_compute_timestep(idfx_gpu* h, double* dt) {
 int idfx_gpu_check_divb(idfx_gpu* h, double* divb) {
   if (!h || !divb) return IDFX_ERR_STATE;
   Engine& e = h->e;
-  IDFX_CK(cudaMemsetAsync(&e.ctl->divb_bits, 0, sizeof(unsigned long long), e.stream));
+  ctl_clear(e, kClrDivB);
   IDFX_DISPATCH_D(k_divb, nblocks(n_active(e.g)), kThreads, e.g, e.f, e.ctl);
   int rc = read_ctl(e);
   if (rc) return rc;
@@ -879,10 +972,40 @@ int idfx_gpu_check_divb(idfx_gpu* h, double* divb) {
   return IDFX_OK;
 }
 
+int idfx_check_wait_timeout(int mode, long long limit, int* gave_up, int* status, int* done) {
+  if ((mode != 0 && mode != 1) || limit < 1 || !gave_up || !status || !done) return IDFX_ERR_STATE;
+  Ctl* ctl = nullptr;
+  int* flag = nullptr;
+  if (cudaMalloc(&ctl, sizeof(Ctl)) != cudaSuccess) return IDFX_ERR_CUDA;
+  if (cudaMalloc(&flag, sizeof(int)) != cudaSuccess) {
+    cudaFree(ctl);
+    return IDFX_ERR_CUDA;
+  }
+  Ctl c{};
+  c.status = kOk;
+  c.done = 0;
+  Ctl back{};
+  int gu = -1;
+  bool ok = cudaMemcpy(ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice) == cudaSuccess;
+  if (ok) {
+    k_wait_probe<<<1, 32>>>(ctl, mode, limit, flag);
+    ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+  }
+  ok = ok && cudaMemcpy(&back, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost) == cudaSuccess;
+  ok = ok && cudaMemcpy(&gu, flag, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(ctl);
+  cudaFree(flag);
+  if (!ok) return IDFX_ERR_CUDA;
+  *gave_up = gu;
+  *status = back.status;
+  *done = back.done;
+  return IDFX_OK;
+}
+
 int idfx_gpu_check_nan(idfx_gpu* h, long long* count) {
   if (!h || !count) return IDFX_ERR_STATE;
   Engine& e = h->e;
-  IDFX_CK(cudaMemsetAsync(&e.ctl->nan_count, 0, sizeof(unsigned long long), e.stream));
+  ctl_clear(e, kClrNan);
   IDFX_DISPATCH_D(k_nan_count, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
   int rc = read_ctl(e);
   if (rc) return rc;

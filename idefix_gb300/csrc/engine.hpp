@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/idefix_gb300.h"
 #include "mhd_kernels.cuh"
 
 namespace idfx {
@@ -15,6 +16,7 @@ struct Engine {
   Fields f{};
   Ctl* ctl = nullptr;        // device control block
   Ctl* ctl_host = nullptr;   // pinned mirror for reads
+  Ctl* ctl_host_dev = nullptr;  // the same mirror as the device addresses it
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int nstages = 2;
@@ -53,6 +55,12 @@ enum KernelClass {
   kKLearned,
   kKNumClasses
 };
+
+// validation of a block configuration and its grid / geometry; march
+// segment lengths for the block's size (both shared by every entry point
+// that sets up a block)
+int block_geometry(const idfx_gpu_config* cfg, Geo& g);
+void choose_segments(Engine& e);
 
 cudaEvent_t take_event(Engine& e);
 void mark_begin(Engine& e, int cls);

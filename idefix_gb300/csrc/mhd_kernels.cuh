@@ -1006,10 +1006,21 @@ __device__ __forceinline__ bool mbar_done(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (long long it = 0; it < kXBSpin; it++)
+// waits for the phase of the given parity, at most `limit` try_wait attempts;
+// false when it gave up
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kXBSpin) {
+  for (long long it = 0; it < limit; it++)
     if (mbar_done(bar, parity)) return true;
   return false;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// a bounded wait gave up: the stage reports a CUDA-side failure and the
+// cycle stops (every later kernel returns at entry; the host maps the status)
+__device__ __forceinline__ void report_wait_timeout(const Ctl* ctl) {
+  ((Ctl*)ctl)->status = kErrCuda;
+  ((Ctl*)ctl)->done = 1;
 }
 
 template <int D, int ORDER, int SOLVER, typename T>
@@ -1175,10 +1186,7 @@ __device__ __forceinline__ void d_sweep_xbulk(const Geo& g, const Fields& f, con
     }
   }
   if (!ok) {  // a copy did not land: stop the cycle, drain what is in flight
-    if (lane == 0) {
-      ((Ctl*)ctl)->status = kErrCuda;
-      ((Ctl*)ctl)->done = 1;
-    }
+    if (lane == 0) report_wait_timeout(ctl);
   }
   // every issued copy lands before the warp's shared memory is released
   for (int q = waited + 1; q <= fetched; q++) mbar_wait(bar + (q % kXB), (uint32_t)((q / kXB) & 1));

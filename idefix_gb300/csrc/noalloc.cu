@@ -18,14 +18,15 @@
 //    behind; the parts that must start at zero are cleared by each call;
 //  * calls whose GPU work overlaps (e.g. on two streams at once) race on the
 //    scratch: serialise them;
-//  * the first call on a device looks up the scratch address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//  * each call looks up the scratch address of the current device
+//    (cudaGetSymbolAddress, which allocates nothing), so a device reset or a
+//    new primary context between calls leaves no stale address behind; the
+//    first call on a device may load the library's device code there - make
+//    that first call before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/idefix_gb300.h"
 #include "engine.hpp"
@@ -36,20 +37,12 @@ static __device__ __align__(256) double g_noalloc_scratch[IDFX_NOALLOC_SCRATCH_D
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-double* s_scratch[kMaxDevices] = {nullptr};
-std::mutex s_scratch_mutex;
-
+// the scratch array as the current device addresses it: in host code the
+// symbol g_noalloc_scratch is a host-side stand-in, never a device address
 int scratch_for_current_device(double** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return IDFX_ERR_CUDA;
-  std::lock_guard<std::mutex> lock(s_scratch_mutex);
-  if (!s_scratch[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return IDFX_ERR_CUDA;
-    s_scratch[dev] = static_cast<double*>(p);
-  }
-  *out = s_scratch[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return IDFX_ERR_CUDA;
+  *out = static_cast<double*>(p);
   return IDFX_OK;
 }
 
@@ -97,67 +90,15 @@ __global__ void k_na_set_dt(Geo g, Ctl* ctl, double dt) {
   for (int d = 0; d < 3; d++) ctl->dtdx[d] = dt / g.dx[d];
 }
 
-// geometry of the block, as idfx_gpu_create sets it up
+// geometry of the block, set up exactly as idfx_gpu_create sets it up
+// (block_geometry), for the configurations this entry point supports:
+// periodic FP64 blocks of the plain reconstructions, no shock flattening
 int na_geometry(const idfx_gpu_config* cfg, Geo& g) {
   if (!cfg) return IDFX_ERR_STATE;
-  if (cfg->dims != 2 && cfg->dims != 3) return IDFX_ERR_CONFIG;
-  if (cfg->order < 1 || cfg->order > 4 || cfg->solver < 0 || cfg->solver > 3) return IDFX_ERR_CONFIG;
-  if (cfg->shock_flattening) return IDFX_ERR_CONFIG;  // not supported by this entry point
+  if (cfg->order > 4 || cfg->shock_flattening || cfg->precision != IDFX_FP64) return IDFX_ERR_CONFIG;
   for (int d = 0; d < 3; d++)  // periodic blocks only
     if (cfg->lbound[d] || cfg->rbound[d]) return IDFX_ERR_CONFIG;
-  if (cfg->emf < 0 || cfg->emf > 4 || cfg->precision != IDFX_FP64) return IDFX_ERR_CONFIG;
-  if (cfg->emf == IDFX_EMF_UCT_HLLD && (cfg->solver == IDFX_HLL || cfg->solver == IDFX_TVDLF))
-    return IDFX_ERR_CONFIG;
-  for (int d = 0; d < cfg->dims; d++)
-    if (cfg->n[d] < 2 || !(cfg->xend[d] > cfg->xbeg[d])) return IDFX_ERR_CONFIG;
-  g.D = cfg->dims;
-  g.order = cfg->order;
-  g.solver = cfg->solver;
-  g.emf = cfg->emf;
-  g.nstages = cfg->nstages;
-  g.ng = (cfg->order == 4) ? 3 : 2;
-  for (int d = 0; d < 3; d++) {
-    const bool act = d < g.D;
-    const int gd = act ? g.ng : 0;
-    g.n[d] = act ? cfg->n[d] : 1;
-    g.nt[d] = g.n[d] + 2 * gd;
-    g.ntv[d] = g.nt[d] + (act ? 1 : 0);
-    g.beg[d] = gd;
-    g.end[d] = gd + g.n[d];
-    const double xb = act ? cfg->xbeg[d] : 0.0, xe = act ? cfg->xend[d] : 1.0;
-    g.dx[d] = (xe - xb) / (g.n[d]);
-  }
-  g.s[0] = 1;
-  g.s[1] = g.nt[0];
-  g.s[2] = (long long)g.nt[0] * g.nt[1];
-  g.fs[0] = 1;
-  g.fs[1] = g.ntv[0];
-  g.fs[2] = (long long)g.ntv[0] * g.ntv[1];
-  g.ncell = (long long)g.nt[0] * g.nt[1] * g.nt[2];
-  g.nface = (long long)g.ntv[0] * g.ntv[1] * g.ntv[2];
-  if (g.D == 2) {
-    g.A[0] = 1.0 * g.dx[1];
-    g.A[1] = g.dx[0] * 1.0;
-    g.A[2] = 1.0;
-  } else {
-    g.A[0] = 1.0 * g.dx[1] * g.dx[2];
-    g.A[1] = g.dx[0] * 1.0 * g.dx[2];
-    g.A[2] = g.dx[0] * g.dx[1] * 1.0;
-  }
-  g.gamma = cfg->gamma;
-  g.gm1 = cfg->gamma - 1.0;
-  g.rgm1 = 1.0 / g.gm1;  // correctly rounded reciprocals (Markstein quotients)
-  for (int d = 0; d < 3; d++) {
-    g.rdx[d] = 1.0 / g.dx[d];
-    const double e = 0.1 * g.dx[d];  // LimO3's r dx, squared as the limiter does
-    g.l3b[d] = e * e;
-    g.l3y[d] = 1.0 / g.l3b[d];
-  }
-  g.ext = 1;
-  if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
-  for (int d = 0; d < 3; d++) g.bc[d][0] = g.bc[d][1] = 0;
-  g.nonper = 0;
-  return IDFX_OK;
+  return block_geometry(cfg, g);
 }
 
 }  // namespace
@@ -227,17 +168,7 @@ extern "C" int idfx_evolve_stage_noalloc(const idfx_gpu_config* cfg, const doubl
     return IDFX_ERR_CUDA;
   }
   // segment length of the marching sweeps, as the handle path chooses it
-  int dev = 0, sms = 148;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long want = (long long)sms * 512;
-  for (int d = 0; d < g.D; d++) {
-    const int a = (d == 0) ? 1 : 0, b = (d == 2) ? 1 : 2;
-    const long long cols = (long long)(g.n[a] + 2 * g.ext) * (g.D == 3 ? g.n[b] + 2 * g.ext : 1);
-    int s = 64;
-    while (s > 2 && cols * ((g.n[d] + s - 1) / s) < want) s /= 2;
-    e.seg[d] = s;
-  }
+  choose_segments(e);
   const int threads = 256;
   const unsigned cell_blocks = (unsigned)((nc + threads - 1) / threads);
   const long long edges = (long long)(g.n[0] + 1) * (g.n[1] + 1) * (g.D == 3 ? g.n[2] + 1 : 1);

@@ -174,6 +174,13 @@ int idfx_check_division(long long n, unsigned long long seed, long long* mismatc
  * (mixed-precision path): n random values each way, bit for bit against the
  * hardware conversions */
 int idfx_check_conversions(long long n, unsigned long long seed, long long* mismatches);
+/* self-check of the bounded device wait (no counterpart in the reference):
+ * the mbarrier wait of the bulk-copy staged sweep, at most `limit` try_wait
+ * attempts, on a barrier that never completes (mode 0, as when a copy never
+ * lands) or completes at once (mode 1); reports whether the wait gave up and
+ * the control block's status / done words that its give-up path leaves
+ * (IDFX_ERR_CUDA and 1 after a timeout).  The context stays usable. */
+int idfx_check_wait_timeout(int mode, long long limit, int* gave_up, int* status, int* done);
 
 /* Allocation-free Fluid::EvolveStage — no counterpart in the reference.
  * For callers that may not allocate GPU memory while they step (state held

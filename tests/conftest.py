@@ -8,7 +8,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE_SRC = os.environ.get("IDEFIX_SRC", "/root/reference/src")
+# the reference's src/ tree: $IDEFIX_SRC, else a `reference/` checkout beside
+# this repository (absent on machines without the reference: those tests skip)
+REFERENCE_SRC = os.environ.get("IDEFIX_SRC") or os.path.join(os.path.dirname(ROOT), "reference", "src")
 
 
 def pytest_configure(config):

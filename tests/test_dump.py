@@ -14,7 +14,9 @@ import idefix_gb300 as ig
 from idefix_gb300 import ic
 from mhd_state import extract
 
-REF_PYTOOLS = "/root/reference/pytools"
+from conftest import REFERENCE_SRC
+
+REF_PYTOOLS = os.path.join(os.path.dirname(REFERENCE_SRC), "pytools")
 
 
 @pytest.fixture(scope="module", autouse=True)

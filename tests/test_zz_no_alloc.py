@@ -38,20 +38,40 @@ def _config(lib, dims, n, **kw):
     return cfg
 
 
-@pytest.mark.parametrize("dims,emf", [(3, 0), (2, 3)])
-def test_noalloc_stage_matches_allocating_entry_point_twice(lib, dims, emf):
+def _cut(Vc, Vs, n, g):
+    """the leading n[1] x n[2] cells (and faces) of a cubic ghosted state"""
+    Vc = np.ascontiguousarray(Vc[:, : n[2] + 2 * g, : n[1] + 2 * g, :])
+    Vs = np.ascontiguousarray(Vs[:, : n[2] + 2 * g + 1, : n[1] + 2 * g + 1, :])
+    return Vc, Vs
+
+
+# (dims, n, order, solver, emf): the schemes of both ghost widths (PPM takes
+# three), every Riemann solver, the five EMF averages, and a 48^3 block with
+# uct_hll whose work arrays fill 94 % of the static scratch (the largest
+# offsets into it)
+CASES = [
+    (3, (20, 18, 16), "plm", "hlld", "uct_contact"),
+    (2, (48, 48, 1), "plm", "hlld", "uct_hll"),
+    (3, (16, 14, 12), "ppm", "hlld", "uct_hlld"),
+    (3, (16, 14, 12), "limo3", "roe", "uct_contact"),
+    (2, (40, 36, 1), "ppm", "roe", "uct_hlld"),
+    (2, (40, 36, 1), "plm", "tvdlf", "uct0"),
+    (3, (12, 10, 8), "order1", "hll", "arithmetic"),
+    (3, (48, 48, 48), "plm", "hlld", "uct_hll"),
+]
+
+
+@pytest.mark.parametrize("dims,n,order,solver,emf", CASES)
+def test_noalloc_stage_matches_allocating_entry_point_twice(lib, dims, n, order, solver, emf):
     torch = pytest.importorskip("torch")
+    g = 3 if order == "ppm" else 2
     if dims == 3:
-        n = (20, 18, 16)
-        Vc, Vs = ic.turbulence_3d(20, seed=4, kmax=4)
-        g = 2
-        Vc = np.ascontiguousarray(Vc[:, : n[2] + 2 * g, : n[1] + 2 * g, :])
-        Vs = np.ascontiguousarray(Vs[:, : n[2] + 2 * g + 1, : n[1] + 2 * g + 1, :])
+        Vc, Vs = _cut(*ic.turbulence_3d(n[0], seed=4, nghost=g, kmax=4), n, g)
     else:
-        n = (48, 48, 1)
-        Vc, Vs = ic.orszag_tang_2d(48)
-    solver = 0
-    blk = ig.GpuBlock(dims, n[:dims], emf=list(ig.EMF)[emf], solver=list(ig.SOLVER)[solver])
+        Vc, Vs = ic.orszag_tang_2d(n[0], nghost=g)
+        Vc = np.ascontiguousarray(Vc[:, :, : n[1] + 2 * g, :])
+        Vs = np.ascontiguousarray(Vs[:, :, : n[1] + 2 * g + 1, :])
+    blk = ig.GpuBlock(dims, n[:dims], order=order, emf=emf, solver=solver)
     blk.upload(Vc, Vs)
     blk.set_boundaries()
     blk.prim_to_cons()
@@ -65,7 +85,7 @@ def test_noalloc_stage_matches_allocating_entry_point_twice(lib, dims, emf):
         expect.append((blk.download_cons(), blk.download()[1]))
     blk.close()
 
-    cfg = _config(lib, dims, n, emf=emf, solver=solver)
+    cfg = _config(lib, dims, n, order=ig.ORDER[order], emf=ig.EMF[emf], solver=ig.SOLVER[solver])
     dVc = torch.from_numpy(vc_in).cuda()
     dUc = torch.from_numpy(uc0).cuda()
     dVs = torch.from_numpy(vs0).cuda()
@@ -83,6 +103,14 @@ def test_noalloc_stage_matches_allocating_entry_point_twice(lib, dims, emf):
         assert np.array_equal(vs, expect[call][1]), call
     # the primitive input is left untouched
     assert np.array_equal(dVc.cpu().numpy(), vc_in)
+
+
+def test_noalloc_scratch_need_of_the_largest_case():
+    """the 48^3 uct_hll case sits just below the static scratch size"""
+    n, ng = 48, 2
+    nc = (n + 2 * ng) ** 3
+    need = 28 * nc  # InvDt, 6 face EMFs, 3 flags, 3 cell EMFs, 3 corners, 12 weights
+    assert 0.9 * 4 * 1024 * 1024 < need < 4 * 1024 * 1024
 
 
 def test_noalloc_refuses_blocks_beyond_the_static_scratch(lib):
