@@ -131,6 +131,26 @@ def run_lowbeta(n=384, cycles=200, seed=0, cfl=0.6, log=sys.stderr):
     return res
 
 
+def run_cycles(n=128, cycles=2, precision="fp64", seed=1, order="plm", log=sys.stderr):
+    """the 3-D turbulence workload (HLLD + CT uct_contact, RK2, CFL 0.6) at n^3
+    for a few cycles on one block, no autotuning, no other work: the target
+    of per-kernel profiles (ncu -k <kernel> on this command)"""
+    import torch
+
+    Vc, Vs = ic.turbulence_3d(n, seed=seed)
+    blk = ig.GpuBlock(3, (n, n, n), order=order, cfl=0.6, first_dt=1e-4, precision=precision)
+    blk.upload(Vc, Vs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    blk.run(max_cycles=cycles)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    t, dt, nc = blk.get_time()
+    blk.close()
+    return {"n": n, "cycles": nc, "precision": precision, "order": order, "t": t, "s": el,
+            "zone_cycles_per_s": n**3 * cycles / el}
+
+
 def run_rotor(n=512, tstop=0.15, repeats=2, log=sys.stderr):
     """MHD rotor of test/MHD/RotorCartesian at its ini settings (n^2 cells
     on [-0.5,0.5]^2, Roe, PLM, uct_contact, RK2, CFL 0.2, outflow on all
@@ -345,7 +365,9 @@ if __name__ == "__main__":
     import argparse
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["ensemble", "learned", "lowbeta", "rotor"], default="ensemble")
+    ap.add_argument("--workload", choices=["ensemble", "learned", "lowbeta", "rotor", "cycles"], default="ensemble")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--order", default="plm")
     ap.add_argument("--n", type=int, default=384)
     ap.add_argument("--nbox", type=int, default=512)
     ap.add_argument("--n-fine", type=int, default=128)
@@ -367,6 +389,8 @@ if __name__ == "__main__":
         r = run_lowbeta(a.n, a.cycles or 200, a.seed)
     elif a.workload == "rotor":
         r = run_rotor(a.n if a.n != 384 else 512)
+    elif a.workload == "cycles":
+        r = run_cycles(a.n, a.cycles or 2, a.precision, order=a.order)
     else:
         pre = None
         if a.load:
