@@ -185,6 +185,19 @@ __device__ __forceinline__ void cons_to_prim(T gm1, T* V, const T* U) {
   if (V[v::PRS] <= T(0)) V[v::PRS] = T(kSmallPressureFix);
 }
 
+// induction flux of the transverse and bi-transverse field components
+// (flux.hpp:28-95)
+template <int D, int DIR, typename T>
+__device__ __forceinline__ T flux_bt(const T* V) {
+  using d = Dir<D, DIR>;
+  return V[d::Xn] * V[d::BXt] - V[d::BXn] * V[d::Xt];
+}
+template <int D, int DIR, typename T>
+__device__ __forceinline__ T flux_bb(const T* V) {
+  using d = Dir<D, DIR>;
+  return V[d::Xn] * V[d::BXb] - V[d::BXn] * V[d::Xb];
+}
+
 // physical MHD flux along DIR (flux.hpp:28-95); U is read before F is written
 template <int D, int DIR, typename T>
 __device__ __forceinline__ void phys_flux(T* F, const T* V, const T* U) {
@@ -199,8 +212,8 @@ __device__ __forceinline__ void phys_flux(T* F, const T* V, const T* U) {
   F[v::MX2] = u2 * V[d::Xn] - V[d::BXn] * V[v::BX2];
   if constexpr (D == 3) F[v::MX3] = u3 * V[d::Xn] - V[d::BXn] * V[v::BX3];
   F[d::BXn] = T(0);
-  F[d::BXt] = V[d::Xn] * V[d::BXt] - V[d::BXn] * V[d::Xt];
-  if constexpr (D == 3) F[d::BXb] = V[d::Xn] * V[d::BXb] - V[d::BXn] * V[d::Xb];
+  F[d::BXt] = flux_bt<D, DIR>(V);
+  if constexpr (D == 3) F[d::BXb] = flux_bb<D, DIR>(V);
   T Bmag2, vB;
   if constexpr (D == 3) {
     Bmag2 = sumsq<3>(V[v::BX1], V[v::BX2], V[v::BX3]);
@@ -351,8 +364,8 @@ __device__ __forceinline__ void ppm_states(T vm2, T vm1, T v0, T vp1, T vp2, T& 
 // the reference evaluates the same limiter twice per cell (once for each
 // face); here it is evaluated once and shared, with identical arithmetic.
 // pos = true for RHO and PRS (positivity fallbacks of ORDER 3 and 4).
-// ORDER 5 (learned) reads its states from the fused learned reconstruction;
-// its stencil half-width is PLM's.
+// ORDER 5 (learned) is the learned sweep's own (learned.cu); its stencil
+// half-width is PLM's.
 template <int ORDER>
 struct Recon {
   static constexpr int H = (ORDER == 1 ? 0 : (ORDER == 4 ? 2 : 1));  // ORDER 5: 1
@@ -459,7 +472,21 @@ __device__ __forceinline__ T half_b2(const T* v) {
 }
 
 // HLLD (Miyoshi & Kusano 2005) with the reference's HLLC fall-back near
-// degeneracy (hlldMHD.hpp:147-457, energy equation branch)
+// degeneracy (hlldMHD.hpp:147-457, energy equation branch).
+//
+// The reference computes both sides' physical fluxes and star states and
+// then picks one of five flux expressions (supersonic left / right, single
+// star left / right, double star left / right).  Every one of them is the
+// physical flux of ONE side plus corrections from that side's star states,
+// so here the side is chosen first - from the same sign tests - and its
+// operands are selected (integer selects of the bit patterns); the physical
+// flux, the star momentum / energy and the double-star state are then
+// evaluated for that side only, each with the reference's expression and
+// operation order, so every face flux is bit-identical to the reference's.
+// Only the HLLC fall-back reads the transverse-field fluxes of both sides.
+// On the FP64 path this removes one physical flux, one side's star energy
+// and momenta and one side's double-star state per face, and the divergent
+// selection of the end (lanes of a warp on both sides issued both branches).
 template <int D, int DIR, typename T>
 __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const T* vR, RiemannOut<D, T>& r) {
   using v = Var<D>;
@@ -469,7 +496,6 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   constexpr int BXn = d::BXn, BXt = d::BXt, BXb = d::BXb;
   T* uL = r.uL;
   T* uR = r.uR;
-  T fluxL[NV], fluxR[NV];
   const T cL = fast_speed<D, DIR>(gamma, vL);
   const T cR = fast_speed<D, DIR>(gamma, vR);
   const T cminL = vL[Xn] - cL, cmaxL = vL[Xn] + cL;
@@ -482,165 +508,158 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
   const T gm1 = gamma - T(1);
   prim_to_cons<D, 2>(gm1, uL, vL, rgm1);
   prim_to_cons<D, 2>(gm1, uR, vR, rgm1);
-  phys_flux<D, DIR>(fluxL, vL, uL);
-  phys_flux<D, DIR>(fluxR, vR, uR);
   const T ptL = vL[v::PRS] + half_b2<D>(vL);
   const T ptR = vR[v::PRS] + half_b2<D>(vR);
-  T* F = r.F;
-  if (gt0(sl)) {
-#pragma unroll
-    for (int n = 0; n < NV; n++) F[n] = fluxL[n];
-    return;
-  }
-  if (lt0(sr)) {
-#pragma unroll
-    for (int n = 0; n < NV; n++) F[n] = fluxR[n];
-    return;
-  }
-  T usL[NV], usR[NV];
-  T scrh, scrhL, scrhR;
+  // supersonic faces: the left physical flux if sl > 0, else the right one
+  // if sr < 0; every other face is subsonic and takes star states
+  bool sideL = gt0(sl);
+  const bool sub = !(sideL || lt0(sr));
+  bool dbl = false;
+  T Bx = T(0), sBx = T(1), SM = T(0), pts = T(0), duL = T(0), duR = T(0);
+  uint64_t sBxb = 0ull;
+  Recip RsL{}, RsR{};
+  T rhoL = T(0), rhoR = T(0), sqrL = T(0), sqrR = T(0), S1L = T(0), S1R = T(0);
+  T bn = T(0), bLt = T(0), bLb = T(0), bRt = T(0), bRb = T(0);  // star field components
   T vsL = T(0), vsR = T(0), wsL = T(0), wsR = T(0);
-  int revert_to_hllc = 0;
-  scrh = rcp(sr - sl);
-  const T Bx = (sr * vR[BXn] - sl * vL[BXn]) * scrh;
-  const bool bpos = gt0(Bx);
-  const T sBx = (bpos ? T(1) : T(-1));
-  const uint64_t sBxb = bpos ? 0ull : (1ull << 63);  // its sign bit
-  const T duL = sl - vL[Xn];
-  const T duR = sr - vR[Xn];
-  scrh = rcp(duR * uR[RHO] - duL * uL[RHO]);
-  const T SM = (duR * uR[Xn] - duL * uL[Xn] - ptR + ptL) * scrh;
-  T pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR + vL[RHO] * vR[RHO] * duR * duL * (vR[Xn] - vL[Xn]);
-  pts *= scrh;
-  // (sl - SM) and (sr - SM) divide the star density and the star energy
-  const Recip RsL = shared_recip(sl - SM), RsR = shared_recip(sr - SM);
-  usL[RHO] = shared_div(uL[RHO] * duL, sl - SM, RsL);
-  usR[RHO] = shared_div(uR[RHO] * duR, sr - SM, RsR);
-  const T sqrL = sqr(usL[RHO]);
-  const T sqrR = sqr(usR[RHO]);
-  T S1L = SM - dv(fabs(Bx), sqrL);
-  T S1R = SM + dv(fabs(Bx), sqrR);
-  if ((S1L - sl) < T(1.e-4) * (SM - sl)) revert_to_hllc = 1;
-  if ((S1R - sr) > T(-1.e-4) * (sr - SM)) revert_to_hllc = 1;
-  if (revert_to_hllc) {
-    scrh = rcp(sr - sl);
-    T Uhll[NV];
-#pragma unroll
-    for (int n = 0; n < NV; n++) {
-      Uhll[n] = sr * uR[n] - sl * uL[n] + fluxL[n] - fluxR[n];
-      Uhll[n] *= scrh;
+  if (sub) {
+    T scrh = rcp(sr - sl);
+    Bx = (sr * vR[BXn] - sl * vL[BXn]) * scrh;
+    const bool bpos = gt0(Bx);
+    sBx = (bpos ? T(1) : T(-1));
+    sBxb = bpos ? 0ull : (1ull << 63);  // its sign bit
+    duL = sl - vL[Xn];
+    duR = sr - vR[Xn];
+    scrh = rcp(duR * uR[RHO] - duL * uL[RHO]);
+    SM = (duR * uR[Xn] - duL * uL[Xn] - ptR + ptL) * scrh;
+    pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR + vL[RHO] * vR[RHO] * duR * duL * (vR[Xn] - vL[Xn]);
+    pts *= scrh;
+    // (sl - SM) and (sr - SM) divide the star density and the star energy
+    RsL = shared_recip(sl - SM);
+    RsR = shared_recip(sr - SM);
+    rhoL = shared_div(uL[RHO] * duL, sl - SM, RsL);
+    rhoR = shared_div(uR[RHO] * duR, sr - SM, RsR);
+    sqrL = sqr(rhoL);
+    sqrR = sqr(rhoR);
+    S1L = SM - dv(fabs(Bx), sqrL);
+    S1R = SM + dv(fabs(Bx), sqrR);
+    int revert_to_hllc = 0;
+    if ((S1L - sl) < T(1.e-4) * (SM - sl)) revert_to_hllc = 1;
+    if ((S1R - sr) > T(-1.e-4) * (sr - SM)) revert_to_hllc = 1;
+    if (revert_to_hllc) {
+      // field components of the HLL state (sr uR - sl uL + FL - FR) / (sr - sl);
+      // the normal component's fluxes are zero
+      scrh = rcp(sr - sl);
+      auto uhll = [&](T ul, T ur, T fl, T fr) {
+        T u = sr * ur - sl * ul + fl - fr;
+        u *= scrh;
+        return u;
+      };
+      bn = uhll(uL[BXn], uR[BXn], T(0), T(0));
+      bLt = bRt = uhll(uL[BXt], uR[BXt], flux_bt<D, DIR>(vL), flux_bt<D, DIR>(vR));
+      if constexpr (D == 3) bLb = bRb = uhll(uL[BXb], uR[BXb], flux_bb<D, DIR>(vL), flux_bb<D, DIR>(vR));
+      S1L = S1R = SM;
+    } else {
+      const T scrhL = dv(uL[RHO] * duL * duL - Bx * Bx, uL[RHO] * duL * (sl - SM) - Bx * Bx);
+      const T scrhR = dv(uR[RHO] * duR * duR - Bx * Bx, uR[RHO] * duR * (sr - SM) - Bx * Bx);
+      bn = Bx;
+      bLt = uL[BXt] * scrhL;
+      bRt = uR[BXt] * scrhR;
+      if constexpr (D == 3) {
+        bLb = uL[BXb] * scrhL;
+        bRb = uR[BXb] * scrhR;
+      }
     }
-    usL[BXn] = usR[BXn] = Uhll[BXn];
-    usL[BXt] = usR[BXt] = Uhll[BXt];
-    if constexpr (D == 3) usL[BXb] = usR[BXb] = Uhll[BXb];
-    S1L = S1R = SM;
-  } else {
-    scrhL = dv(uL[RHO] * duL * duL - Bx * Bx, uL[RHO] * duL * (sl - SM) - Bx * Bx);
-    scrhR = dv(uR[RHO] * duR * duR - Bx * Bx, uR[RHO] * duR * (sr - SM) - Bx * Bx);
-    usL[BXn] = Bx;
-    usL[BXt] = uL[BXt] * scrhL;
-    if constexpr (D == 3) usL[BXb] = uL[BXb] * scrhL;
-    usR[BXn] = Bx;
-    usR[BXt] = uR[BXt] * scrhR;
-    if constexpr (D == 3) usR[BXb] = uR[BXb] * scrhR;
-  }
-  scrhL = dv(Bx, uL[RHO] * duL);
-  scrhR = dv(Bx, uR[RHO] * duR);
-  vsL = vL[Xt] - scrhL * (usL[BXt] - uL[BXt]);
-  vsR = vR[Xt] - scrhR * (usR[BXt] - uR[BXt]);
-  if constexpr (D == 3) {
-    wsL = vL[Xb] - scrhL * (usL[BXb] - uL[BXb]);
-    wsR = vR[Xb] - scrhR * (usR[BXb] - uR[BXb]);
-  }
-  usL[Xn] = usL[RHO] * SM;
-  usR[Xn] = usR[RHO] * SM;
-  usL[Xt] = usL[RHO] * vsL;
-  usR[Xt] = usR[RHO] * vsR;
-  if constexpr (D == 3) {
-    usL[Xb] = usL[RHO] * wsL;
-    usR[Xb] = usR[RHO] * wsR;
-  }
-  {
-    T a = vL[Xn] * Bx + vL[Xt] * uL[BXt];
-    if constexpr (D == 3) a = a + vL[Xb] * uL[BXb];
-    T b = SM * Bx + vsL * usL[BXt];
-    if constexpr (D == 3) b = b + wsL * usL[BXb];
-    scrhL = a;
-    scrhL -= b;
-  }
-  usL[ENG] = duL * uL[ENG] - ptL * vL[Xn] + pts * SM + Bx * scrhL;
-  usL[ENG] = shared_div(usL[ENG], sl - SM, RsL);
-  {
-    T a = vR[Xn] * Bx + vR[Xt] * uR[BXt];
-    if constexpr (D == 3) a = a + vR[Xb] * uR[BXb];
-    T b = SM * Bx + vsR * usR[BXt];
-    if constexpr (D == 3) b = b + wsR * usR[BXb];
-    scrhR = a;
-    scrhR -= b;
-  }
-  usR[ENG] = duR * uR[ENG] - ptR * vR[Xn] + pts * SM + Bx * scrhR;
-  usR[ENG] = shared_div(usR[ENG], sr - SM, RsR);
-
-  if (ge0(S1L)) {
-#pragma unroll
-    for (int n = 0; n < NV; n++) F[n] = fluxL[n] + sl * (usL[n] - uL[n]);
-  } else if (le0(S1R)) {
-#pragma unroll
-    for (int n = 0; n < NV; n++) F[n] = fluxR[n] + sr * (usR[n] - uR[n]);
-  } else {
-    T vss = T(0), wss = T(0);
-    T ussl[NV], ussr[NV];
-    ussl[RHO] = usL[RHO];
-    ussr[RHO] = usR[RHO];
-    // (sqrL + sqrR) divides the four double-star velocity and field values
-    const Recip Rq = shared_recip(sqrL + sqrR);
-    vss = sqrL * vsL + sqrR * vsR + times_sign(usR[BXt] - usL[BXt], sBx, sBxb);
-    vss = shared_div(vss, sqrL + sqrR, Rq);
+    const T scrhL = dv(Bx, uL[RHO] * duL);
+    const T scrhR = dv(Bx, uR[RHO] * duR);
+    vsL = vL[Xt] - scrhL * (bLt - uL[BXt]);
+    vsR = vR[Xt] - scrhR * (bRt - uR[BXt]);
     if constexpr (D == 3) {
-      wss = sqrL * wsL + sqrR * wsR + times_sign(usR[BXb] - usL[BXb], sBx, sBxb);
+      wsL = vL[Xb] - scrhL * (bLb - uL[BXb]);
+      wsR = vR[Xb] - scrhR * (bRb - uR[BXb]);
+    }
+    // single star left if S1L >= 0, else single star right if S1R <= 0,
+    // else double star on the side of the contact (SM >= 0: left)
+    sideL = ge0(S1L) || (!le0(S1R) && ge0(SM));
+    dbl = !ge0(S1L) && !le0(S1R);
+  }
+  // the chosen side's primitive and conserved state and its physical flux
+  T vS[NV], uS[NV];
+#pragma unroll
+  for (int n = 0; n < NV; n++) {
+    vS[n] = sideL ? vL[n] : vR[n];
+    uS[n] = sideL ? uL[n] : uR[n];
+  }
+  T* F = r.F;
+  phys_flux<D, DIR>(F, vS, uS);
+  if (!sub) return;
+  // star state of the chosen side (us)
+  const T s = sideL ? sl : sr;
+  const T du = sideL ? duL : duR;
+  const T pt = sideL ? ptL : ptR;
+  const Recip Rs = sideL ? RsL : RsR;
+  const T vs = sideL ? vsL : vsR;
+  const T ws = sideL ? wsL : wsR;
+  T us[NV];
+  us[RHO] = sideL ? rhoL : rhoR;
+  us[BXn] = bn;
+  us[BXt] = sideL ? bLt : bRt;
+  if constexpr (D == 3) us[BXb] = sideL ? bLb : bRb;
+  us[Xn] = us[RHO] * SM;
+  us[Xt] = us[RHO] * vs;
+  if constexpr (D == 3) us[Xb] = us[RHO] * ws;
+  {
+    T a = vS[Xn] * Bx + vS[Xt] * uS[BXt];
+    if constexpr (D == 3) a = a + vS[Xb] * uS[BXb];
+    T b = SM * Bx + vs * us[BXt];
+    if constexpr (D == 3) b = b + ws * us[BXb];
+    T scrh = a;
+    scrh -= b;
+    us[ENG] = du * uS[ENG] - pt * vS[Xn] + pts * SM + Bx * scrh;
+    us[ENG] = shared_div(us[ENG], s - SM, Rs);
+  }
+  if (dbl) {
+    // double-star state of the chosen side (uss); F += S1 (uss - us)
+    const Recip Rq = shared_recip(sqrL + sqrR);  // divides the four double-star values
+    T vss = sqrL * vsL + sqrR * vsR + times_sign(bRt - bLt, sBx, sBxb);
+    vss = shared_div(vss, sqrL + sqrR, Rq);
+    T wss = T(0);
+    if constexpr (D == 3) {
+      wss = sqrL * wsL + sqrR * wsR + times_sign(bRb - bLb, sBx, sBxb);
       wss = shared_div(wss, sqrL + sqrR, Rq);
     }
-    ussl[Xn] = ussl[RHO] * SM;
-    ussr[Xn] = ussr[RHO] * SM;
-    ussl[Xt] = ussl[RHO] * vss;
-    ussr[Xt] = ussr[RHO] * vss;
+    T uss[NV];
+    uss[RHO] = us[RHO];
+    uss[Xn] = uss[RHO] * SM;
+    uss[Xt] = uss[RHO] * vss;
+    if constexpr (D == 3) uss[Xb] = uss[RHO] * wss;
+    uss[BXn] = Bx;
+    uss[BXt] = sqrL * bRt + sqrR * bLt + times_sign(sqrL * sqrR * (vsR - vsL), sBx, sBxb);
+    uss[BXt] = shared_div(uss[BXt], sqrL + sqrR, Rq);
     if constexpr (D == 3) {
-      ussl[Xb] = ussl[RHO] * wss;
-      ussr[Xb] = ussr[RHO] * wss;
+      uss[BXb] = sqrL * bRb + sqrR * bLb + times_sign(sqrL * sqrR * (wsR - wsL), sBx, sBxb);
+      uss[BXb] = shared_div(uss[BXb], sqrL + sqrR, Rq);
     }
-    ussl[BXn] = ussr[BXn] = Bx;
-    ussl[BXt] = sqrL * usR[BXt] + sqrR * usL[BXt] + times_sign(sqrL * sqrR * (vsR - vsL), sBx, sBxb);
-    ussl[BXt] = shared_div(ussl[BXt], sqrL + sqrR, Rq);
-    ussr[BXt] = ussl[BXt];
-    if constexpr (D == 3) {
-      ussl[BXb] = sqrL * usR[BXb] + sqrR * usL[BXb] + times_sign(sqrL * sqrR * (wsR - wsL), sBx, sBxb);
-      ussl[BXb] = shared_div(ussl[BXb], sqrL + sqrR, Rq);
-      ussr[BXb] = ussl[BXb];
-    }
-    {
-      T a = SM * Bx + vsL * usL[BXt];
-      if constexpr (D == 3) a = a + wsL * usL[BXb];
-      T b = SM * Bx + vss * ussl[BXt];
-      if constexpr (D == 3) b = b + wss * ussl[BXb];
-      scrhL = a;
-      scrhL -= b;
-      a = SM * Bx + vsR * usR[BXt];
-      if constexpr (D == 3) a = a + wsR * usR[BXb];
-      b = SM * Bx + vss * ussr[BXt];
-      if constexpr (D == 3) b = b + wss * ussr[BXb];
-      scrhR = a;
-      scrhR -= b;
-    }
-    ussl[ENG] = usL[ENG] - times_sign(sqrL * scrhL, sBx, sBxb);
-    ussr[ENG] = usR[ENG] + times_sign(sqrR * scrhR, sBx, sBxb);
-    if (ge0(SM)) {
+    T a = SM * Bx + vs * us[BXt];
+    if constexpr (D == 3) a = a + ws * us[BXb];
+    T b = SM * Bx + vss * uss[BXt];
+    if constexpr (D == 3) b = b + wss * uss[BXb];
+    T scrh = a;
+    scrh -= b;
+    // left: usL - sign(Bx) sqrL scrh, right: usR + sign(Bx) sqrR scrh; the
+    // left difference is the sum with the sign-flipped term (IEEE defines
+    // x - y as x + (-y), so the bits are the same)
+    const T sq = sideL ? sqrL : sqrR;
+    const T sgn = sideL ? -sBx : sBx;
+    const uint64_t sgnb = sideL ? (sBxb ^ (1ull << 63)) : sBxb;
+    uss[ENG] = us[ENG] + times_sign(sq * scrh, sgn, sgnb);
+    const T S1 = sideL ? S1L : S1R;
 #pragma unroll
-      for (int n = 0; n < NV; n++) F[n] = fluxL[n] + S1L * (ussl[n] - usL[n]) + sl * (usL[n] - uL[n]);
-    } else {
-#pragma unroll
-      for (int n = 0; n < NV; n++) F[n] = fluxR[n] + S1R * (ussr[n] - usR[n]) + sr * (usR[n] - uR[n]);
-    }
+    for (int n = 0; n < NV; n++) F[n] = F[n] + S1 * (uss[n] - us[n]);
   }
+  // F += s (us - u) of the chosen side: single star F = Fs + s (us - u),
+  // double star F = (Fs + S1 (uss - us)) + s (us - u), the reference's order
+#pragma unroll
+  for (int n = 0; n < NV; n++) F[n] = F[n] + s * (us[n] - uS[n]);
 }
 
 // HLL (hllMHD.hpp:154-453; the Hall whistler term is not part of ideal MHD)
