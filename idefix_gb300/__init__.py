@@ -88,7 +88,7 @@ EXPORTS = [
     "idfx_mlp_eval", "idfx_mlp_feature_range", "idfx_mlp_batch_device", "idfx_mlp_grad_device",
     "idfx_mlp_forward_device", "idfx_learn_coarsen_device", "idfx_measure_fp64_peak",
     "idfx_gpu_autotune", "idfx_gpu_get_segments", "idfx_gpu_set_segments", "idfx_check_division",
-    "idfx_check_conversions", "idfx_check_wait_timeout",
+    "idfx_check_conversions", "idfx_check_wait_timeout", "idfx_check_umma",
     "idfx_dump_write", "idfx_dump_read",
 ]
 
@@ -157,6 +157,8 @@ def load_library(path=LIB_PATH):
     lib.idfx_check_conversions.argtypes = [LL, ctypes.c_ulonglong, ctypes.POINTER(LL)]
     ip = ctypes.POINTER(ctypes.c_int)
     lib.idfx_check_wait_timeout.argtypes = [ctypes.c_int, LL, ip, ip, ip]
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.idfx_check_umma.argtypes = [ctypes.c_int, ctypes.c_int, fp, fp, fp]
     lib.idfx_gpu_get_segments.argtypes = [P, ctypes.POINTER(I)]
     lib.idfx_gpu_set_segments.argtypes = [P, ctypes.POINTER(I)]
     lib.idfx_gpu_set_learned.argtypes = [P, fp, fp, fp]

@@ -328,7 +328,6 @@ void queue_cycle(Engine& e, int use_tstop) {
     const int cons = kSbCons | (e.precision == IDFX_MIXED ? kSbKeepCons : 0);
     launch_stage_begin(e, cons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
     if (e.f.shock) launch_find_shock(e);  // RiemannSolver::CalcFlux (calcFlux.hpp:33)
-    if (g.order == IDFX_LEARNED) launch_learned_recon(e);
     launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
     const int combine = stage > 0;
     const double wc = combine ? e.wc[stage - 1] : 1.0, w0 = combine ? e.w0[stage - 1] : 0.0;
@@ -544,7 +543,6 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
   size_t len = 3 * NV * nc + 2 * g.D * nf + nc  // Vc, Uc, Uc0, Vs, Vs0, InvDt
                + 6 * nc + 3 * nc + 3 * nc + 3 * nc  // face EMFs, sv, cell EMFs, corner EMFs
                + (hll_emf ? 12 * nc : 0)
-               + (g.order == IDFX_LEARNED ? 48 * nc : 0)   // learned face states
                + (cfg->precision == IDFX_MIXED ? (NV * nc + 1) / 2 : 0)   // FP32 primitives
                + (cfg->shock_flattening ? (nc + 7) / 8 : 0);               // shock flags
   int rc = IDFX_OK;
@@ -585,7 +583,6 @@ int idfx_gpu_create(const idfx_gpu_config* cfg, void* stream, idfx_gpu** out) {
     f.dL[d] = hll_emf ? take(nc) : nullptr;
     f.dR[d] = hll_emf ? take(nc) : nullptr;
   }
-  f.ls = (g.order == IDFX_LEARNED) ? take(48 * nc) : nullptr;
   f.Vc32 = (cfg->precision == IDFX_MIXED) ? reinterpret_cast<float*>(take((NV * nc + 1) / 2)) : nullptr;
   f.shock = cfg->shock_flattening ? reinterpret_cast<unsigned char*>(take((nc + 7) / 8)) : nullptr;
   Ctl c{};
@@ -634,7 +631,6 @@ int idfx_gpu_autotune(idfx_gpu* h, int reps) {
   cudaEventCreate(&b);
   const bool prof = e.profile;
   e.profile = false;
-  if (!rc && e.g.order == IDFX_LEARNED) launch_learned_recon(e);
   for (int d = 0; d < e.g.D && !rc; d++) {
     e.only_dir = d;
     // candidates timed in two passes (ascending, then descending), the best
@@ -935,7 +931,6 @@ int idfx_gpu_evolve_stage(idfx_gpu* h, double t, double dt) {
   k_set_stage_dt<<<1, 1, 0, e.stream>>>(e.g, e.ctl, dt);
   if (e.f.Vc32) k_vc32<<<nblocks(e.g.ncell), kThreads, 0, e.stream>>>(e.g, e.f, 2 * e.g.D + 2);
   if (e.f.shock) launch_find_shock(e);
-  if (e.g.order == IDFX_LEARNED) launch_learned_recon(e);
   if (e.g.emf == kEmfContact || e.g.emf == kEmfUct0)
     IDFX_DISPATCH_DE(k_cell_emf_all, nblocks(e.g.ncell), kThreads, e.g, e.f);
   launch_sweeps(e, 2, 0);

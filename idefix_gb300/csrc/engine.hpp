@@ -66,8 +66,10 @@ cudaEvent_t take_event(Engine& e);
 void mark_begin(Engine& e, int cls);
 void mark_end(Engine& e);
 
-// fused learned reconstruction of one stage (ORDER 5) and its release
-void launch_learned_recon(Engine& e);
+// learned sweeps of one stage (ORDER 5: reconstruction with the network's
+// correction, Riemann solve and flux difference in one kernel per
+// direction) and the release of the network
+void launch_learned_sweeps(Engine& e, int invdt, int fold_max);
 void free_learned(Engine& e);
 
 // launches the D flux sweeps of one stage (one function per Riemann solver,

@@ -1,7 +1,9 @@
-// Learned interface-state correction (see learned.cuh): BF16 tensor-core
-// training kernels (forward, backward, Adam), the training-data kernels
-// (coarsening of fine snapshots, batch assembly) and the fused learned
-// reconstruction used by the ORDER 5 sweeps, with their C ABI.
+// Learned interface-state correction (see learned.cuh): BF16 training
+// kernels on the 5th-generation tensor cores (forward, backward; Adam), the
+// training-data kernels (coarsening of fine snapshots, batch assembly) and
+// the learned sweep of the ORDER 5 solver (network inference fused with the
+// reconstruction, the Riemann solve and the flux difference), with their C
+// ABI.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -14,6 +16,7 @@
 #include "../../include/idefix_gb300.h"
 #include "engine.hpp"
 #include "learned.cuh"
+#include "umma.cuh"
 
 using namespace idfx;
 using namespace idfx::learn;
@@ -21,10 +24,15 @@ using namespace idfx::learn;
 namespace {
 
 // ---------------------------------------------------------------------------
-// Generic BF16 GEMM for training: C[M][N] = op(A)[M][K] . op(B)[K][N] with
-// FP32 accumulation, 64x64 block tiles, BK = 32, 4 warps of 32x32.
+// BF16 GEMM of the training on the 5th-generation tensor cores:
+// C[M][N] = op(A)[M][K] . op(B)[K][N], FP32 accumulation in tensor memory.
 // A(m,k) = transA ? A[k*lda + m] : A[m*lda + k]
 // B(k,n) = transB ? B[n*ldb + k] : B[k*ldb + n]
+// CTA tile 128 x N (N <= 128, a multiple of 16); K in chunks of 64 staged
+// in the canonical K-major layout by all threads, two stages (the next chunk
+// is staged while the tensor core works on the current one); one thread
+// issues the MMAs and commits them to the stage's mbarrier; the epilogue
+// reads each row from tensor memory (thread = row).
 // ---------------------------------------------------------------------------
 enum Epi { kEpiF32 = 0, kEpiBiasSilu = 1, kEpiBias = 2, kEpiDsilu = 3 };
 
@@ -37,107 +45,133 @@ struct EpiArgs {
   int ldo;
 };
 
-constexpr int GB_M = 64, GB_N = 64, GB_K = 32, GB_LD = GB_K + 8;
+constexpr int GT_M = 128, GT_N = 128, GT_KC = 64;
+constexpr size_t GT_A = (size_t)GT_M * GT_KC * 2, GT_B = (size_t)GT_N * GT_KC * 2;
+constexpr size_t GT_STAGE = GT_A + GT_B;
+constexpr size_t GT_SMEM = 2 * GT_STAGE + 64;
 
-__global__ void __launch_bounds__(128) k_gemm(int M, int N, int K, const __nv_bfloat16* __restrict__ A, int lda,
-                                              int transA, const __nv_bfloat16* __restrict__ B, int ldb, int transB,
-                                              EpiArgs ep) {
-  __shared__ __align__(16) __nv_bfloat16 As[GB_M * GB_LD];
-  __shared__ __align__(16) __nv_bfloat16 Bs[GB_N * GB_LD];
-  const int m0 = blockIdx.y * GB_M, n0 = blockIdx.x * GB_N;
-  const int warp = threadIdx.x >> 5;
-  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
-  float acc[2][4][4];
-#pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int b = 0; b < 4; b++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
+__global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A,
+                                                    int lda, int transA, const __nv_bfloat16* __restrict__ B,
+                                                    int ldb, int transB, EpiArgs ep, int* status) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * GT_STAGE);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * GT_M, n0 = blockIdx.x * GT_N;
+  const int nt = min(GT_N, N - n0);  // a multiple of 16
+  uint32_t ncols = 32;
+  while ((int)ncols < nt) ncols <<= 1;
+  if (warp == 0) umma::tmem_alloc(slot, ncols);
+  if (tid == 0) {
+    umma::mbar_init1(bar);
+    umma::mbar_init1(bar + 1);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t taddr = *slot;
+  const uint32_t idesc = umma::idesc_bf16_f32(GT_M, nt);
   const __nv_bfloat16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < K; k0 += GB_K) {
-    // stage the tiles: As[m][k], Bs[n][k] (k contiguous)
-    for (int e = threadIdx.x; e < GB_M * GB_K; e += blockDim.x) {
+  const int nq = (K + GT_KC - 1) / GT_KC;
+  bool ok = true;
+  for (int q = 0; q < nq; q++) {
+    const int st = q & 1;
+    if (q >= 2) {  // stage st is free once the MMAs of chunk q - 2 have landed
+      const bool w = umma::mbar_wait_bounded(bar + st, (uint32_t)(((q - 2) >> 1) & 1), umma::kMmaSpin);
+      ok = __syncthreads_and(w);
+      if (!ok) break;
+    }
+    __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(sm + st * GT_STAGE);
+    __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(sm + st * GT_STAGE + GT_A);
+    const int k0 = q * GT_KC;
+    for (int e = tid; e < GT_M * GT_KC; e += blockDim.x) {
       int r, k;
       if (transA) {  // consecutive threads walk m (contiguous in memory)
-        r = e % GB_M;
-        k = e / GB_M;
+        r = e % GT_M;
+        k = e / GT_M;
       } else {
-        r = e / GB_K;
-        k = e % GB_K;
+        r = e / GT_KC;
+        k = e % GT_KC;
       }
       const int gm = m0 + r, gk = k0 + k;
       __nv_bfloat16 v = zero;
       if (gm < M && gk < K) v = transA ? A[(long long)gk * lda + gm] : A[(long long)gm * lda + gk];
-      As[r * GB_LD + k] = v;
+      As[umma::kmajor_offset(r, k, GT_KC) / 2] = v;
     }
-    for (int e = threadIdx.x; e < GB_N * GB_K; e += blockDim.x) {
+    for (int e = tid; e < nt * GT_KC; e += blockDim.x) {
       int n, k;
       if (transB) {
-        n = e / GB_K;
-        k = e % GB_K;
+        n = e / GT_KC;
+        k = e % GT_KC;
       } else {
-        n = e % GB_N;
-        k = e / GB_N;
+        n = e % nt;
+        k = e / nt;
       }
       const int gn = n0 + n, gk = k0 + k;
       __nv_bfloat16 v = zero;
       if (gn < N && gk < K) v = transB ? B[(long long)gn * ldb + gk] : B[(long long)gk * ldb + gn];
-      Bs[n * GB_LD + k] = v;
+      Bs[umma::kmajor_offset(n, k, GT_KC) / 2] = v;
     }
+    umma::fence_async_smem();
     __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < GB_K; kk += 16) {
-      uint32_t af[2][4], bf[4][2];
-#pragma unroll
-      for (int a = 0; a < 2; a++) load_a(af[a], As, GB_LD, wm + 16 * a, kk);
-#pragma unroll
-      for (int b = 0; b < 4; b++) load_b(bf[b], Bs, GB_LD, wn + 8 * b, kk);
-#pragma unroll
-      for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 4; b++) mma_bf16(acc[a][b], af[a], bf[b]);
+    if (tid == 0) {
+      umma::fence_after_sync();
+      umma::mma_tile(taddr, umma::smem_addr(As), umma::smem_addr(Bs), GT_KC, idesc, q > 0);
+      umma::mma_commit(bar + st);
     }
-    __syncthreads();
   }
-  // epilogue: accumulator element (row, col) of the C fragment layout
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  if (ok) {  // the last commit lands after every MMA issued before it
+    const int q = nq - 1;
+    const bool w = umma::mbar_wait_bounded(bar + (q & 1), (uint32_t)((q >> 1) & 1), umma::kMmaSpin);
+    ok = __syncthreads_and(w);
+  }
+  umma::fence_after_sync();
+  if (ok) {
+    const int m = m0 + 32 * warp + lane;
+    for (int c = 0; c < nt; c += 16) {
+      float v[16];
+      umma::tmem_ld16(taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+      if (m >= M) continue;
 #pragma unroll
-  for (int a = 0; a < 2; a++)
-#pragma unroll
-    for (int b = 0; b < 4; b++)
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const int m = m0 + wm + 16 * a + g + ((c & 2) ? 8 : 0);
-        const int n = n0 + wn + 8 * b + 2 * t + (c & 1);
-        if (m >= M || n >= N) continue;
+      for (int i = 0; i < 16; i++) {
+        const int n = n0 + c + i;
+        if (n >= N) continue;
         const long long o = (long long)m * ep.ldo + n;
-        float v = acc[a][b][c];
+        float x = v[i];
         switch (ep.mode) {
           case kEpiF32:
-            ep.out_f[o] = v;
+            ep.out_f[o] = x;
             break;
           case kEpiBiasSilu:
-            v += ep.bias[n];
-            ep.out_f[o] = v;
-            ep.out_b[o] = __float2bfloat16(silu_f(v));
+            x += ep.bias[n];
+            ep.out_f[o] = x;
+            ep.out_b[o] = __float2bfloat16(silu_f(x));
             break;
           case kEpiBias:
-            ep.out_f[o] = v + ep.bias[n];
+            ep.out_f[o] = x + ep.bias[n];
             break;
           default:  // kEpiDsilu
-            v *= dsilu_f(ep.zin[o]);
-            ep.out_f[o] = v;
-            ep.out_b[o] = __float2bfloat16(v);
+            x *= dsilu_f(ep.zin[o]);
+            ep.out_f[o] = x;
+            ep.out_b[o] = __float2bfloat16(x);
             break;
         }
       }
+    }
+  } else if (tid == 0) {
+    atomicExch(status, 1);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(taddr, ncols);
 }
 
+// N a multiple of 16 (every use: NH, NOUT); status: set when a bounded wait
+// of the tensor-core pipeline gave up
 void gemm(cudaStream_t s, int M, int N, int K, const __nv_bfloat16* A, int lda, int transA, const __nv_bfloat16* B,
-          int ldb, int transB, const EpiArgs& ep) {
-  dim3 grid((N + GB_N - 1) / GB_N, (M + GB_M - 1) / GB_M);
-  k_gemm<<<grid, 128, 0, s>>>(M, N, K, A, lda, transA, B, ldb, transB, ep);
+          int ldb, int transB, const EpiArgs& ep, int* status) {
+  dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
+  k_gemm_tc<<<grid, 128, GT_SMEM, s>>>(M, N, K, A, lda, transA, B, ldb, transB, ep, status);
 }
 
 // column sums (bias gradients): out[n] = sum_m in[m][n]
@@ -371,30 +405,50 @@ __global__ void k_make_batch(const float* __restrict__ prims, const float* __res
 }
 
 // ---------------------------------------------------------------------------
-// Fused learned reconstruction (ORDER 5): for every cell with a full 3x3x3
-// stencil and every direction, the PLM (van Leer) states of the cell plus
-// the network's correction, or the plain PLM states where the stencil is
-// outside the trained feature range or a corrected density / pressure is
-// not positive.  Persistent CTAs of 256 threads over tiles of 128 cells; the
-// BF16 weights stay in shared memory, the three layers run on the tensor
-// cores (m16n8k16, FP32 accumulation).
-// ls[(d * 16 + face * 8 + var) * ncell + cell]: face 0 minus, 1 plus.
+// Learned sweep (ORDER 5): reconstruction with the network's correction,
+// Riemann solve and flux difference of one direction in one kernel, over
+// tiles of 128 cells laid along the sweep's pencils (lines of cells along
+// DIR: the active cells plus one ghost cell at each end, for every column
+// of the other two directions including the CT extension).  Per tile:
+//   1. stencil features of the 128 cells (BF16, canonical K-major layout);
+//   2. the three layers on the 5th-generation tensor cores - one thread
+//      issues tcgen05.mma over the shared-memory operands, the FP32
+//      accumulators live in tensor memory, the epilogues (bias, SiLU) read
+//      them back with tcgen05.ld and write the next layer's operand;
+//   3. each cell's PLM (van Leer) states plus the correction, or the plain
+//      PLM states where the stencil is outside the trained feature range or
+//      a corrected density / pressure is not positive (the cell's two faces
+//      together), kept in shared memory;
+//   4. the HLLD solve of every face between two cells of the tile, its EMF
+//      outputs, and the flux difference of every cell with both faces in the
+//      tile (the march's expressions, so that with a zero correction the
+//      sweep is bit-identical to the plain PLM march).
+// Pencils of up to 128 cells are packed whole into a tile; longer pencils
+// are cut into segments of 128 cells that overlap by two (the face between
+// them is solved by both, with the same result).  Persistent CTAs of 256
+// threads, the BF16 weights resident in shared memory.  With states != null
+// the kernel writes the face states ([3][16][ncell]: direction, face
+// (minus / plus) x variable) and stops before the Riemann solves.
 // ---------------------------------------------------------------------------
-constexpr int RT = 128;             // cells per tile
-constexpr int LD1 = K1 + 8;         // row pitch (elements) of K1-wide operands
-constexpr int LD2 = NH + 8;         // row pitch of 128-wide operands
-constexpr int LDY = NOUT + 1;
-constexpr size_t SM_W1 = (size_t)NH * LD1 * 2;
-constexpr size_t SM_W2 = (size_t)NH * LD2 * 2;
-constexpr size_t SM_W3 = (size_t)NOUT * LD2 * 2;
-constexpr size_t SM_X = (size_t)RT * LD1 * 2;
-constexpr size_t SM_H = (size_t)RT * LD2 * 2;
-constexpr size_t SM_Y = (size_t)RT * LDY * 4;
-constexpr size_t SM_B = (size_t)(NH + NH + NOUT) * 4;
-constexpr size_t SM_R = (size_t)2 * NIN * 4;
-constexpr size_t SM_F = (size_t)RT * 4 + 16;
-constexpr size_t SM_LEARN = SM_W1 + SM_W2 + SM_W3 + SM_X + SM_H + SM_Y + SM_B + SM_R + SM_F;
-static_assert(SM_LEARN <= 227 * 1024, "learned reconstruction does not fit in shared memory");
+constexpr int LT = 128;  // cells (rows) per tile
+constexpr size_t LS_W1 = 0;                                  // W1: N 128 x K 224
+constexpr size_t LS_W2 = LS_W1 + (size_t)NH * K1 * 2;        // W2: 128 x 128
+constexpr size_t LS_W3 = LS_W2 + (size_t)NH * NH * 2;        // W3: 16 x 128
+constexpr size_t LS_X = LS_W3 + (size_t)NOUT * NH * 2;       // features 128 x 224 (reused)
+constexpr size_t LS_H = LS_X + (size_t)LT * K1 * 2;          // layer-1 output 128 x 128
+constexpr size_t LS_B = LS_H + (size_t)LT * NH * 2;          // biases
+constexpr size_t LS_R = LS_B + (size_t)(2 * NH + NOUT) * 4;  // trained range
+constexpr size_t LS_F = LS_R + (size_t)2 * NIN * 4;          // per-row fallback flags
+constexpr size_t LS_M = LS_F + (size_t)LT * 4;               // counter, mbarrier, TMEM slot
+constexpr size_t SM_LEARN = LS_M + 32;
+// inside the feature region once the network is done with it
+constexpr size_t LX_Y = 0;                                   // outputs 128 x 16 FP32
+constexpr size_t LX_S = LX_Y + (size_t)LT * NOUT * 4;        // face states 128 x 2 x 8 FP64
+constexpr size_t LX_FA = LX_S + (size_t)LT * 16 * 8;         // flux x area 128 x 5 FP64
+constexpr size_t LX_CM = LX_FA + (size_t)LT * 5 * 8;         // wave speed 128 FP64
+static_assert(LX_CM + (size_t)LT * 8 <= (size_t)LT * K1 * 2, "tile outputs exceed the feature region");
+static_assert(LS_X % 128 == 0 && LS_H % 128 == 0 && LS_W2 % 128 == 0 && LS_W3 % 128 == 0, "operand alignment");
+static_assert(SM_LEARN <= 227 * 1024, "learned sweep does not fit in shared memory");
 
 struct LearnedDev {
   const __nv_bfloat16* W1b;  // [K1][NH]
@@ -405,36 +459,76 @@ struct LearnedDev {
   const float* fmax;
 };
 
-__global__ void __launch_bounds__(256, 1) k_learned_recon(Geo g, const double* __restrict__ Vc, double* __restrict__ ls,
-                                                          LearnedDev L, const Ctl* ctl,
+// tiling of one direction's pencils into tiles of LT cells
+struct LTiles {
+  int L;              // cells per pencil: n[DIR] + 2
+  int per_tile;       // pencils per tile when L <= LT, else 0
+  int nseg;           // segments of LT cells per pencil when L > LT
+  int nA;             // pencils along the first transverse direction (with the CT extension)
+  long long npencil;  // pencils
+  long long ntiles;
+};
+
+__host__ inline LTiles make_tiles(const Geo& g, int dir) {
+  const int A = (dir == 0) ? 1 : 0, B = (dir == 2) ? 1 : 2;
+  LTiles t{};
+  t.L = g.n[dir] + 2;
+  t.nA = g.n[A] + 2 * g.ext;
+  t.npencil = (long long)t.nA * (g.n[B] + 2 * g.ext);
+  if (t.L <= LT) {
+    t.per_tile = LT / t.L;
+    t.nseg = 1;
+    t.ntiles = (t.npencil + t.per_tile - 1) / t.per_tile;
+  } else {
+    t.per_tile = 0;
+    t.nseg = (t.L - 2 + (LT - 2) - 1) / (LT - 2);
+    t.ntiles = t.npencil * t.nseg;
+  }
+  return t;
+}
+
+// element (r, k) of a BF16 operand tile with K columns
+__device__ __forceinline__ void put_bf16(unsigned char* base, int r, int k, int K, float v) {
+  reinterpret_cast<__nv_bfloat16*>(base)[umma::kmajor_offset(r, k, K) / 2] = __float2bfloat16(v);
+}
+
+template <int DIR>
+__global__ void __launch_bounds__(256, 1) k_learned_sweep(Geo g, Fields f, LearnedDev L, const Ctl* ctl, LTiles T,
+                                                          int invdt, int last_dir, double* __restrict__ states,
                                                           unsigned long long* __restrict__ counters) {
-  if (ctl && ctl->done) return;
-  extern __shared__ __align__(16) unsigned char smem[];
-  __nv_bfloat16* W1t = reinterpret_cast<__nv_bfloat16*>(smem);
-  __nv_bfloat16* W2t = reinterpret_cast<__nv_bfloat16*>(smem + SM_W1);
-  __nv_bfloat16* W3t = reinterpret_cast<__nv_bfloat16*>(smem + SM_W1 + SM_W2);
-  __nv_bfloat16* Xs = reinterpret_cast<__nv_bfloat16*>(smem + SM_W1 + SM_W2 + SM_W3);
-  __nv_bfloat16* Hs = reinterpret_cast<__nv_bfloat16*>(smem + SM_W1 + SM_W2 + SM_W3 + SM_X);
-  float* Ys = reinterpret_cast<float*>(smem + SM_W1 + SM_W2 + SM_W3 + SM_X + SM_H);
-  float* bs = reinterpret_cast<float*>(smem + SM_W1 + SM_W2 + SM_W3 + SM_X + SM_H + SM_Y);
-  float* rmin = bs + NH + NH + NOUT;
+  if (ctl->done) return;
+  constexpr int A = (DIR == 0) ? 1 : 0, B = (DIR == 2) ? 1 : 2;
+  using v = Var<3>;
+  extern __shared__ __align__(128) unsigned char sm[];
+  unsigned char* W1s = sm + LS_W1;
+  unsigned char* W2s = sm + LS_W2;
+  unsigned char* W3s = sm + LS_W3;
+  unsigned char* Xs = sm + LS_X;
+  unsigned char* Hs = sm + LS_H;
+  float* bs = reinterpret_cast<float*>(sm + LS_B);
+  float* rmin = reinterpret_cast<float*>(sm + LS_R);
   float* rmax = rmin + NIN;
-  int* flag = reinterpret_cast<int*>(rmax + NIN);
-  int* nfall = flag + RT;
-  __nv_bfloat16* H2s = Xs;  // layer-2 output reuses the input tile
-  const int tid = threadIdx.x;
-  // weights, transposed to [n][k] (k contiguous) for the B operand
+  int* flag = reinterpret_cast<int*>(sm + LS_F);
+  int* nfall = reinterpret_cast<int*>(sm + LS_M);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + LS_M + 8);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(sm + LS_M + 16);
+  float* Ys = reinterpret_cast<float*>(Xs + LX_Y);
+  double* FS = reinterpret_cast<double*>(Xs + LX_S);
+  double* FA = reinterpret_cast<double*>(Xs + LX_FA);
+  double* CM = reinterpret_cast<double*>(Xs + LX_CM);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // weights as the B operands (N x K, K-major): element (n, k) of layer l
   for (int e = tid; e < K1 * NH; e += blockDim.x) {
     const int k = e / NH, n = e % NH;
-    W1t[n * LD1 + k] = L.W1b[e];
+    reinterpret_cast<__nv_bfloat16*>(W1s)[umma::kmajor_offset(n, k, K1) / 2] = L.W1b[e];
   }
   for (int e = tid; e < NH * NH; e += blockDim.x) {
     const int k = e / NH, n = e % NH;
-    W2t[n * LD2 + k] = L.W2b[e];
+    reinterpret_cast<__nv_bfloat16*>(W2s)[umma::kmajor_offset(n, k, NH) / 2] = L.W2b[e];
   }
   for (int e = tid; e < NH * NOUT; e += blockDim.x) {
     const int k = e / NOUT, n = e % NOUT;
-    W3t[n * LD2 + k] = L.W3b[e];
+    reinterpret_cast<__nv_bfloat16*>(W3s)[umma::kmajor_offset(n, k, NH) / 2] = L.W3b[e];
   }
   for (int e = tid; e < NH; e += blockDim.x) {
     bs[e] = L.w[OB1 + e];
@@ -446,159 +540,129 @@ __global__ void __launch_bounds__(256, 1) k_learned_recon(Geo g, const double* _
     rmin[e] = ranged ? L.fmin[e] : 0.f;
     rmax[e] = ranged ? L.fmax[e] : 0.f;
   }
-  const int m0 = g.nt[0] - 2, m1 = g.nt[1] - 2, m2 = g.nt[2] - 2;
-  const long long nr = (long long)m0 * m1 * m2;
-  const long long tiles_per_dir = (nr + RT - 1) / RT;
-  const int warp = tid >> 5, lane = tid & 31, gq = lane >> 2, tq = lane & 3;
-  for (long long tile = blockIdx.x; tile < 3 * tiles_per_dir; tile += gridDim.x) {
-    const int d = (int)(tile / tiles_per_dir);
-    const long long r0 = (tile % tiles_per_dir) * RT;
-    const int slot = tid & (RT - 1), half = tid >> 7;
-    const long long r = r0 + slot;
-    const bool valid = r < nr;
-    int ix[3] = {1, 1, 1};
-    if (valid) {
-      ix[0] = 1 + (int)(r % m0);
-      ix[1] = 1 + (int)((r / m0) % m1);
-      ix[2] = 1 + (int)(r / ((long long)m0 * m1));
+  if (warp == 0) umma::tmem_alloc(slot, 256);  // layer 1: columns 0-127, layer 2: 128-255, layer 3: 0-15
+  if (tid == 0) umma::mbar_init1(bar);
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = *slot;
+  uint32_t phase = 0;
+  bool ok = true;
+  const int row = tid & (LT - 1), half = tid >> 7;
+  const int a1 = (DIR + 1) % 3, a2 = (DIR + 2) % 3;
+  const long long sd = g.s[DIR], s1 = g.s[a1], s2 = g.s[a2];
+  const double dtdV = ctl->dtdV;
+  const double areaT = g.A[DIR];
+  double run_max = 0.0;  // max of InvDt over this thread's cells
+  // one MMA run of a layer, then every thread waits (bounded) for it
+  auto layer = [&](uint32_t d_col, const unsigned char* a, const unsigned char* b, int K, int N) {
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    if (tid == 0) {
+      umma::mma_tile(tmem + d_col, umma::smem_addr(a), umma::smem_addr(b), K, umma::idesc_bf16_f32(LT, N), false);
+      umma::mma_commit(bar);
     }
-    const int a1 = (d + 1) % 3, a2 = (d + 2) % 3;
-    const long long sd = g.s[d], s1 = g.s[a1], s2 = g.s[a2];
+    const bool w = umma::mbar_wait_bounded(bar, phase, umma::kMmaSpin);
+    phase ^= 1u;
+    ok = __syncthreads_and(w) != 0;
+    umma::fence_after_sync();
+  };
+  // hidden-layer epilogue: SiLU(acc + bias) -> BF16 operand of the next layer
+  // (warp w: rows 32 (w % 4) .., columns 64 (w / 4) ..)
+  auto hidden = [&](uint32_t d_col, const float* bias, unsigned char* out) {
+    const int r = 32 * (warp & 3) + lane, c0 = 64 * (warp >> 2);
+    for (int c = c0; c < c0 + 64; c += 16) {
+      float x[16];
+      umma::tmem_ld16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + d_col + (uint32_t)c, x);
+#pragma unroll
+      for (int i = 0; i < 16; i++) put_bf16(out, r, c + i, NH, silu_f(x[i] + bias[c + i]));
+    }
+  };
+  for (long long tile = blockIdx.x; tile < T.ntiles && ok; tile += gridDim.x) {
+    // ---- this thread's row: pencil, cell along DIR, segment ends --------
+    long long pencil;
+    int pos;
+    bool valid, first, last;
+    if (T.per_tile) {
+      const int q = row / T.L;
+      pos = row - q * T.L;
+      pencil = tile * T.per_tile + q;
+      valid = q < T.per_tile && pencil < T.npencil;
+      first = pos == 0;
+      last = pos == T.L - 1;
+    } else {
+      pencil = tile / T.nseg;
+      pos = (int)(tile % T.nseg) * (LT - 2) + row;
+      valid = pos < T.L;
+      first = row == 0;
+      last = row == LT - 1 || pos == T.L - 1;
+    }
+    if (!valid) {
+      pencil = 0;
+      pos = 1;
+    }
+    int ix[3];
+    ix[DIR] = g.beg[DIR] - 1 + pos;
+    ix[A] = g.beg[A] - g.ext + (int)(pencil % T.nA);
+    ix[B] = g.beg[B] - g.ext + (int)(pencil / T.nA);
+    const bool active_col = ix[A] >= g.beg[A] && ix[A] < g.end[A] && ix[B] >= g.beg[B] && ix[B] < g.end[B];
     const long long cc = cidx(g, ix[2], ix[1], ix[0]);
-    __syncthreads();  // previous tile done with flag / Ys / H2s
-    if (tid < RT) flag[tid] = valid ? 0 : 1;
+    if (tid < LT) flag[tid] = valid ? 0 : 1;
     if (tid == 0) *nfall = 0;
     __syncthreads();
-    // ---- stencil features (half 0: rotated vars 0-3, half 1: 4-7) ----
+    // ---- 1. stencil features (half 0: rotated variables 0-3, half 1: 4-7)
     {
       float cen[8];
 #pragma unroll
-      for (int rv = 0; rv < 8; rv++) cen[rv] = (float)Vc[rot_var(rv, d) * g.ncell + cc];
+      for (int rv = 0; rv < 8; rv++) cen[rv] = (float)f.Vc[rot_var(rv, DIR) * g.ncell + cc];
       const float cs = sqrtf((float)g.gamma * cen[4] / cen[0]), sb = sqrtf(cen[0]) * cs;
       int bad = 0;
-      __nv_bfloat16* xr = Xs + slot * LD1;
       for (int q = 0; q < 4; q++) {
         const int rv = half * 4 + q;
-        const double* base = Vc + rot_var(rv, d) * g.ncell + cc;
+        const double* base = f.Vc + rot_var(rv, DIR) * g.ncell + cc;
         for (int o2 = -1; o2 <= 1; o2++)
           for (int o1 = -1; o1 <= 1; o1++)
             for (int o0 = -1; o0 <= 1; o0++) {
               const float sv = valid ? (float)base[o0 * sd + o1 * s1 + o2 * s2] : 0.f;
-              float f;
-              if (rv == 0 || rv == 4) f = sv / cen[rv] - 1.f;
-              else if (rv < 4) f = (sv - cen[rv]) / cs;
-              else f = sv / sb;
+              float x;
+              if (rv == 0 || rv == 4) x = sv / cen[rv] - 1.f;
+              else if (rv < 4) x = (sv - cen[rv]) / cs;
+              else x = sv / sb;
               const int col = rv * 27 + (o2 + 1) * 9 + (o1 + 1) * 3 + (o0 + 1);
-              if (!valid) f = 0.f;
-              if (ranged && !(f >= rmin[col] && f <= rmax[col])) bad = 1;
-              xr[col] = __float2bfloat16(f);
+              if (!valid) x = 0.f;
+              if (ranged && !(x >= rmin[col] && x <= rmax[col])) bad = 1;
+              put_bf16(Xs, row, col, K1, x);
             }
       }
       if (half == 1)
-        for (int col = NIN; col < K1; col++) xr[col] = __float2bfloat16(0.f);
-      if (bad) atomicOr(flag + slot, 1);
+        for (int col = NIN; col < K1; col++) put_bf16(Xs, row, col, K1, 0.f);
+      if (bad) atomicOr(flag + row, 1);
+    }
+    // ---- 2. the network on the tensor cores -----------------------------
+    layer(0, Xs, W1s, K1, NH);  // layer 1 -> TMEM columns 0-127
+    if (!ok) break;
+    hidden(0, bs, Hs);
+    layer(NH, Hs, W2s, NH, NH);  // layer 2 -> TMEM columns 128-255
+    if (!ok) break;
+    hidden(NH, bs + NH, Xs);     // layer-2 output over the features
+    layer(0, Xs, W3s, NH, NOUT);  // layer 3 -> TMEM columns 0-15
+    if (!ok) break;
+    if (warp < 4) {
+      float y[16];
+      umma::tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16), y);
+#pragma unroll
+      for (int i = 0; i < 16; i++) Ys[row * NOUT + i] = y[i] + bs[2 * NH + i];
     }
     __syncthreads();
-    // ---- layer 1: [128 x K1] . [K1 x 128], warp tile 32 x 64 ----
+    // ---- 3. corrected face states (thread: cell row, face = half) -------
     {
-      const int wm = (warp & 3) * 32, wn = (warp >> 2) * 64;
-      float acc[2][8][4];
-#pragma unroll
-      for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 8; b++)
-#pragma unroll
-          for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
-      for (int k0 = 0; k0 < K1; k0 += 16) {
-        uint32_t af[2][4], bf[8][2];
-#pragma unroll
-        for (int a = 0; a < 2; a++) load_a(af[a], Xs, LD1, wm + 16 * a, k0);
-#pragma unroll
-        for (int b = 0; b < 8; b++) load_b(bf[b], W1t, LD1, wn + 8 * b, k0);
-#pragma unroll
-        for (int a = 0; a < 2; a++)
-#pragma unroll
-          for (int b = 0; b < 8; b++) mma_bf16(acc[a][b], af[a], bf[b]);
-      }
-#pragma unroll
-      for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 8; b++)
-#pragma unroll
-          for (int c = 0; c < 4; c++) {
-            const int m = wm + 16 * a + gq + ((c & 2) ? 8 : 0);
-            const int n = wn + 8 * b + 2 * tq + (c & 1);
-            Hs[m * LD2 + n] = __float2bfloat16(silu_f(acc[a][b][c] + bs[n]));
-          }
-    }
-    __syncthreads();
-    // ---- layer 2: [128 x 128] . [128 x 128] -> H2s (over the input tile) ----
-    {
-      const int wm = (warp & 3) * 32, wn = (warp >> 2) * 64;
-      float acc[2][8][4];
-#pragma unroll
-      for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 8; b++)
-#pragma unroll
-          for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
-      for (int k0 = 0; k0 < NH; k0 += 16) {
-        uint32_t af[2][4], bf[8][2];
-#pragma unroll
-        for (int a = 0; a < 2; a++) load_a(af[a], Hs, LD2, wm + 16 * a, k0);
-#pragma unroll
-        for (int b = 0; b < 8; b++) load_b(bf[b], W2t, LD2, wn + 8 * b, k0);
-#pragma unroll
-        for (int a = 0; a < 2; a++)
-#pragma unroll
-          for (int b = 0; b < 8; b++) mma_bf16(acc[a][b], af[a], bf[b]);
-      }
-#pragma unroll
-      for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 8; b++)
-#pragma unroll
-          for (int c = 0; c < 4; c++) {
-            const int m = wm + 16 * a + gq + ((c & 2) ? 8 : 0);
-            const int n = wn + 8 * b + 2 * tq + (c & 1);
-            H2s[m * LD2 + n] = __float2bfloat16(silu_f(acc[a][b][c] + bs[NH + n]));
-          }
-    }
-    __syncthreads();
-    // ---- layer 3: [128 x 128] . [128 x 16], warp tile 16 x 16 ----
-    {
-      const int wm = warp * 16;
-      float acc[2][4];
-#pragma unroll
-      for (int b = 0; b < 2; b++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) acc[b][c] = 0.f;
-      for (int k0 = 0; k0 < NH; k0 += 16) {
-        uint32_t af[4], bf[2][2];
-        load_a(af, H2s, LD2, wm, k0);
-#pragma unroll
-        for (int b = 0; b < 2; b++) load_b(bf[b], W3t, LD2, 8 * b, k0);
-#pragma unroll
-        for (int b = 0; b < 2; b++) mma_bf16(acc[b], af, bf[b]);
-      }
-#pragma unroll
-      for (int b = 0; b < 2; b++)
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const int m = wm + gq + ((c & 2) ? 8 : 0);
-          const int n = 8 * b + 2 * tq + (c & 1);
-          Ys[m * LDY + n] = acc[b][c] + bs[2 * NH + n];
-        }
-    }
-    __syncthreads();
-    // ---- corrected states (thread: cell slot, face = half) ----
-    double st[8];
-    {
-      double cen[8], vl[8], vr[8];
-      const double dxd = g.dx[d];
+      double cen[8], vl[8], vr[8], st[8];
+      const double dxd = g.dx[DIR];
 #pragma unroll
       for (int sv = 0; sv < 8; sv++) {
-        const double* base = Vc + sv * g.ncell + cc;
+        const double* base = f.Vc + sv * g.ncell + cc;
         double w[3];
         w[0] = valid ? base[-sd] : 1.0;
         w[1] = valid ? base[0] : 1.0;
@@ -608,36 +672,95 @@ __global__ void __launch_bounds__(256, 1) k_learned_recon(Geo g, const double* _
       }
       const double cs = sqrt(g.gamma * cen[4] / cen[0]), sb = sqrt(cen[0]) * cs;
       const double sc[8] = {cen[0], cs, cs, cs, cen[4], sb, sb, sb};
-      int bad = 0;
 #pragma unroll
       for (int rv = 0; rv < 8; rv++) {
-        const int sv = rot_var(rv, d);
+        const int sv = rot_var(rv, DIR);
         const double plm = half ? vr[sv] : vl[sv];
         st[sv] = plm;
         if (rv == 5) continue;  // normal field: the face value is used
-        st[sv] = plm + (double)Ys[slot * LDY + half * 8 + rv] * sc[rv];
+        st[sv] = plm + (double)Ys[row * NOUT + half * 8 + rv] * sc[rv];
       }
-      if (!(st[0] > 0.0) || !(st[4] > 0.0)) bad = 1;
-      if (bad) atomicOr(flag + slot, 1);
+      if (!(st[0] > 0.0) || !(st[4] > 0.0)) atomicOr(flag + row, 1);
       __syncthreads();
-      const bool fall = flag[slot] != 0;
+      const bool fall = flag[row] != 0;
       if (fall) {
 #pragma unroll
         for (int sv = 0; sv < 8; sv++) st[sv] = half ? vr[sv] : vl[sv];
       }
-      if (valid) {
 #pragma unroll
-        for (int sv = 0; sv < 8; sv++) ls[((long long)d * 16 + half * 8 + sv) * g.ncell + cc] = st[sv];
-        if (half == 0 && fall) atomicAdd(nfall, 1);
+      for (int sv = 0; sv < 8; sv++) FS[(row * 2 + half) * 8 + sv] = st[sv];
+      if (valid && states) {
+#pragma unroll
+        for (int sv = 0; sv < 8; sv++) states[((long long)DIR * 16 + half * 8 + sv) * g.ncell + cc] = st[sv];
       }
+      if (valid && half == 0 && fall) atomicAdd(nfall, 1);
     }
     __syncthreads();
     if (tid == 0 && counters) {
-      const long long nvalid = (nr - r0 < RT) ? (nr - r0) : RT;
+      long long nvalid;
+      if (T.per_tile) {
+        const long long left = T.npencil - tile * T.per_tile;
+        nvalid = (long long)T.L * (left < T.per_tile ? left : T.per_tile);
+      } else {
+        const long long p0 = (tile % T.nseg) * (LT - 2);
+        nvalid = (T.L - p0 < LT) ? (T.L - p0) : LT;
+      }
       atomicAdd(counters, (unsigned long long)nvalid);
       atomicAdd(counters + 1, (unsigned long long)*nfall);
     }
+    if (states) continue;
+    // ---- 4. Riemann solve of the face between this row and the next -----
+    if (tid < LT && valid && !last) {
+      double vL[8], vR[8];
+#pragma unroll
+      for (int n = 0; n < 8; n++) {
+        vL[n] = FS[(row * 2 + 1) * 8 + n];        // plus-face state of this cell
+        vR[n] = FS[((row + 1) * 2 + 0) * 8 + n];  // minus-face state of the next
+      }
+      int jx[3] = {ix[0], ix[1], ix[2]};
+      jx[DIR] += 1;
+      const long long cn = cidx(g, jx[2], jx[1], jx[0]);  // the face is the next cell's minus face
+      const double bn = f.Vs[DIR * g.nface + fidx(g, jx[2], jx[1], jx[0])];
+      vL[v::BX1 + DIR] = bn;
+      vR[v::BX1 + DIR] = bn;
+      RiemannOut<3, double> r;
+      riemann<3, DIR, kHLLD>(g.gamma, g.rgm1, vL, vR, r);
+      store_emf<3, DIR>(g, f, cn, r, vL, vR);
+      if (active_col) {
+#pragma unroll
+        for (int n = 0; n < v::BX1; n++) FA[row * 5 + n] = r.F[n] * areaT;
+        CM[row] = r.cmax;
+      }
+    }
+    __syncthreads();
+    // ---- flux difference of the cells with both faces in the tile -------
+    if (tid < LT && valid && !first && !last && active_col) {
+#pragma unroll
+      for (int n = 0; n < v::BX1; n++) {
+        const double rhs = -dtdV * (FA[row * 5 + n] - FA[(row - 1) * 5 + n]);
+        f.Uc[n * g.ncell + cc] = f.Uc[n * g.ncell + cc] + rhs;
+      }
+      if (invdt) {
+        const double prev = (invdt == 1) ? 0.0 : f.InvDt[cc];
+        const double inv = prev + div_r(0.5 * (CM[row] + CM[row - 1]), Recip{g.dx[DIR], g.rdx[DIR]});
+        f.InvDt[cc] = inv;
+        if (inv > run_max) run_max = inv;  // NaN never compares greater
+      }
+    }
+    __syncthreads();  // the feature region is rewritten by the next tile
   }
+  if (!ok && tid == 0) report_wait_timeout(ctl);
+  if (last_dir && invdt && !states) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double w = __shfl_xor_sync(0xffffffffu, run_max, o);
+      if (w > run_max) run_max = w;
+    }
+    if (lane == 0 && run_max > 0.0) atomic_max_pos((unsigned long long*)&((Ctl*)ctl)->invdt_max_bits, run_max);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(tmem, 256);
 }
 
 __global__ void k_sumsq_targets(const float* __restrict__ T, int B, double* __restrict__ out) {
@@ -656,6 +779,56 @@ __global__ void k_init_keys(unsigned* kmin, unsigned* kmax) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Self-check of the tcgen05 building blocks (umma.cuh): one CTA of 128
+// threads computes D[128][N] = A[128][K] . B[N][K]^T with BF16 operands staged
+// in the canonical K-major layout, the FP32 accumulator in TMEM, and writes D
+// from TMEM to global memory.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128, 1) k_umma_check(int N, int K, const __nv_bfloat16* __restrict__ A,
+                                                       const __nv_bfloat16* __restrict__ B, float* __restrict__ D,
+                                                       int* status) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(sm);
+  __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(sm + 128 * K * 2);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 128 * K * 2 + N * K * 2);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int e = tid; e < 128 * K; e += blockDim.x)
+    As[umma::kmajor_offset(e / K, e % K, K) / 2] = A[e];
+  for (int e = tid; e < N * K; e += blockDim.x)
+    Bs[umma::kmajor_offset(e / K, e % K, K) / 2] = B[e];
+  uint32_t ncols = 32;
+  while ((int)ncols < N) ncols *= 2;
+  if (warp == 0) umma::tmem_alloc(slot, ncols);
+  if (tid == 0) umma::mbar_init1(bar);
+  umma::fence_async_smem();
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t taddr = *slot;
+  if (tid == 0) {
+    umma::mma_tile(taddr, umma::smem_addr(As), umma::smem_addr(Bs), K, umma::idesc_bf16_f32(128, N), false);
+    umma::mma_commit(bar);
+  }
+  const bool ok = umma::mbar_wait_bounded(bar, 0, umma::kMmaSpin);
+  umma::fence_after_sync();
+  if (ok) {
+    const int row = 32 * warp + lane;
+    for (int c = 0; c < N; c += 16) {
+      float v[16];
+      umma::tmem_ld16(taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+#pragma unroll
+      for (int i = 0; i < 16; i++) D[row * N + c + i] = v[i];
+    }
+  } else if (lane == 0) {
+    atomicExch(status, 1);
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) umma::tmem_dealloc(taddr, ncols);
+}
+
 }  // namespace
 
 // the network as the engine holds it (ORDER 5)
@@ -669,19 +842,31 @@ struct LearnedModel {
 
 namespace idfx {
 
-void launch_learned_recon(Engine& e) {
+// the learned sweeps of one stage, direction after direction (the same
+// InvDt modes as the march: 1 first contribution, 2 accumulate; the last
+// direction folds the CFL maximum); states: face states instead (see
+// k_learned_sweep)
+static void launch_learned(Engine& e, int invdt, int fold_max, double* states) {
   LearnedModel* m = static_cast<LearnedModel*>(e.learned);
   LearnedDev L{m->W1b, m->W2b, m->W3b, m->w, m->ranged ? m->fmin : nullptr, m->ranged ? m->fmax : nullptr};
   int dev = 0, sms = 148;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const long long nr = (long long)(e.g.nt[0] - 2) * (e.g.nt[1] - 2) * (e.g.nt[2] - 2);
-  const long long tiles = 3 * ((nr + RT - 1) / RT);
-  const int grid = (int)(tiles < sms ? tiles : sms);
-  mark_begin(e, kKLearned);
-  k_learned_recon<<<grid, 256, SM_LEARN, e.stream>>>(e.g, e.f.Vc, e.f.ls, L, e.ctl, m->counters);
-  mark_end(e);
+  for (int d = 0; d < 3; d++) {
+    if (e.only_dir >= 0 && e.only_dir != d) continue;
+    const LTiles T = make_tiles(e.g, d);
+    const int grid = (int)(T.ntiles < sms ? T.ntiles : sms);
+    const int inv = (invdt == 0) ? 0 : (d == 0 ? invdt : 2);
+    const int last = fold_max && d == 2;
+    mark_begin(e, kKSweepX + d);
+    if (d == 0) k_learned_sweep<0><<<grid, 256, SM_LEARN, e.stream>>>(e.g, e.f, L, e.ctl, T, inv, last, states, m->counters);
+    if (d == 1) k_learned_sweep<1><<<grid, 256, SM_LEARN, e.stream>>>(e.g, e.f, L, e.ctl, T, inv, last, states, m->counters);
+    if (d == 2) k_learned_sweep<2><<<grid, 256, SM_LEARN, e.stream>>>(e.g, e.f, L, e.ctl, T, inv, last, states, m->counters);
+    mark_end(e);
+  }
 }
+
+void launch_learned_sweeps(Engine& e, int invdt, int fold_max) { launch_learned(e, invdt, fold_max, nullptr); }
 
 void free_learned(Engine& e) {
   LearnedModel* m = static_cast<LearnedModel*>(e.learned);
@@ -711,6 +896,7 @@ struct idfx_mlp {
   float *T = nullptr, *Z1 = nullptr, *Z2 = nullptr, *Y = nullptr, *dYf = nullptr, *dZ2f = nullptr, *dZ1f = nullptr;
   double* loss = nullptr;
   unsigned *kmin = nullptr, *kmax = nullptr;
+  int* status = nullptr;  // set by a GEMM whose bounded tensor-core wait gave up
   const float* prims = nullptr;
   const float* tgt = nullptr;
   int nsnap = 0, nc = 0;
@@ -730,24 +916,29 @@ bool dalloc(idfx_mlp* h, P** p, size_t n) {
 // forward + loss + backward of one batch held in h->X / h->T (loss added to *loss)
 void fwd_bwd(idfx_mlp* h, int B, double* loss) {
   cudaStream_t s = h->stream;
-  gemm(s, B, NH, K1, h->X, K1, 0, h->W1b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH});
-  gemm(s, B, NH, NH, h->H1, NH, 0, h->W2b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH});
-  gemm(s, B, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0, EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT});
+  gemm(s, B, NH, K1, h->X, K1, 0, h->W1b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status);
+  gemm(s, B, NH, NH, h->H1, NH, 0, h->W2b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status);
+  gemm(s, B, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0, EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT}, h->status);
   const int ne = B * NOUT;
   k_loss<<<(ne + 255) / 256, 256, 0, s>>>(h->Y, h->T, B, h->dYf, h->dYb, loss);
-  gemm(s, NH, NOUT, B, h->H2, NH, 1, h->dYb, NOUT, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW3, nullptr, NOUT});
+  gemm(s, NH, NOUT, B, h->H2, NH, 1, h->dYb, NOUT, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW3, nullptr, NOUT}, h->status);
   k_colsum<<<NOUT, 256, 0, s>>>(h->dYf, B, NOUT, h->g + OB3);
-  gemm(s, B, NH, NOUT, h->dYb, NOUT, 0, h->W3b, NOUT, 1, EpiArgs{kEpiDsilu, nullptr, h->Z2, h->dZ2f, h->dZ2b, NH});
-  gemm(s, NH, NH, B, h->H1, NH, 1, h->dZ2b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW2, nullptr, NH});
+  gemm(s, B, NH, NOUT, h->dYb, NOUT, 0, h->W3b, NOUT, 1, EpiArgs{kEpiDsilu, nullptr, h->Z2, h->dZ2f, h->dZ2b, NH}, h->status);
+  gemm(s, NH, NH, B, h->H1, NH, 1, h->dZ2b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW2, nullptr, NH}, h->status);
   k_colsum<<<NH, 256, 0, s>>>(h->dZ2f, B, NH, h->g + OB2);
-  gemm(s, B, NH, NH, h->dZ2b, NH, 0, h->W2b, NH, 1, EpiArgs{kEpiDsilu, nullptr, h->Z1, h->dZ1f, h->dZ1b, NH});
-  gemm(s, NIN, NH, B, h->X, K1, 1, h->dZ1b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW1, nullptr, NH});
+  gemm(s, B, NH, NH, h->dZ2b, NH, 0, h->W2b, NH, 1, EpiArgs{kEpiDsilu, nullptr, h->Z1, h->dZ1f, h->dZ1b, NH}, h->status);
+  gemm(s, NIN, NH, B, h->X, K1, 1, h->dZ1b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW1, nullptr, NH}, h->status);
   k_colsum<<<NH, 256, 0, s>>>(h->dZ1f, B, NH, h->g + OB1);
 }
 
 int sync_ok(idfx_mlp* h) {
   if (cudaGetLastError() != cudaSuccess) return IDFX_ERR_CUDA;
-  return cudaStreamSynchronize(h->stream) == cudaSuccess ? IDFX_OK : IDFX_ERR_CUDA;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return IDFX_ERR_CUDA;
+  if (h->status) {  // a bounded tensor-core wait that gave up
+    int st = 0;
+    if (cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess || st) return IDFX_ERR_CUDA;
+  }
+  return IDFX_OK;
 }
 
 }  // namespace
@@ -773,8 +964,12 @@ int idfx_gpu_set_learned(idfx_gpu* hg, const float* params, const float* fmin, c
     ok = ok && cudaMalloc(&m->fmin, sizeof(float) * NIN) == cudaSuccess;
     ok = ok && cudaMalloc(&m->fmax, sizeof(float) * NIN) == cudaSuccess;
     ok = ok && cudaMalloc(&m->counters, sizeof(unsigned long long) * 2) == cudaSuccess;
-    ok = ok && cudaFuncSetAttribute(k_learned_recon, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SM_LEARN) ==
-                   cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(k_learned_sweep<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)SM_LEARN) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(k_learned_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)SM_LEARN) == cudaSuccess;
+    ok = ok && cudaFuncSetAttribute(k_learned_sweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)SM_LEARN) == cudaSuccess;
     if (!ok) {
       free_learned(e);
       e.err = "set_learned: CUDA allocation failed";
@@ -799,12 +994,18 @@ int idfx_gpu_learned_states(idfx_gpu* hg, double* ls) {
   if (!hg || !ls || !hg->e.learned) return IDFX_ERR_STATE;
   Engine& e = hg->e;
   if (idfx_gpu_set_boundaries(hg) != IDFX_OK) return IDFX_ERR_CUDA;
-  launch_learned_recon(e);
   const size_t n = (size_t)48 * e.g.ncell;
-  if (cudaMemcpyAsync(ls, e.f.ls, n * sizeof(double), cudaMemcpyDeviceToHost, e.stream) != cudaSuccess ||
-      cudaStreamSynchronize(e.stream) != cudaSuccess)
-    return IDFX_ERR_CUDA;
-  return IDFX_OK;
+  double* tmp = nullptr;
+  if (cudaMalloc(&tmp, n * sizeof(double)) != cudaSuccess) return IDFX_ERR_CUDA;
+  bool ok = cudaMemsetAsync(tmp, 0, n * sizeof(double), e.stream) == cudaSuccess;
+  if (ok) {
+    launch_learned(e, 0, 0, tmp);
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  ok = ok && cudaMemcpyAsync(ls, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, e.stream) == cudaSuccess;
+  ok = ok && cudaStreamSynchronize(e.stream) == cudaSuccess;
+  cudaFree(tmp);
+  return ok ? IDFX_OK : IDFX_ERR_CUDA;
 }
 
 int idfx_gpu_learned_stats(idfx_gpu* hg, long long* cells, long long* fallbacks) {
@@ -818,6 +1019,37 @@ int idfx_gpu_learned_stats(idfx_gpu* hg, long long* cells, long long* fallbacks)
   if (cells) *cells = (long long)c[0];
   if (fallbacks) *fallbacks = (long long)c[1];
   return IDFX_OK;
+}
+
+int idfx_check_umma(int N, int K, const float* A, const float* B, float* D) {
+  if (!A || !B || !D || N < 16 || N > 256 || N % 16 || K < 16 || K > 256 || K % 16) return IDFX_ERR_CONFIG;
+  std::vector<__nv_bfloat16> a((size_t)128 * K), b((size_t)N * K);
+  for (size_t i = 0; i < a.size(); i++) a[i] = __float2bfloat16(A[i]);
+  for (size_t i = 0; i < b.size(); i++) b[i] = __float2bfloat16(B[i]);
+  __nv_bfloat16 *da = nullptr, *db = nullptr;
+  float* dd = nullptr;
+  int* dst = nullptr;
+  int st = 0;
+  const size_t smem = (size_t)128 * K * 2 + (size_t)N * K * 2 + 16;
+  bool ok = cudaMalloc(&da, a.size() * 2) == cudaSuccess && cudaMalloc(&db, b.size() * 2) == cudaSuccess &&
+            cudaMalloc(&dd, (size_t)128 * N * 4) == cudaSuccess && cudaMalloc(&dst, sizeof(int)) == cudaSuccess;
+  ok = ok && cudaMemcpy(da, a.data(), a.size() * 2, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok = ok && cudaMemcpy(db, b.data(), b.size() * 2, cudaMemcpyHostToDevice) == cudaSuccess;
+  ok = ok && cudaMemset(dst, 0, sizeof(int)) == cudaSuccess && cudaMemset(dd, 0, (size_t)128 * N * 4) == cudaSuccess;
+  ok = ok && cudaFuncSetAttribute(k_umma_check, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+                 cudaSuccess;
+  if (ok) {
+    k_umma_check<<<1, 128, smem>>>(N, K, da, db, dd, dst);
+    ok = cudaGetLastError() == cudaSuccess && cudaDeviceSynchronize() == cudaSuccess;
+  }
+  ok = ok && cudaMemcpy(D, dd, (size_t)128 * N * 4, cudaMemcpyDeviceToHost) == cudaSuccess;
+  ok = ok && cudaMemcpy(&st, dst, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dd);
+  cudaFree(dst);
+  if (!ok) return IDFX_ERR_CUDA;
+  return st ? IDFX_ERR_CUDA : IDFX_OK;
 }
 
 int idfx_mlp_create(int max_batch, void* stream, idfx_mlp** out) {
@@ -843,7 +1075,9 @@ int idfx_mlp_create(int max_batch, void* stream, idfx_mlp** out) {
             dalloc(h, &h->dZ1b, B * NH) && dalloc(h, &h->T, B * NOUT) && dalloc(h, &h->Z1, B * NH) &&
             dalloc(h, &h->Z2, B * NH) && dalloc(h, &h->Y, B * NOUT) && dalloc(h, &h->dYf, B * NOUT) &&
             dalloc(h, &h->dZ2f, B * NH) && dalloc(h, &h->dZ1f, B * NH) && dalloc(h, &h->loss, 2) &&
-            dalloc(h, &h->kmin, NIN) && dalloc(h, &h->kmax, NIN);
+            dalloc(h, &h->kmin, NIN) && dalloc(h, &h->kmax, NIN) && dalloc(h, &h->status, 1);
+  ok = ok && cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_SMEM) ==
+                 cudaSuccess;
   if (ok) {
     k_init_keys<<<1, 256, 0, h->stream>>>(h->kmin, h->kmax);
     ok = sync_ok(h) == IDFX_OK;
@@ -939,11 +1173,11 @@ int idfx_mlp_eval(idfx_mlp* h, int batch, unsigned long long seed, double* loss,
   k_make_batch<<<(batch + 127) / 128, 128, 0, h->stream>>>(h->prims, h->tgt, h->nsnap, h->nc, (float)h->gamma, seed,
                                                            0, batch, h->X, h->T, nullptr, nullptr);
   gemm(h->stream, batch, NH, K1, h->X, K1, 0, h->W1b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH});
+       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status);
   gemm(h->stream, batch, NH, NH, h->H1, NH, 0, h->W2b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH});
+       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status);
   gemm(h->stream, batch, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0,
-       EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT});
+       EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT}, h->status);
   const int ne = batch * NOUT;
   k_loss<<<(ne + 255) / 256, 256, 0, h->stream>>>(h->Y, h->T, batch, h->dYf, h->dYb, h->loss);
   k_sumsq_targets<<<(ne + 255) / 256, 256, 0, h->stream>>>(h->T, batch, h->loss + 1);
@@ -986,11 +1220,11 @@ int idfx_mlp_forward_device(idfx_mlp* h, const void* X, int batch, float* Y) {
   if (!h || !X || !Y || batch < 1 || batch > h->max_batch) return IDFX_ERR_STATE;
   cudaMemcpyAsync(h->X, X, sizeof(__nv_bfloat16) * (size_t)batch * K1, cudaMemcpyDeviceToDevice, h->stream);
   gemm(h->stream, batch, NH, K1, h->X, K1, 0, h->W1b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH});
+       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status);
   gemm(h->stream, batch, NH, NH, h->H1, NH, 0, h->W2b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH});
+       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status);
   gemm(h->stream, batch, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0, EpiArgs{kEpiBias, h->w + OB3, nullptr, Y, nullptr,
-                                                                           NOUT});
+                                                                           NOUT}, h->status);
   return sync_ok(h);
 }
 

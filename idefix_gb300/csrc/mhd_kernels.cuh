@@ -76,7 +76,6 @@ struct Fields {
   double *Ex1, *Ex2, *Ex3;
   double *ex, *ey, *ez;
   double *aL[3], *aR[3], *dL[3], *dR[3];
-  double* ls;   // learned face states [3][16][ncell] (ORDER 5)
   float* Vc32;  // FP32 copy of Vc read by the mixed-precision sweeps (else null)
   unsigned char* shock;  // FlagShock per cell when shock flattening is on (else null)
 };
@@ -692,14 +691,9 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
       } else {
         w[n][W - 1] = vcT[n * g.ncell + cc + H * sd];
       }
-      if constexpr (ORDER == 5) {  // states of the fused learned reconstruction
-        vl[n] = (T)f.ls[((long long)DIR * 16 + n) * g.ncell + cc];
-        vr[n] = (T)f.ls[((long long)DIR * 16 + 8 + n) * g.ncell + cc];
-      } else {
-        // FP64: odd variables' limiter quotient on the integer pipe
-        Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk, l3,
-                           sizeof(T) == 8 && (n & 1));
-      }
+      // FP64: odd variables' limiter quotient on the integer pipe
+      Recon<ORDER>::cell(w[n], dxd, n == v::RHO || n == v::PRS, vl[n], vr[n], shk, l3,
+                         sizeof(T) == 8 && (n & 1));
     }
     if (c >= m0) {
       T vL[NV], vR[NV];

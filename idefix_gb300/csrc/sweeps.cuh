@@ -62,8 +62,8 @@ void launch_sweeps_solver(Engine& e, int invdt, int fold_max) {
   IDFX_CASE(2, 1) IDFX_CASE(2, 2) IDFX_CASE(2, 3) IDFX_CASE(2, 4)
   IDFX_CASE(3, 1) IDFX_CASE(3, 2) IDFX_CASE(3, 3) IDFX_CASE(3, 4)
 #undef IDFX_CASE
-  if constexpr (SOLVER == kHLLD)  // learned reconstruction: 3-D, HLLD, FP64
-    if (D == 3 && O == 5) launch_sweeps_tt<3, 5, SOLVER, double>(e, invdt, fold_max);
+  if constexpr (SOLVER == kHLLD)  // learned reconstruction: 3-D, HLLD, FP64 (learned.cu)
+    if (D == 3 && O == 5) launch_learned_sweeps(e, invdt, fold_max);
 }
 
 // ---------------------------------------------------------------------------

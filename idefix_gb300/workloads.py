@@ -225,7 +225,7 @@ def _coarse_of(Vc, Vs, n, r, learned):
 def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=(200, 201, 202, 203),
                 nsnap=50, t_end=1.0, steps=3000, batch=8192, lr=2e-3, lr_end=2e-5,
                 train_precision="mixed", kmax=None, params=None, alphas=(0.25, 0.5, 0.75, 1.0),
-                val_seeds=(300, 301), log=sys.stderr):
+                val_seeds=(300, 301), truth=2, log=sys.stderr):
     """kmax: largest wavenumber of the initial fields; by default 8 x n_fine
     / 512, i.e. the spectrum of the 512^3 fine run scaled with the grid, so
     that the coarse grid resolves it as the 128^3 coarse grid of the
@@ -233,7 +233,12 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
     skips data generation and training.  alphas: candidate scale factors of
     the network's correction (the output layer is linear, so alpha scales W3
     and b3); the one with the lowest error on the validation seeds is used
-    on the held-out seeds."""
+    on the held-out seeds.  truth: the errors are measured against a run
+    `truth` times finer than the fine grid (mixed precision: its own error
+    against FP64, ~1e-5, is far below the errors measured), coarsened to the
+    coarse grid, so that the plain fine run has an error of its own; every
+    run starts from the truth's initial state coarsened to its grid.
+    truth = 1: the plain fine FP64 run is the reference (its error is 0)."""
     import torch
 
     from idefix_gb300 import learned
@@ -295,15 +300,34 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
     held_p, held_t = [], []
 
     def evaluate(s, alist, plain=True):
-        Vc, Vs = ic.turbulence_3d(n_fine, seed=s, kmax=kmax)
+        row = {"seed": s}
+        if truth > 1:
+            nt = n_fine * truth
+            Tc, Ts = ic.turbulence_3d(nt, seed=s, kmax=kmax)
+            tb = ig.GpuBlock(3, (nt,) * 3, cfl=0.6, first_dt=1e-4, precision="mixed")
+            tb.upload(Tc, Ts)
+            row["truth_s"] = _timed_run(tb, t_end)
+            tv = tb.download()
+            tb.close()
+            ref_d = _coarse_of(*tv, nt, nt // nc, learned)[0]
+            pf, ff = _coarse_of(Tc, Ts, nt, truth, learned)
+            Vc, Vs = learned.coarse_state(pf, ff)  # the fine run's initial state
+            del tv, Tc, Ts
+        else:
+            Vc, Vs = ic.turbulence_3d(n_fine, seed=s, kmax=kmax)
         fine = ig.GpuBlock(3, (n_fine,) * 3, cfl=0.6, first_dt=1e-4)
         fine.upload(Vc, Vs)
-        t_fine = _timed_run(fine, t_end)
+        row["fine_s"] = _timed_run(fine, t_end)
         fv = fine.download()
-        ref_d, _, tg_d = learned.coarsen(torch.from_numpy(fv[0]).cuda(), torch.from_numpy(fv[1]).cuda(), n_fine, 2, r)
-        ref = ref_d.cpu().numpy()
+        fine_d, _, tg_d = learned.coarsen(torch.from_numpy(fv[0]).cuda(), torch.from_numpy(fv[1]).cuda(), n_fine, 2,
+                                          r)
         fine.close()
-        row = {"seed": s, "fine_s": t_fine}
+        if truth > 1:
+            row["fine_l1"] = _l1(fine_d.cpu().numpy(), ref_d.cpu().numpy())
+            row["fine_l1_vars"] = _l1_vars(fine_d.cpu().numpy(), ref_d.cpu().numpy())
+        else:
+            ref_d = fine_d
+        ref = ref_d.cpu().numpy()
         runs = [("plain", "plm", nc, 0.0)] if plain else []
         runs += [(f"learned_a{a:g}", "learned", nc, a) for a in alist]
         runs += [("plain_2x", "plm", 2 * nc, 0.0)] if plain else []
@@ -358,6 +382,15 @@ def run_learned(n_fine=128, r=4, train_seeds=tuple(range(100, 140)), eval_seeds=
     res["learned_over_plain_2x_l1"] = res["learned_l1"] / res["plain_2x_l1"]
     res["fine_over_learned_time"] = res["fine_s"] / res["learned_s"]
     res["plain_2x_over_learned_time"] = res["plain_2x_s"] / res["learned_s"]
+    if truth > 1:
+        # the spec criterion: learned coarse L1 within 1.5x of the plain
+        # fine run's L1, at >= 10x lower wall time
+        res["truth_factor"] = truth
+        res["learned_over_fine_l1"] = res["learned_l1"] / res["fine_l1"]
+        res["target_l1_ratio"] = 1.5
+        res["target_time_ratio"] = 10.0
+        res["meets_l1_target"] = bool(res["learned_over_fine_l1"] <= 1.5)
+        res["meets_time_target"] = bool(res["fine_over_learned_time"] >= 10.0)
     return res, params, fmin, fmax
 
 
@@ -378,6 +411,7 @@ if __name__ == "__main__":
     ap.add_argument("--save", default=None, help="npz file for the trained parameters and range")
     ap.add_argument("--load", default=None, help="npz file of a trained network (skips training)")
     ap.add_argument("--alphas", default="0.25,0.5,0.75,1.0", help="comma-separated correction scale factors")
+    ap.add_argument("--truth", type=int, default=2, help="reference run this many times finer than the fine grid")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cycles", type=int, default=None, help="default: 500 (ensemble), 200 (lowbeta)")
     ap.add_argument("--no-check", action="store_true")
@@ -398,7 +432,7 @@ if __name__ == "__main__":
             pre = (z["params"], z["fmin"], z["fmax"])
         r, params, fmin, fmax = run_learned(a.n_fine, train_seeds=tuple(range(100, 100 + a.train_runs)),
                                             nsnap=a.snapshots, t_end=a.t_end, steps=a.steps, params=pre,
-                                            alphas=tuple(float(x) for x in a.alphas.split(",")))
+                                            alphas=tuple(float(x) for x in a.alphas.split(",")), truth=a.truth)
         if a.save:
             np.savez(a.save, params=params, fmin=fmin, fmax=fmax)
     print(json.dumps(r))

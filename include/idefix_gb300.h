@@ -181,6 +181,12 @@ int idfx_check_conversions(long long n, unsigned long long seed, long long* mism
  * the control block's status / done words that its give-up path leaves
  * (IDFX_ERR_CUDA and 1 after a timeout).  The context stays usable. */
 int idfx_check_wait_timeout(int mode, long long limit, int* gave_up, int* status, int* done);
+/* self-check of the 5th-generation tensor-core path of the learned
+ * correction (no counterpart in the reference): D[128][N] = A[128][K] .
+ * B[N][K]^T with A and B rounded to BF16, FP32 accumulation in tensor memory
+ * (tcgen05.mma / tcgen05.ld); host arrays, row-major; N, K multiples of 16 in
+ * 16..256 */
+int idfx_check_umma(int N, int K, const float* A, const float* B, float* D);
 
 /* Allocation-free Fluid::EvolveStage — no counterpart in the reference.
  * For callers that may not allocate GPU memory while they step (state held
