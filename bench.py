@@ -45,8 +45,8 @@ BYTES_PER_ZONE_CYCLE = 320.0  # 8 FP64 state values x 5 transfers per RK2 cycle
 # active cell of one sweep launch: ncu on the 128^3 case of this workload
 # (stage 0, the three sweep launches of the first warm-up cycle).  Both scale with the
 # cells processed; at 256^3 the CT-extension columns add 1.6 % instead of 3.1 %.
-FP64_INST_PER_CELL = {"sweep_x": 578.6, "sweep_y": 567.9, "sweep_z": 572.2}
-DRAM_BYTES_PER_CELL = {"sweep_x": 193.3, "sweep_y": 172.7, "sweep_z": 171.7}
+FP64_INST_PER_CELL = {"sweep_x": 539.1, "sweep_y": 526.2, "sweep_z": 532.8}
+DRAM_BYTES_PER_CELL = {"sweep_x": 193.7, "sweep_y": 172.6, "sweep_z": 171.7}
 # FP64 operations per active zone and RK2 cycle of the reference algorithm on
 # this workload at 256^3, each add/sub, mul, div and sqrt counted once
 # (1465.5 + 1662.8 + 215.5 + 35.8): the operation-counting build of the CPU

@@ -82,7 +82,7 @@ EXPORTS = [
     "idfx_ens_create", "idfx_ens_destroy", "idfx_ens_last_error", "idfx_ens_sizes",
     "idfx_ens_upload_prim", "idfx_ens_download_prim", "idfx_ens_get_time", "idfx_ens_run",
     "idfx_ens_autotune", "idfx_ens_get_segments", "idfx_ens_set_schedule",
-    "idfx_ens_download_prim_device",
+    "idfx_ens_download_prim_device", "idfx_ens_persistent_info",
     "idfx_gpu_set_learned", "idfx_gpu_learned_states", "idfx_gpu_learned_stats", "idfx_mlp_create", "idfx_mlp_destroy",
     "idfx_mlp_set_params", "idfx_mlp_get_params", "idfx_mlp_set_dataset_device", "idfx_mlp_train",
     "idfx_mlp_eval", "idfx_mlp_feature_range", "idfx_mlp_batch_device", "idfx_mlp_grad_device",
@@ -143,6 +143,7 @@ def load_library(path=LIB_PATH):
     lib.idfx_ens_download_prim.argtypes = [P, I, P, P]
     lib.idfx_ens_get_time.argtypes = [P, I, dp, dp, ctypes.POINTER(LL), ctypes.POINTER(I)]
     lib.idfx_ens_run.argtypes = [P, D, LL, I]
+    lib.idfx_ens_persistent_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
     lib.idfx_ens_autotune.argtypes = [P, I]
     lib.idfx_ens_get_segments.argtypes = [P, I, ctypes.POINTER(I)]
     lib.idfx_ens_set_schedule.argtypes = [P, I]
@@ -579,8 +580,18 @@ class Ensemble:
                                                ctypes.byref(nc), ctypes.byref(st)))
         return t.value, dt.value, nc.value, st.value
 
-    def run(self, tstop=-1.0, max_cycles=-1, graph=True):
-        self._check(self.lib.idfx_ens_run(self.h, float(tstop), int(max_cycles), 1 if graph else 0))
+    def run(self, tstop=-1.0, max_cycles=-1, graph=True, persistent=False):
+        """persistent: every chunk of cycles as one persistent launch (grid
+        barrier between phases); else one CUDA graph of batched launches per
+        cycle (graph=True) or the launches queued one by one"""
+        mode = 2 if persistent else (1 if graph else 0)
+        self._check(self.lib.idfx_ens_run(self.h, float(tstop), int(max_cycles), mode))
+
+    def persistent_info(self):
+        """(co-resident blocks of the persistent launch, replayed from a graph)"""
+        b, g = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.idfx_ens_persistent_info(self.h, ctypes.byref(b), ctypes.byref(g)))
+        return b.value, bool(g.value)
 
     def write_dump(self, path, vtk_file_number=0):
         """Restart dump of the current state in the reference's format."""

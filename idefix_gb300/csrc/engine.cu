@@ -271,6 +271,19 @@ void launch_stage_begin(Engine& e, int flags) {
   IDFX_DISPATCH_DE(k_stage_begin, nblocks(e.g.ncell), kThreads, e.g, e.f, e.ctl, flags);
   mark_end(e);
 }
+// the ghost cells alone (mixed path, periodic block, after a stage end that
+// wrote the active cells' outputs)
+void launch_stage_ghosts(Engine& e, int flags) {
+  long long slab = 0;
+  for (int d = 0; d < e.g.D; d++) {
+    const int a = (d == 0) ? 1 : 0, b = (d == 2) ? 1 : 2;
+    const long long n = 2LL * e.g.ng * e.g.nt[a] * e.g.nt[b];
+    if (n > slab) slab = n;
+  }
+  mark_begin(e, kKStageBegin);
+  IDFX_DISPATCH_DE(k_stage_ghosts, dim3(nblocks(slab), e.g.D), kThreads, e.g, e.f, e.ctl, flags);
+  mark_end(e);
+}
 void launch_ct(Engine& e, int combine, double wc, double w0) {
   mark_begin(e, kKCtCorner);
   IDFX_DISPATCH_DE(k_ct_corner, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
@@ -315,6 +328,7 @@ void launch_divb_check(Engine& e) {
 void queue_cycle(Engine& e, int use_tstop) {
   const Geo& g = e.g;
   const bool cell_emf = (g.emf == kEmfContact || g.emf == kEmfUct0);
+  const bool fused = (e.precision == IDFX_MIXED) && !g.nonper;
   k_cycle_begin<<<1, 1, 0, e.stream>>>(g, e.ctl, use_tstop);
   if (e.log_period > 0 && e.ncycles % e.log_period == 0) launch_divb_check(e);
   const bool nan_check = e.check_nan_period > 0 && e.ncycles % e.check_nan_period == 0;
@@ -326,7 +340,12 @@ void queue_cycle(Engine& e, int use_tstop) {
     // still the state Vc came from (Ctl::uc_fresh); the FP64 path rebuilds it
     // as the reference does
     const int cons = kSbCons | (e.precision == IDFX_MIXED ? kSbKeepCons : 0);
-    launch_stage_begin(e, cons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0));
+    const int sb_flags = cons | (save ? kSbSaveBegin : 0) | (cell_emf ? kSbCellEmf : 0);
+    // mixed path, periodic block: once a stage end of this run has written
+    // the active cells' FP32 primitives, cell EMF and Runge-Kutta begin copy,
+    // the stage begin fills the ghost cells alone
+    if (fused && e.stage_outputs) launch_stage_ghosts(e, sb_flags);
+    else launch_stage_begin(e, sb_flags);
     if (e.f.shock) launch_find_shock(e);  // RiemannSolver::CalcFlux (calcFlux.hpp:33)
     launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
     const int combine = stage > 0;
@@ -343,9 +362,13 @@ void queue_cycle(Engine& e, int use_tstop) {
     } else {
       launch_ct(e, combine, wc, w0);
     }
+    const int out = fused ? (kSeOutputs | (cell_emf ? kSbCellEmf : 0) |
+                             (e.nstages > 1 && stage == e.nstages - 1 ? kSeSaveBegin : 0))
+                          : 0;
     mark_begin(e, kKStageEnd);
-    IDFX_DISPATCH_DE(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0);
+    IDFX_DISPATCH_DE(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0, out);
     mark_end(e);
+    if (fused) e.stage_outputs = true;
   }
   k_cycle_end<<<1, 1, 0, e.stream>>>(e.ctl);
   e.ncycles++;
@@ -845,6 +868,7 @@ static int run_cycles(idfx_gpu* h, double tstop, long long max_cycles) {
   e.ctl_host->status = 0;
   e.ncycles = e.ctl_host->ncycles;
   ctl_push(e);
+  e.stage_outputs = false;  // the run's first stage begin rebuilds from the stored state
   const int use_tstop = tstop >= 0.0;
   long long done = 0;
   const long long chunk = 64;  // host polls t / status every chunk of queued cycles

@@ -26,6 +26,7 @@ struct Engine {
   long long ncycles = 0;     // host mirror of the cycle counter
   int seg[3] = {32, 32, 32}; // marching segment per direction
   int only_dir = -1;         // >= 0: sweeps launch that direction alone (autotuner)
+  bool stage_outputs = false;  // mixed path: a stage end queued in this run wrote the next stage's inputs
   std::string err;
   double* pool = nullptr;    // one allocation for every field
   size_t pool_len = 0;

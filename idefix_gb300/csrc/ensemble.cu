@@ -187,22 +187,33 @@ std::vector<int4> sweep_items(const EnsEngine& e, int dir, const std::vector<int
   return v;
 }
 
-int build_tables(EnsEngine& e) {
-  const std::vector<int> order = schedule(e);
-  std::vector<int4> fill, begin, edges, active;
+// the per-box phases' work lists for blocks of bt threads
+void phase_items(const EnsEngine& e, const std::vector<int>& order, int bt, std::vector<int4>& fill,
+                 std::vector<int4>& begin, std::vector<int4>& edges, std::vector<int4>& active) {
   for (int b : order) {
     const Geo& g = e.boxes[b].g;
-    const long long nf = (g.nface + kT - 1) / kT;
+    const long long nf = (g.nface + bt - 1) / bt;
     for (int comp = 0; comp < g.D; comp++)
       for (long long x = 0; x < nf; x++) fill.push_back(make_int4(b, (int)x, comp, 0));
-    for (long long x = 0; x < (g.ncell + kT - 1) / kT; x++) begin.push_back(make_int4(b, (int)x, 0, 0));
-    for (long long x = 0; x < (edge_count(g) + kT - 1) / kT; x++) edges.push_back(make_int4(b, (int)x, 0, 0));
-    for (long long x = 0; x < (active_cells(g) + kT - 1) / kT; x++) active.push_back(make_int4(b, (int)x, 0, 0));
+    for (long long x = 0; x < (g.ncell + bt - 1) / bt; x++) begin.push_back(make_int4(b, (int)x, 0, 0));
+    for (long long x = 0; x < (edge_count(g) + bt - 1) / bt; x++) edges.push_back(make_int4(b, (int)x, 0, 0));
+    for (long long x = 0; x < (active_cells(g) + bt - 1) / bt; x++) active.push_back(make_int4(b, (int)x, 0, 0));
   }
+}
+
+int build_tables(EnsEngine& e) {
+  const std::vector<int> order = schedule(e);
+  std::vector<int4> fill, begin, edges, active, fill64, begin64, edges64, active64;
+  phase_items(e, order, kT, fill, begin, edges, active);
+  phase_items(e, order, kTM, fill64, begin64, edges64, active64);
   int rc = upload_table(e, e.fill, fill);
   if (!rc) rc = upload_table(e, e.begin, begin);
   if (!rc) rc = upload_table(e, e.edges, edges);
   if (!rc) rc = upload_table(e, e.active, active);
+  if (!rc) rc = upload_table(e, e.fill64, fill64);
+  if (!rc) rc = upload_table(e, e.begin64, begin64);
+  if (!rc) rc = upload_table(e, e.edges64, edges64);
+  if (!rc) rc = upload_table(e, e.active64, active64);
   for (int d = 0; d < e.D && !rc; d++) rc = upload_table(e, e.sweep[d], sweep_items(e, d, order));
   return rc;
 }
@@ -274,7 +285,62 @@ int capture_one(EnsEngine& e, bool checks, cudaGraphExec_t* exec) {
 int capture_graph(EnsEngine& e) {
   int rc = capture_one(e, false, &e.exec);
   if (!rc && (e.log_period > 0 || e.check_nan_period > 0)) rc = capture_one(e, true, &e.exec_checks);
+  if (e.exec_persist) {  // the persistent graph is captured again on its next use
+    cudaGraphExecDestroy(e.exec_persist);
+    e.exec_persist = nullptr;
+    e.persist_chunk = 0;
+  }
   return rc;
+}
+
+int persist_blocks(const EnsEngine& e) {
+  switch (e.solver) {
+    case kHLLD: return ens_persist_blocks_hlld(e);
+    case kHLL: return ens_persist_blocks_hll(e);
+    case kROE: return ens_persist_blocks_roe(e);
+    default: return ens_persist_blocks_tvdlf(e);
+  }
+}
+
+__global__ void ke_bar_reset(GridBar* b) { *b = GridBar{0u, 0u, 0, 0}; }
+
+// ncyc cycles of every box as one persistent launch (the barrier reset first)
+cudaError_t queue_persist(EnsEngine& e, int ncyc) {
+  const int grid = persist_blocks(e);
+  if (grid < 1) return cudaErrorInvalidConfiguration;
+  ke_bar_reset<<<1, 1, 0, e.stream>>>(e.d_bar);
+  switch (e.solver) {
+    case kHLLD: return launch_ens_persist_hlld(e, ncyc, grid);
+    case kHLL: return launch_ens_persist_hll(e, ncyc, grid);
+    case kROE: return launch_ens_persist_roe(e, ncyc, grid);
+    default: return launch_ens_persist_tvdlf(e, ncyc, grid);
+  }
+}
+
+// the persistent launch of `ncyc` cycles replayed from a CUDA graph (captured
+// once per chunk length); where the capture of a cooperative launch is not
+// available, the launch goes to the stream directly
+cudaError_t run_persist(EnsEngine& e, int ncyc) {
+  if (e.persist_graph && e.exec_persist && e.persist_chunk == ncyc) return cudaGraphLaunch(e.exec_persist, e.stream);
+  if (e.exec_persist) {
+    cudaGraphExecDestroy(e.exec_persist);
+    e.exec_persist = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  e.persist_graph = false;
+  if (cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    const cudaError_t lr = queue_persist(e, ncyc);
+    const cudaError_t cr = cudaStreamEndCapture(e.stream, &graph);
+    if (lr == cudaSuccess && cr == cudaSuccess && graph &&
+        cudaGraphInstantiate(&e.exec_persist, graph, 0) == cudaSuccess) {
+      e.persist_graph = true;
+      e.persist_chunk = ncyc;
+    }
+    if (graph) cudaGraphDestroy(graph);
+  }
+  cudaGetLastError();  // a refused capture leaves no error behind
+  if (e.persist_graph) return cudaGraphLaunch(e.exec_persist, e.stream);
+  return queue_persist(e, ncyc);
 }
 
 int ens_fail(EnsEngine& e, int code, const std::string& msg) {
@@ -288,62 +354,12 @@ int read_ctl(EnsEngine& e) {
   return cudaStreamSynchronize(e.stream) == cudaSuccess ? IDFX_OK : IDFX_ERR_CUDA;
 }
 
-// geometry of one box, as idfx_gpu_create sets it up
+// geometry of one box, set up as idfx_gpu_create sets it up (the boxes are
+// periodic)
 bool box_geometry(const idfx_gpu_config* cfg, Geo& g) {
-  if (cfg->dims != 2 && cfg->dims != 3) return false;
-  for (int d = 0; d < 3; d++)  // the boxes are periodic
+  for (int d = 0; d < 3; d++)
     if (cfg->lbound[d] || cfg->rbound[d]) return false;
-  for (int d = 0; d < cfg->dims; d++)
-    if (cfg->n[d] < 2 || !(cfg->xend[d] > cfg->xbeg[d])) return false;
-  g.D = cfg->dims;
-  g.order = cfg->order;
-  g.solver = cfg->solver;
-  g.emf = cfg->emf;
-  g.nstages = cfg->nstages;
-  g.ng = (cfg->order == 4) ? 3 : 2;
-  for (int d = 0; d < 3; d++) {
-    const bool act = d < g.D;
-    const int gd = act ? g.ng : 0;
-    g.n[d] = act ? cfg->n[d] : 1;
-    g.nt[d] = g.n[d] + 2 * gd;
-    g.ntv[d] = g.nt[d] + (act ? 1 : 0);
-    g.beg[d] = gd;
-    g.end[d] = gd + g.n[d];
-    const double xb = act ? cfg->xbeg[d] : 0.0, xe = act ? cfg->xend[d] : 1.0;
-    g.dx[d] = (xe - xb) / (g.n[d]);
-  }
-  g.s[0] = 1;
-  g.s[1] = g.nt[0];
-  g.s[2] = (long long)g.nt[0] * g.nt[1];
-  g.fs[0] = 1;
-  g.fs[1] = g.ntv[0];
-  g.fs[2] = (long long)g.ntv[0] * g.ntv[1];
-  g.ncell = (long long)g.nt[0] * g.nt[1] * g.nt[2];
-  g.nface = (long long)g.ntv[0] * g.ntv[1] * g.ntv[2];
-  if (g.D == 2) {
-    g.A[0] = 1.0 * g.dx[1];
-    g.A[1] = g.dx[0] * 1.0;
-    g.A[2] = 1.0;
-  } else {
-    g.A[0] = 1.0 * g.dx[1] * g.dx[2];
-    g.A[1] = g.dx[0] * 1.0 * g.dx[2];
-    g.A[2] = g.dx[0] * g.dx[1] * 1.0;
-  }
-  g.gamma = cfg->gamma;
-  g.gm1 = cfg->gamma - 1.0;
-  g.rgm1 = 1.0 / g.gm1;  // correctly rounded reciprocals (Markstein quotients)
-  for (int d = 0; d < 3; d++) {
-    g.rdx[d] = 1.0 / g.dx[d];
-    const double e = 0.1 * g.dx[d];  // LimO3's r dx, squared as the limiter does
-    g.l3b[d] = e * e;
-    g.l3y[d] = 1.0 / g.l3b[d];
-  }
-  g.ext = 1;
-  if ((g.emf == kEmfUctHll || g.emf == kEmfUctHlld) && (g.solver == kHLLD || g.solver == kHLL)) g.ext = g.ng;
-  g.shock_smoothing = cfg->shock_smoothing;
-  for (int d = 0; d < 3; d++) g.bc[d][0] = g.bc[d][1] = 0;
-  g.nonper = 0;
-  return true;
+  return block_geometry(cfg, g) == IDFX_OK;
 }
 
 // first guess of the march segment (the autotuner refines it)
@@ -458,6 +474,8 @@ void release(EnsEngine& e) {
   if (e.stream) cudaStreamSynchronize(e.stream);
   if (e.exec) cudaGraphExecDestroy(e.exec);
   if (e.exec_checks) cudaGraphExecDestroy(e.exec_checks);
+  if (e.exec_persist) cudaGraphExecDestroy(e.exec_persist);
+  if (e.d_bar) cudaFree(e.d_bar);
   for (EnsTable* t : e.tables())
     if (t->items) cudaFree(t->items);
   if (e.d_boxes) cudaFree(e.d_boxes);
@@ -468,6 +486,38 @@ void release(EnsEngine& e) {
 }
 
 }  // namespace
+
+namespace idfx {
+
+EnsPersist ens_persist_args(const EnsEngine& e) {
+  EnsPersist P{};
+  P.fill = e.fill64.items;
+  P.nfill = e.fill64.n;
+  P.begin = e.begin64.items;
+  P.nbegin = e.begin64.n;
+  P.edges = e.edges64.items;
+  P.nedges = e.edges64.n;
+  P.active = e.active64.items;
+  P.nactive = e.active64.n;
+  for (int d = 0; d < 3; d++) {
+    P.sweep[d] = e.sweep[d].items;
+    P.nsweep[d] = d < e.D ? e.sweep[d].n : 0;
+  }
+  P.nbox = e.nbox;
+  P.nstages = e.nstages;
+  P.log_period = e.log_period;
+  P.check_nan_period = e.check_nan_period;
+  P.shock = e.shock ? 1 : 0;
+  P.keep_cons = e.precision == IDFX_MIXED ? 1 : 0;
+  P.cell_emf = (e.emf == kEmfContact || e.emf == kEmfUct0) ? 1 : 0;
+  for (int k = 0; k < 2; k++) {
+    P.wc[k] = e.wc[k];
+    P.w0[k] = e.w0[k];
+  }
+  return P;
+}
+
+}  // namespace idfx
 
 // ===========================================================================
 // C ABI
@@ -544,6 +594,7 @@ int idfx_ens_create(int nbox, const idfx_gpu_config* cfgs, void* stream, idfx_en
   if (!rc && cudaMalloc(&e.d_ctl, sizeof(Ctl) * nbox) != cudaSuccess) rc = IDFX_ERR_CUDA;
   if (!rc && cudaMallocHost(&e.h_ctl, sizeof(Ctl) * nbox) != cudaSuccess) rc = IDFX_ERR_CUDA;
   if (!rc && cudaMalloc(&e.d_boxes, sizeof(EnsBox) * nbox) != cudaSuccess) rc = IDFX_ERR_CUDA;
+  if (!rc && cudaMalloc(&e.d_bar, sizeof(GridBar)) != cudaSuccess) rc = IDFX_ERR_CUDA;
   if (rc) {
     std::fprintf(stderr, "idfx_ens_create: CUDA allocation failed (%.3f GB of fields)\n", len * 8.0 / 1e9);
     release(e);
@@ -677,10 +728,12 @@ int idfx_ens_get_time(idfx_ens* h, int box, double* t, double* dt, long long* nc
 // most max_cycles cycles (< 0: no limit); boxes that reach tstop or fail stop
 // while the others go on.  Returns IDFX_OK when no box failed, else the
 // status of the first failed box (idfx_ens_get_time gives every box's).
-int idfx_ens_run(idfx_ens* h, double tstop, long long max_cycles, int use_graph) {
+// mode: IDFX_ENS_LAUNCHES, IDFX_ENS_GRAPH, IDFX_ENS_PERSISTENT.
+int idfx_ens_run(idfx_ens* h, double tstop, long long max_cycles, int mode) {
   if (!h) return IDFX_ERR_STATE;
   EnsEngine& e = h->e;
   if (tstop < 0.0 && max_cycles < 0) return ens_fail(e, IDFX_ERR_CONFIG, "run needs tstop or max_cycles");
+  if (mode < IDFX_ENS_LAUNCHES || mode > IDFX_ENS_PERSISTENT) return ens_fail(e, IDFX_ERR_CONFIG, "run: unknown mode");
   if (read_ctl(e)) return ens_fail(e, IDFX_ERR_CUDA, "run: CUDA failure");
   std::vector<long long> nc(e.nbox);
   std::vector<char> live(e.nbox);
@@ -704,11 +757,16 @@ int idfx_ens_run(idfx_ens* h, double tstop, long long max_cycles, int use_graph)
     if (!any_live) break;
     long long n = chunk;
     if (max_cycles >= 0 && max_cycles - done < n) n = max_cycles - done;
-    for (long long q = 0; q < n; q++) {
+    if (mode == IDFX_ENS_PERSISTENT) {
+      const cudaError_t pr = run_persist(e, (int)n);
+      if (pr != cudaSuccess)
+        return ens_fail(e, IDFX_ERR_CUDA, std::string("persistent launch: ") + cudaGetErrorString(pr));
+    }
+    for (long long q = 0; q < n && mode != IDFX_ENS_PERSISTENT; q++) {
       bool checks = false;  // some live box runs a diagnostic this cycle
       for (int b = 0; b < e.nbox && !checks; b++)
         checks = live[b] && (is_due(nc[b] + q, e.log_period) || is_due(nc[b] + q, e.check_nan_period));
-      if (use_graph) {
+      if (mode == IDFX_ENS_GRAPH) {
         cudaGraphExec_t g = checks ? e.exec_checks : e.exec;
         if (cudaGraphLaunch(g, e.stream) != cudaSuccess) return ens_fail(e, IDFX_ERR_CUDA, "cudaGraphLaunch failed");
       } else {
@@ -738,6 +796,13 @@ int idfx_ens_autotune(idfx_ens* h, int reps) {
 int idfx_ens_get_segments(const idfx_ens* h, int box, int* seg) {
   if (!h || !seg || box < 0 || box >= h->e.nbox) return IDFX_ERR_STATE;
   for (int d = 0; d < 3; d++) seg[d] = h->e.boxes[box].seg[d];
+  return IDFX_OK;
+}
+
+int idfx_ens_persistent_info(idfx_ens* h, int* blocks, int* graph) {
+  if (!h) return IDFX_ERR_STATE;
+  if (blocks) *blocks = persist_blocks(h->e);
+  if (graph) *graph = h->e.persist_graph ? 1 : 0;
   return IDFX_OK;
 }
 

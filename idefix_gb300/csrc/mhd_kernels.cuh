@@ -181,19 +181,44 @@ __global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
 // kSbSaveBegin it is copied to Uc0.
 enum { kSbCons = 1, kSbSaveBegin = 2, kSbCellEmf = 4, kSbKeepCons = 8 };
 
+// the cell-centred EMF E = -v x B from the primitives W (in the EMF type)
+template <int D, typename E>
+__device__ __forceinline__ void cell_emf_store(const Fields& f, long long c, const E* W) {
+  using v = Var<D>;
+  const E vx1 = W[v::MX1], vx2 = W[v::MX2];
+  const E Bx1 = W[v::BX1], Bx2 = W[v::BX2];
+  if constexpr (D == 3) {
+    const E vx3 = W[v::MX3], Bx3 = W[v::BX3];
+    emf<E>(f.Ex1)[c] = (vx3 * Bx2 - vx2 * Bx3);
+    emf<E>(f.Ex2)[c] = (vx1 * Bx3 - vx3 * Bx1);
+  }
+  emf<E>(f.Ex3)[c] = (vx2 * Bx1 - vx1 * Bx2);
+}
+
+// the primitives of cell c in the EMF type, their FP32 copy for the
+// mixed-precision sweeps and the cell EMF
+template <int D, typename E>
+__device__ __forceinline__ void cell_outputs(const Fields& f, const Geo& g, long long c, const double* V,
+                                             bool cell_emf) {
+  constexpr int NV = Var<D>::NV;
+  E W[NV];
+#pragma unroll
+  for (int n = 0; n < NV; n++) W[n] = from_f64<E>(V[n]);
+  if (cell_emf) cell_emf_store<D, E>(f, c, W);
+  if (f.Vc32) {  // mixed precision: the sweeps read the primitives in FP32
+#pragma unroll
+    for (int n = 0; n < NV; n++) f.Vc32[n * g.ncell + c] = (sizeof(E) == 4) ? (float)W[n] : d2f_rn(V[n]);
+  }
+}
+
 // E: type of the EMF buffers (float on the mixed path: the cell EMF is then
 // computed in FP32 from the FP32 primitives that the sweeps read)
 template <int D, typename E = double>
-__device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, const Ctl* ctl, int flags, dim3 bid) {
-  if (ctl->done) return;
+__device__ __forceinline__ void stage_begin_cell(const Geo& g, const Fields& f, const Ctl* ctl, int flags, int i,
+                                                 int j, int k) {
   using v = Var<D>;
   constexpr int NV = v::NV;
-  const long long c = (long long)bid.x * blockDim.x + threadIdx.x;
-  if (c >= g.ncell) return;
-  int i = (int)(c % g.nt[0]);
-  long long r = c / g.nt[0];
-  int j = (int)(r % g.nt[1]);
-  int k = (int)(r / g.nt[1]);
+  const long long c = cidx(g, k, j, i);
   int src[3] = {i, j, k};
   bool ghost = false;
   const int idx3[3] = {i, j, k};
@@ -235,24 +260,51 @@ __device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, con
 #pragma unroll
     for (int n = 0; n < v::BX1; n++) f.Uc0[n * g.ncell + c] = f.Uc[n * g.ncell + c];
   }
-  // the primitives in the EMF type (the FP32 copy on the mixed path)
-  E W[NV];
-#pragma unroll
-  for (int n = 0; n < NV; n++) W[n] = from_f64<E>(V[n]);
-  if (flags & kSbCellEmf) {
-    const E vx1 = W[v::MX1], vx2 = W[v::MX2];
-    const E Bx1 = W[v::BX1], Bx2 = W[v::BX2];
-    if constexpr (D == 3) {
-      const E vx3 = W[v::MX3], Bx3 = W[v::BX3];
-      emf<E>(f.Ex1)[c] = (vx3 * Bx2 - vx2 * Bx3);
-      emf<E>(f.Ex2)[c] = (vx1 * Bx3 - vx3 * Bx1);
-    }
-    emf<E>(f.Ex3)[c] = (vx2 * Bx1 - vx1 * Bx2);
-  }
-  if (f.Vc32) {  // mixed precision: the sweeps read the primitives in FP32
-#pragma unroll
-    for (int n = 0; n < NV; n++) f.Vc32[n * g.ncell + c] = (sizeof(E) == 4) ? (float)W[n] : d2f_rn(V[n]);
-  }
+  cell_outputs<D, E>(f, g, c, V, (flags & kSbCellEmf) != 0);
+}
+
+template <int D, typename E = double>
+__device__ __forceinline__ void d_stage_begin(const Geo& g, const Fields& f, const Ctl* ctl, int flags, dim3 bid) {
+  if (ctl->done) return;
+  const long long c = (long long)bid.x * blockDim.x + threadIdx.x;
+  if (c >= g.ncell) return;
+  const int i = (int)(c % g.nt[0]);
+  const long long r = c / g.nt[0];
+  const int j = (int)(r % g.nt[1]);
+  const int k = (int)(r / g.nt[1]);
+  stage_begin_cell<D, E>(g, f, ctl, flags, i, j, k);
+}
+
+// Stage begin of the ghost cells only (periodic blocks, mixed path, when the
+// previous stage end left Uc, Vc, the FP32 primitives and the cell EMF of
+// every active cell): the two ghost slabs of direction bid.y, each over the
+// full extent of the other two directions (cells in two slabs get the same
+// values from both).
+template <int D, typename E = double>
+__device__ __forceinline__ void d_stage_ghosts(const Geo& g, const Fields& f, const Ctl* ctl, int flags, dim3 bid) {
+  if (ctl->done) return;
+  const int dir = bid.y;
+  if (dir >= D) return;
+  const int a = (dir == 0) ? 1 : 0, b = (dir == 2) ? 1 : 2;
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
+  const long long per_side = (long long)g.ng * g.nt[a] * g.nt[b];
+  if (tid >= 2 * per_side) return;
+  const int side = (int)(tid / per_side);
+  long long r = tid % per_side;
+  const int layer = (int)(r % g.ng);
+  r /= g.ng;
+  const int ia = (int)(r % g.nt[a]);
+  const int ib = (int)(r / g.nt[a]);
+  int idx[3];
+  idx[dir] = side ? g.end[dir] + layer : layer;
+  idx[a] = ia;
+  idx[b] = ib;
+  stage_begin_cell<D, E>(g, f, ctl, flags, idx[0], idx[1], idx[2]);
+}
+
+template <int D, typename E = double>
+__global__ void k_stage_ghosts(Geo g, Fields f, const Ctl* ctl, int flags) {
+  d_stage_ghosts<D, E>(g, f, ctl, flags, blockIdx);
 }
 
 template <int D, typename E = double>
@@ -1436,9 +1488,15 @@ __global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double 
 // cell-centred field from the faces (ReconstructVcField on Uc), and
 // ConvertConsToPrim.  Writes Uc and Vc.
 // ---------------------------------------------------------------------------
-// E: EMF type of the path (FP32: mixed path, see rk_combine)
+// E: EMF type of the path (FP32: mixed path, see rk_combine).  out (mixed
+// path, periodic blocks): kSeOutputs also writes what the next stage begin
+// derives for the active cells - the FP32 primitives and (kSbCellEmf) the
+// cell EMF - and kSeSaveBegin the Runge-Kutta begin copy of the next cycle
+// (Uc0 = Uc), so that the next stage begin only fills the ghost cells.
+enum { kSeOutputs = 16, kSeSaveBegin = 32 };
 template <int D, typename E = double>
-__device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc, double w0, dim3 bid) {
+__device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc,
+                                            double w0, dim3 bid, int out = 0) {
   if (ctl->done) return;
   using v = Var<D>;
   constexpr int NV = v::NV;
@@ -1470,11 +1528,16 @@ __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const
     f.Uc[n * g.ncell + c] = U[n];
     f.Vc[n * g.ncell + c] = V[n];
   }
+  if (out & kSeOutputs) cell_outputs<D, E>(f, g, c, V, (out & kSbCellEmf) != 0);
+  if (out & kSeSaveBegin) {
+#pragma unroll
+    for (int n = 0; n < v::BX1; n++) f.Uc0[n * g.ncell + c] = U[n];
+  }
 }
 
 template <int D, typename E = double>
-__global__ void k_stage_end(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
-  d_stage_end<D, E>(g, f, ctl, combine, wc, w0, blockIdx);
+__global__ void k_stage_end(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0, int out) {
+  d_stage_end<D, E>(g, f, ctl, combine, wc, w0, blockIdx, out);
 }
 
 // ---------------------------------------------------------------------------

@@ -40,20 +40,27 @@ def ensemble_case(nbox=512, seed=0, sizes=ic.ENSEMBLE_SIZES, cfl=0.6, first_dt=1
 
 
 def run_ensemble(nbox=512, seed=0, cycles=500, sizes=ic.ENSEMBLE_SIZES, check=True, autotune=True,
-                 graph=True, log=sys.stderr):
+                 graph=True, persistent=True, log=sys.stderr):
+    """the batched ensemble (graph of batched launches per cycle, or launches
+    one by one); persistent: the same boxes again in the persistent mode
+    (one launch per chunk of cycles), timed and compared bit for bit"""
     import torch
 
     case = ensemble_case(nbox, seed, sizes)
-    ens = ig.Ensemble([c[0] for c in case])
-    cells = 0
-    for k, (cfg, mach, beta) in enumerate(case):
-        Vc, Vs = ic.orszag_tang_like_2d(cfg["n"][0], mach=mach, beta=beta)
-        ens.upload(k, Vc, Vs)
-        cells += cfg["n"][0] * cfg["n"][1]
-    t0 = time.perf_counter()
-    if autotune:
-        ens.autotune(reps=3)
-    t_tune = time.perf_counter() - t0
+
+    def build():
+        ens = ig.Ensemble([c[0] for c in case])
+        cells = 0
+        for k, (cfg, mach, beta) in enumerate(case):
+            Vc, Vs = ic.orszag_tang_like_2d(cfg["n"][0], mach=mach, beta=beta)
+            ens.upload(k, Vc, Vs)
+            cells += cfg["n"][0] * cfg["n"][1]
+        t0 = time.perf_counter()
+        if autotune:
+            ens.autotune(reps=3)
+        return ens, cells, time.perf_counter() - t0
+
+    ens, cells, t_tune = build()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     ens.run(max_cycles=cycles, graph=graph)
@@ -62,6 +69,20 @@ def run_ensemble(nbox=512, seed=0, cycles=500, sizes=ic.ENSEMBLE_SIZES, check=Tr
            "ensemble_s": t_ens, "autotune_s": t_tune,
            "zone_cycles_per_s": cells * cycles / t_ens,
            "segments": sorted({(c[0]["n"][0], tuple(ens.segments(k)[:2])) for k, c in enumerate(case)})}
+    if persistent:
+        pens, _, _ = build()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pens.run(max_cycles=cycles, persistent=True)
+        t_p = time.perf_counter() - t0
+        blocks, from_graph = pens.persistent_info()
+        same = sum(1 for k in range(nbox)
+                   if all(np.array_equal(a, b) for a, b in zip(pens.download(k), ens.download(k)))
+                   and pens.get_time(k) == ens.get_time(k))
+        pens.close()
+        res.update({"persistent_s": t_p, "persistent_zone_cycles_per_s": cells * cycles / t_p,
+                    "persistent_blocks": blocks, "persistent_from_graph": from_graph,
+                    "persistent_boxes_identical": same})
     if not check:
         ens.close()
         return res

@@ -291,8 +291,19 @@ int idfx_ens_download_prim_device(idfx_ens* h, int box, double* Vc, double* Vs);
 int idfx_ens_get_time(idfx_ens* h, int box, double* t, double* dt, long long* ncycles, int* status);
 /* every box cycles until its t reaches tstop (< 0: no limit), at most
  * max_cycles cycles (< 0: no limit); a box that stops or fails leaves the
- * others running.  use_graph = 0 queues the launches one by one. */
-int idfx_ens_run(idfx_ens* h, double tstop, long long max_cycles, int use_graph);
+ * others running.  mode: IDFX_ENS_GRAPH (1) replays one CUDA graph of
+ * batched launches (one per phase) per cycle; IDFX_ENS_LAUNCHES (0) queues
+ * the same launches one by one; IDFX_ENS_PERSISTENT (2) runs each chunk of
+ * 64 cycles as ONE persistent cooperative launch (replayed from a CUDA
+ * graph where the capture of a cooperative launch is available), its phases
+ * separated by a grid-wide barrier whose every wait is bounded (a wait that
+ * gives up stops every box with IDFX_ERR_CUDA).  All modes give identical
+ * results. */
+enum { IDFX_ENS_LAUNCHES = 0, IDFX_ENS_GRAPH = 1, IDFX_ENS_PERSISTENT = 2 };
+int idfx_ens_run(idfx_ens* h, double tstop, long long max_cycles, int mode);
+/* co-resident blocks of the persistent launch, and whether it replays from
+ * a CUDA graph (after a persistent run) */
+int idfx_ens_persistent_info(idfx_ens* h, int* blocks, int* graph);
 /* Autotuner: per box size and direction, the march segment length of the
  * fastest batched sweep (timed over reps launches); the state is restored. */
 int idfx_ens_autotune(idfx_ens* h, int reps);

@@ -6,7 +6,9 @@ single-block entry points (GpuBlock, itself bit-identical to the reference),
 so every comparison here is exact equality of the state, the time, the time
 step and the cycle count: with and without the CUDA graph, after the
 autotuner, with the divB / NaN diagnostics on, with boxes that stop at
-tstop after different numbers of cycles, and with a box that fails.
+tstop after different numbers of cycles, and with a box that fails; and
+in the persistent mode (every chunk of cycles one cooperative launch, its
+phases separated by a bounded grid barrier).
 """
 import numpy as np
 import pytest
@@ -45,7 +47,7 @@ def _single(cfg, Vc, Vs, tstop=-1.0, cycles=-1):
     return out, (t, dt, nc), rc
 
 
-def _ensemble(boxes, tstop=-1.0, cycles=-1, graph=True, autotune=False, schedule=None):
+def _ensemble(boxes, tstop=-1.0, cycles=-1, graph=True, autotune=False, schedule=None, persistent=False):
     ens = ig.Ensemble([b[0] for b in boxes])
     for k, (_, Vc, Vs) in enumerate(boxes):
         ens.upload(k, Vc, Vs)
@@ -55,7 +57,7 @@ def _ensemble(boxes, tstop=-1.0, cycles=-1, graph=True, autotune=False, schedule
         ens.autotune(reps=2)
     err = None
     try:
-        ens.run(tstop=tstop, max_cycles=cycles, graph=graph)
+        ens.run(tstop=tstop, max_cycles=cycles, graph=graph, persistent=persistent)
     except (ig.IdefixError, RuntimeError) as exc:
         err = exc
     res = [(ens.download(k), ens.get_time(k)) for k in range(len(boxes))]
@@ -157,3 +159,54 @@ def test_ensemble_with_shock_flattening():
     res, err, _ = _ensemble(boxes, cycles=8)
     assert err is None
     _assert_same(res, boxes, cycles=8)
+
+
+def _persistent_cases():
+    return {
+        "plain": (_mixed_boxes(), dict(cycles=10)),
+        "diagnostics_rk3": (_mixed_boxes(log_period=3, check_nan_period=2, nstages=3), dict(cycles=9)),
+        "tstop": (_mixed_boxes(log_period=4, check_nan_period=5), dict(tstop=0.1)),
+        "chunks": (_mixed_boxes(log_period=7, check_nan_period=11), dict(cycles=150)),
+        "mixed_precision": (_mixed_boxes(precision="mixed"), dict(cycles=6)),
+        "shock": (_mixed_boxes(shock_flattening=0.0), dict(cycles=8)),
+    }
+
+
+@pytest.mark.parametrize("case", ["plain", "diagnostics_rk3", "tstop", "chunks", "mixed_precision", "shock"])
+def test_persistent_launch_matches_single_boxes(case):
+    boxes, kw = _persistent_cases()[case]
+    res, err, _ = _ensemble(boxes, persistent=True, **kw)
+    assert err is None
+    _assert_same(res, boxes, **kw)
+
+
+def test_persistent_launch_3d_and_failed_box():
+    boxes = []
+    for n, seed in ((24, 1), (12, 2), (8, 3)):
+        Vc, Vs = ic.turbulence_3d(n, seed=seed, kmax=3)
+        boxes.append((dict(dims=3, n=(n, n, n), cfl=0.6), Vc, Vs))
+    res, err, _ = _ensemble(boxes, cycles=5, persistent=True)
+    assert err is None
+    _assert_same(res, boxes, cycles=5)
+    boxes = _mixed_boxes()
+    boxes[2] = (dict(boxes[2][0], first_dt=1.0), boxes[2][1], boxes[2][2])
+    res, err, _ = _ensemble(boxes, cycles=7, persistent=True)
+    assert isinstance(err, ig.IdefixError) and "box 2" in str(err)
+    assert res[2][1][3] == ig.ERR_FIRST_DT
+    good = [k for k in range(len(boxes)) if k != 2]
+    _assert_same([res[k] for k in good], [boxes[k] for k in good], cycles=7)
+
+
+def test_persistent_launch_is_one_cooperative_launch():
+    """the persistent mode's chunk is a single cooperative launch of all
+    co-resident blocks (replayed from a CUDA graph where the capture of a
+    cooperative launch is available; either way the results are equal)"""
+    boxes = _mixed_boxes()
+    ens = ig.Ensemble([b[0] for b in boxes])
+    for k, (_, Vc, Vs) in enumerate(boxes):
+        ens.upload(k, Vc, Vs)
+    ens.run(max_cycles=3, persistent=True)
+    blocks, graph = ens.persistent_info()
+    ens.close()
+    assert blocks >= 148
+    assert graph in (True, False)
