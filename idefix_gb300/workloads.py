@@ -437,9 +437,11 @@ if __name__ == "__main__":
     ap.add_argument("--cycles", type=int, default=None, help="default: 500 (ensemble), 200 (lowbeta)")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--sizes", default=None, help="comma-separated box sizes of the ensemble (default: config 4's)")
     a = ap.parse_args()
     if a.workload == "ensemble":
-        r = run_ensemble(a.nbox, a.seed, a.cycles or 500, check=not a.no_check, graph=not a.no_graph)
+        sizes = tuple(int(x) for x in a.sizes.split(",")) if a.sizes else ic.ENSEMBLE_SIZES
+        r = run_ensemble(a.nbox, a.seed, a.cycles or 500, sizes=sizes, check=not a.no_check, graph=not a.no_graph)
     elif a.workload == "lowbeta":
         r = run_lowbeta(a.n, a.cycles or 200, a.seed)
     elif a.workload == "rotor":

@@ -66,7 +66,11 @@ WORKLOADS = {
                 "low-beta 3-D {n}^3 FP64, HLLD + LimO3 + uct_contact, RK2"),
     "ot3d": ("orszag_tang_3d", lambda n, seed: dict(nx=n, ny=n, nz=n), "plm", 0.9,
              "Orszag-Tang 3-D {n}^3 FP64, HLLD + PLM + uct_contact, RK2, CFL 0.9"),
+    # one box of the ensemble workload (Mach 1, beta 10/3, the middle of its ranges)
+    "ot2d": ("orszag_tang_like_2d", lambda n, seed: dict(n=n, mach=1.0, beta=10.0 / 3.0), "plm", 0.6,
+             "Orszag-Tang-like 2-D {n}^2 FP64, HLLD + PLM + uct_contact, RK2, CFL 0.6"),
 }
+DIMS = {"ot2d": 2}
 
 
 def count(n=64, cycles=1, seed=1, workload="turbulence"):
@@ -77,7 +81,8 @@ def count(n=64, cycles=1, seed=1, workload="turbulence"):
     subprocess.run(["make", "-s", "-C", HERE, "libofx_count.so"], check=True)
     make_ic, ic_args, order, cfl, desc = WORKLOADS[workload]
     Vc, Vs = getattr(ic, make_ic)(**ic_args(n, seed))
-    o = Oracle(3, (n, n, n), order=order, cfl=cfl, kind="count")
+    dims = DIMS.get(workload, 3)
+    o = Oracle(dims, (n,) * dims, order=order, cfl=cfl, kind="count")
     o.set_prim(Vc, Vs)
     lib = o.lib
     lib.ofx_opcount_reset()
@@ -86,7 +91,8 @@ def count(n=64, cycles=1, seed=1, workload="turbulence"):
         if st != 0:
             raise RuntimeError(f"oracle cycle failed with status {st}")
     cyc = _read(lib)
-    phases = {name: _summary(_read_phase(lib, p), n**3 * cycles) for p, name in enumerate(PHASES)}
+    cells = n**dims
+    phases = {name: _summary(_read_phase(lib, p), cells * cycles) for p, name in enumerate(PHASES)}
     # one stage on the current state, its inputs prepared outside the count
     t, dt, _ = o.get_time()
     lib.ofx_set_boundaries(o.h)
@@ -95,7 +101,6 @@ def count(n=64, cycles=1, seed=1, workload="turbulence"):
     lib.ofx_opcount_reset()
     lib.ofx_evolve_stage(o.h, t, dt)
     stage = _read(lib)
-    cells = n**3
     return {
         "workload": desc.format(n=n),
         "cells": cells,
