@@ -46,6 +46,48 @@ struct EpiArgs {
 };
 
 constexpr int GT_M = 128, GT_N = 128, GT_KC = 64;
+
+// One operand chunk (R rows x GT_KC columns of k) into the canonical K-major
+// layout, zero outside rows < Rmax and k < K.  kcontig: element (r, k) at
+// src[r * ld + k] - eight consecutive k are one 16-byte load and one 16-byte
+// core-matrix row in shared memory; else at src[k * ld + r] - eight
+// consecutive rows are one 16-byte load, scattered over a core matrix's rows.
+// Vector loads where ld and the base allow them (ld a multiple of 8, base
+// 16-byte aligned; chunk and tile origins are multiples of 8).
+__device__ __forceinline__ void stage_tile(__nv_bfloat16* dst, const __nv_bfloat16* __restrict__ src, int ld,
+                                           bool kcontig, int r0, int Rmax, int k0, int K, int R) {
+  const bool vec = (ld & 7) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+  const __nv_bfloat16 zero = __float2bfloat16(0.f);
+  if (kcontig) {
+    for (int e = threadIdx.x; e < R * (GT_KC / 8); e += blockDim.x) {
+      const int r = e / (GT_KC / 8), kv = (e % (GT_KC / 8)) * 8;
+      const int gr = r0 + r, gk = k0 + kv;
+      alignas(16) __nv_bfloat16 t[8];
+      if (gr < Rmax && vec && gk + 8 <= K) {
+        *reinterpret_cast<uint4*>(t) = *reinterpret_cast<const uint4*>(src + (long long)gr * ld + gk);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++) t[i] = (gr < Rmax && gk + i < K) ? src[(long long)gr * ld + gk + i] : zero;
+      }
+      *reinterpret_cast<uint4*>(dst + umma::kmajor_offset(r, kv, GT_KC) / 2) = *reinterpret_cast<const uint4*>(t);
+    }
+  } else {
+    const int rg = R / 8;  // groups of eight rows; consecutive threads take consecutive groups
+    for (int e = threadIdx.x; e < rg * GT_KC; e += blockDim.x) {
+      const int rv = (e % rg) * 8, k = e / rg;
+      const int gr = r0 + rv, gk = k0 + k;
+      alignas(16) __nv_bfloat16 t[8];
+      if (gk < K && vec && gr + 8 <= Rmax) {
+        *reinterpret_cast<uint4*>(t) = *reinterpret_cast<const uint4*>(src + (long long)gk * ld + gr);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++) t[i] = (gk < K && gr + i < Rmax) ? src[(long long)gk * ld + gr + i] : zero;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; i++) dst[umma::kmajor_offset(rv + i, k, GT_KC) / 2] = t[i];
+    }
+  }
+}
 constexpr size_t GT_A = (size_t)GT_M * GT_KC * 2, GT_B = (size_t)GT_N * GT_KC * 2;
 constexpr size_t GT_STAGE = GT_A + GT_B;
 constexpr size_t GT_SMEM = 2 * GT_STAGE + 64;
@@ -71,7 +113,6 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const _
   umma::fence_after_sync();
   const uint32_t taddr = *slot;
   const uint32_t idesc = umma::idesc_bf16_f32(GT_M, nt);
-  const __nv_bfloat16 zero = __float2bfloat16(0.f);
   const int nq = (K + GT_KC - 1) / GT_KC;
   bool ok = true;
   for (int q = 0; q < nq; q++) {
@@ -84,34 +125,10 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const _
     __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(sm + st * GT_STAGE);
     __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(sm + st * GT_STAGE + GT_A);
     const int k0 = q * GT_KC;
-    for (int e = tid; e < GT_M * GT_KC; e += blockDim.x) {
-      int r, k;
-      if (transA) {  // consecutive threads walk m (contiguous in memory)
-        r = e % GT_M;
-        k = e / GT_M;
-      } else {
-        r = e / GT_KC;
-        k = e % GT_KC;
-      }
-      const int gm = m0 + r, gk = k0 + k;
-      __nv_bfloat16 v = zero;
-      if (gm < M && gk < K) v = transA ? A[(long long)gk * lda + gm] : A[(long long)gm * lda + gk];
-      As[umma::kmajor_offset(r, k, GT_KC) / 2] = v;
-    }
-    for (int e = tid; e < nt * GT_KC; e += blockDim.x) {
-      int n, k;
-      if (transB) {
-        n = e / GT_KC;
-        k = e % GT_KC;
-      } else {
-        n = e % nt;
-        k = e / nt;
-      }
-      const int gn = n0 + n, gk = k0 + k;
-      __nv_bfloat16 v = zero;
-      if (gn < N && gk < K) v = transB ? B[(long long)gn * ldb + gk] : B[(long long)gk * ldb + gn];
-      Bs[umma::kmajor_offset(n, k, GT_KC) / 2] = v;
-    }
+    // A(m, k): k contiguous in memory unless transposed; B(k, n) as the
+    // N x K operand: k contiguous when transposed
+    stage_tile(As, A, lda, !transA, m0, M, k0, K, GT_M);
+    stage_tile(Bs, B, ldb, transB != 0, n0, N, k0, K, nt);
     umma::fence_async_smem();
     __syncthreads();
     if (tid == 0) {
