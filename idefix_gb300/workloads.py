@@ -172,6 +172,53 @@ def run_cycles(n=128, cycles=2, precision="fp64", seed=1, order="plm", log=sys.s
             "zone_cycles_per_s": n**3 * cycles / el}
 
 
+def run_learned_cycles(n=32, cycles=4, seed=3, scale=0.05, log=sys.stderr):
+    """a few cycles of the learned order (3-D turbulence, HLLD) at n^3 with a
+    seeded random network (weights ~ N(0, scale^2), no trained range): the
+    target of profiles of the learned sweep kernels"""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    nparam = 216 * 128 + 128 + 128 * 128 + 128 + 128 * 16 + 16
+    params = (scale * rng.standard_normal(nparam)).astype(np.float32)
+    Vc, Vs = ic.turbulence_3d(n, seed=seed, kmax=max(1, n // 16))
+    blk = ig.GpuBlock(3, (n, n, n), order="learned", cfl=0.6, first_dt=1e-4)
+    blk.set_learned(params)
+    blk.upload(Vc, Vs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    blk.run(max_cycles=cycles)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    cells, fall = blk.learned_stats()
+    blk.close()
+    return {"n": n, "cycles": cycles, "s": el, "zone_cycles_per_s": n**3 * cycles / el,
+            "cell_evaluations": cells, "fallbacks": fall}
+
+
+def run_train(steps=300, batch=8192, nsnap=64, nc=32, seed=2, log=sys.stderr):
+    """training steps of the learned part's network on a seeded random
+    snapshot store (the tensor-core GEMMs, loss and Adam): time per step, the
+    target of profiles of the training kernels"""
+    import torch
+
+    from idefix_gb300 import learned
+
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    prims = torch.rand((nsnap, 8, nc, nc, nc), dtype=torch.float32, device="cuda", generator=g) + 0.5
+    tg = torch.rand((nsnap, 3, 16, nc**3), dtype=torch.float32, device="cuda", generator=g)
+    tr = learned.Trainer(max_batch=batch)
+    tr.set_dataset(prims, tg)
+    tr.train(20, batch, lr=1e-3, lr_end=1e-4, seed=1)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = tr.train(steps, batch, lr=1e-3, lr_end=1e-4, seed=seed)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    return {"steps": steps, "batch": batch, "s": el, "ms_per_step": el / steps * 1e3,
+            "loss_first": float(np.mean(losses[:5])), "loss_last": float(np.mean(losses[-5:]))}
+
+
 def run_rotor(n=512, tstop=0.15, repeats=2, log=sys.stderr):
     """MHD rotor of test/MHD/RotorCartesian at its ini settings (n^2 cells
     on [-0.5,0.5]^2, Roe, PLM, uct_contact, RK2, CFL 0.2, outflow on all
@@ -419,7 +466,8 @@ if __name__ == "__main__":
     import argparse
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", choices=["ensemble", "learned", "lowbeta", "rotor", "cycles"], default="ensemble")
+    ap.add_argument("--workload", choices=["ensemble", "learned", "lowbeta", "rotor", "cycles", "learned_cycles",
+                                           "train"], default="ensemble")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--order", default="plm")
     ap.add_argument("--n", type=int, default=384)
@@ -448,6 +496,10 @@ if __name__ == "__main__":
         r = run_rotor(a.n if a.n != 384 else 512)
     elif a.workload == "cycles":
         r = run_cycles(a.n, a.cycles or 2, a.precision, order=a.order)
+    elif a.workload == "learned_cycles":
+        r = run_learned_cycles(a.n if a.n != 384 else 32, a.cycles or 4)
+    elif a.workload == "train":
+        r = run_train(a.steps if a.steps != 3000 else 300)
     else:
         pre = None
         if a.load:
