@@ -17,8 +17,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libidefix_gb300.so")
 
-SOURCES = ["engine.cu", "sweep_hlld.cu", "sweep_hll.cu", "sweep_roe.cu", "sweep_tvdlf.cu",
-           "noalloc.cu", "ensemble.cu", "learned.cu", "peak.cu", "dump.cpp"]
+SOURCES = ["sweep_hlld.cu", "sweep_hll.cu", "sweep_roe.cu", "sweep_tvdlf.cu", "persist_hlld.cu", "persist_hll.cu",
+           "persist_roe.cu", "persist_tvdlf.cu", "engine.cu", "noalloc.cu", "ensemble.cu", "learned.cu", "peak.cu",
+           "dump.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xptxas", "-warn-spills"]
@@ -55,6 +56,7 @@ def build_library(verbose=False, jobs=None, extra=()):
         r = subprocess.run(cmd, capture_output=True, text=True, errors="replace")
         return cmd, r
 
+    # the longest units (the sweeps and the persistent kernels) are listed first
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(SOURCES), os.cpu_count() or 4)) as ex:
         for cmd, r in ex.map(run, cmds):
             if verbose or r.returncode:

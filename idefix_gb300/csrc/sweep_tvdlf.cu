@@ -6,8 +6,4 @@ void launch_sweeps_tvdlf(Engine& e, int invdt, int fold_max) { launch_sweeps_sol
 void launch_ens_sweep_tvdlf(EnsEngine& e, int dir, const EnsTable& t, int invdt, int last) {
   launch_ens_sweep_solver<kTVDLF>(e, dir, t, invdt, last);
 }
-cudaError_t launch_ens_persist_tvdlf(EnsEngine& e, int ncyc, int grid) {
-  return launch_ens_persist_solver<kTVDLF>(e, ncyc, grid);
-}
-int ens_persist_blocks_tvdlf(const EnsEngine& e) { return ens_persist_blocks_solver<kTVDLF>(e); }
 }  // namespace idfx
