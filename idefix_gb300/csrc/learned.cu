@@ -6,6 +6,7 @@
 // ABI.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -94,7 +95,8 @@ constexpr size_t GT_SMEM = 2 * GT_STAGE + 64;
 
 __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const __nv_bfloat16* __restrict__ A,
                                                     int lda, int transA, const __nv_bfloat16* __restrict__ B,
-                                                    int ldb, int transB, EpiArgs ep, int* status) {
+                                                    int ldb, int transB, EpiArgs ep, int* status, int cps,
+                                                    float* __restrict__ part) {
   extern __shared__ __align__(128) unsigned char sm[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 2 * GT_STAGE);
   uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 2);
@@ -113,7 +115,10 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const _
   umma::fence_after_sync();
   const uint32_t taddr = *slot;
   const uint32_t idesc = umma::idesc_bf16_f32(GT_M, nt);
-  const int nq = (K + GT_KC - 1) / GT_KC;
+  // split K (blockIdx.z): this CTA's chunks of GT_KC start at q0
+  const int nq_all = (K + GT_KC - 1) / GT_KC;
+  const int q0 = blockIdx.z * cps;
+  const int nq = min(cps, nq_all - q0);
   bool ok = true;
   for (int q = 0; q < nq; q++) {
     const int st = q & 1;
@@ -124,7 +129,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const _
     }
     __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(sm + st * GT_STAGE);
     __nv_bfloat16* Bs = reinterpret_cast<__nv_bfloat16*>(sm + st * GT_STAGE + GT_A);
-    const int k0 = q * GT_KC;
+    const int k0 = (q0 + q) * GT_KC;
     // A(m, k): k contiguous in memory unless transposed; B(k, n) as the
     // N x K operand: k contiguous when transposed
     stage_tile(As, A, lda, !transA, m0, M, k0, K, GT_M);
@@ -155,6 +160,10 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const _
         if (n >= N) continue;
         const long long o = (long long)m * ep.ldo + n;
         float x = v[i];
+        if (part) {  // split K: this split's partial product, summed by k_splitk_sum
+          part[((long long)blockIdx.z * M + m) * N + n] = x;
+          continue;
+        }
         switch (ep.mode) {
           case kEpiF32:
             ep.out_f[o] = x;
@@ -183,12 +192,42 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(int M, int N, int K, const _
   if (warp == 0) umma::tmem_dealloc(taddr, ncols);
 }
 
+// out = sum over the S partial products, in split order (deterministic)
+__global__ void k_splitk_sum(const float* __restrict__ part, int S, int M, int N, float* __restrict__ out, int ldo) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)M * N) return;
+  float acc = 0.f;
+  for (int z = 0; z < S; z++) acc += part[(long long)z * M * N + e];
+  out[(e / N) * ldo + e % N] = acc;
+}
+
+constexpr int GT_MAX_SPLITS = 64;
+// split-K workspace of a trainer: GT_MAX_SPLITS partial products of up to
+// 256 x 128
+constexpr size_t GT_WS_FLOATS = (size_t)GT_MAX_SPLITS * 256 * 128;
+
 // N a multiple of 16 (every use: NH, NOUT); status: set when a bounded wait
-// of the tensor-core pipeline gave up
+// of the tensor-core pipeline gave up.  A product with few output tiles and
+// a long K (the weight gradients: K = the batch) is split over K into up to
+// GT_MAX_SPLITS CTAs per tile, the partial products summed in split order
+// by a second kernel (ws: GT_WS_FLOATS floats).
 void gemm(cudaStream_t s, int M, int N, int K, const __nv_bfloat16* A, int lda, int transA, const __nv_bfloat16* B,
-          int ldb, int transB, const EpiArgs& ep, int* status) {
-  dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M);
-  k_gemm_tc<<<grid, 128, GT_SMEM, s>>>(M, N, K, A, lda, transA, B, ldb, transB, ep, status);
+          int ldb, int transB, const EpiArgs& ep, int* status, float* ws) {
+  dim3 grid((N + GT_N - 1) / GT_N, (M + GT_M - 1) / GT_M, 1);
+  const int nq = (K + GT_KC - 1) / GT_KC;
+  const int tiles = (int)(grid.x * grid.y);
+  int cps = nq;
+  if (ws && ep.mode == kEpiF32 && tiles < 64 && nq >= 4 && (size_t)M * N <= 256 * 128) {
+    int splits = std::min(std::min(GT_MAX_SPLITS, (128 + tiles - 1) / tiles), nq / 2);
+    cps = (nq + splits - 1) / splits;
+    grid.z = (unsigned)((nq + cps - 1) / cps);
+  }
+  float* part = grid.z > 1 ? ws : nullptr;
+  k_gemm_tc<<<grid, 128, GT_SMEM, s>>>(M, N, K, A, lda, transA, B, ldb, transB, ep, status, cps, part);
+  if (part) {
+    const long long mn = (long long)M * N;
+    k_splitk_sum<<<(unsigned)((mn + 255) / 256), 256, 0, s>>>(part, (int)grid.z, M, N, ep.out_f, ep.ldo);
+  }
 }
 
 // column sums (bias gradients): out[n] = sum_m in[m][n]
@@ -914,6 +953,7 @@ struct idfx_mlp {
   double* loss = nullptr;
   unsigned *kmin = nullptr, *kmax = nullptr;
   int* status = nullptr;  // set by a GEMM whose bounded tensor-core wait gave up
+  float* ws = nullptr;    // split-K partial products of the weight-gradient GEMMs
   const float* prims = nullptr;
   const float* tgt = nullptr;
   int nsnap = 0, nc = 0;
@@ -933,18 +973,18 @@ bool dalloc(idfx_mlp* h, P** p, size_t n) {
 // forward + loss + backward of one batch held in h->X / h->T (loss added to *loss)
 void fwd_bwd(idfx_mlp* h, int B, double* loss) {
   cudaStream_t s = h->stream;
-  gemm(s, B, NH, K1, h->X, K1, 0, h->W1b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status);
-  gemm(s, B, NH, NH, h->H1, NH, 0, h->W2b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status);
-  gemm(s, B, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0, EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT}, h->status);
+  gemm(s, B, NH, K1, h->X, K1, 0, h->W1b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status, h->ws);
+  gemm(s, B, NH, NH, h->H1, NH, 0, h->W2b, NH, 0, EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status, h->ws);
+  gemm(s, B, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0, EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT}, h->status, h->ws);
   const int ne = B * NOUT;
   k_loss<<<(ne + 255) / 256, 256, 0, s>>>(h->Y, h->T, B, h->dYf, h->dYb, loss);
-  gemm(s, NH, NOUT, B, h->H2, NH, 1, h->dYb, NOUT, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW3, nullptr, NOUT}, h->status);
+  gemm(s, NH, NOUT, B, h->H2, NH, 1, h->dYb, NOUT, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW3, nullptr, NOUT}, h->status, h->ws);
   k_colsum<<<NOUT, 256, 0, s>>>(h->dYf, B, NOUT, h->g + OB3);
-  gemm(s, B, NH, NOUT, h->dYb, NOUT, 0, h->W3b, NOUT, 1, EpiArgs{kEpiDsilu, nullptr, h->Z2, h->dZ2f, h->dZ2b, NH}, h->status);
-  gemm(s, NH, NH, B, h->H1, NH, 1, h->dZ2b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW2, nullptr, NH}, h->status);
+  gemm(s, B, NH, NOUT, h->dYb, NOUT, 0, h->W3b, NOUT, 1, EpiArgs{kEpiDsilu, nullptr, h->Z2, h->dZ2f, h->dZ2b, NH}, h->status, h->ws);
+  gemm(s, NH, NH, B, h->H1, NH, 1, h->dZ2b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW2, nullptr, NH}, h->status, h->ws);
   k_colsum<<<NH, 256, 0, s>>>(h->dZ2f, B, NH, h->g + OB2);
-  gemm(s, B, NH, NH, h->dZ2b, NH, 0, h->W2b, NH, 1, EpiArgs{kEpiDsilu, nullptr, h->Z1, h->dZ1f, h->dZ1b, NH}, h->status);
-  gemm(s, NIN, NH, B, h->X, K1, 1, h->dZ1b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW1, nullptr, NH}, h->status);
+  gemm(s, B, NH, NH, h->dZ2b, NH, 0, h->W2b, NH, 1, EpiArgs{kEpiDsilu, nullptr, h->Z1, h->dZ1f, h->dZ1b, NH}, h->status, h->ws);
+  gemm(s, NIN, NH, B, h->X, K1, 1, h->dZ1b, NH, 0, EpiArgs{kEpiF32, nullptr, nullptr, h->g + OW1, nullptr, NH}, h->status, h->ws);
   k_colsum<<<NH, 256, 0, s>>>(h->dZ1f, B, NH, h->g + OB1);
 }
 
@@ -1092,7 +1132,8 @@ int idfx_mlp_create(int max_batch, void* stream, idfx_mlp** out) {
             dalloc(h, &h->dZ1b, B * NH) && dalloc(h, &h->T, B * NOUT) && dalloc(h, &h->Z1, B * NH) &&
             dalloc(h, &h->Z2, B * NH) && dalloc(h, &h->Y, B * NOUT) && dalloc(h, &h->dYf, B * NOUT) &&
             dalloc(h, &h->dZ2f, B * NH) && dalloc(h, &h->dZ1f, B * NH) && dalloc(h, &h->loss, 2) &&
-            dalloc(h, &h->kmin, NIN) && dalloc(h, &h->kmax, NIN) && dalloc(h, &h->status, 1);
+            dalloc(h, &h->kmin, NIN) && dalloc(h, &h->kmax, NIN) && dalloc(h, &h->status, 1) &&
+            dalloc(h, &h->ws, GT_WS_FLOATS);
   ok = ok && cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GT_SMEM) ==
                  cudaSuccess;
   if (ok) {
@@ -1190,11 +1231,11 @@ int idfx_mlp_eval(idfx_mlp* h, int batch, unsigned long long seed, double* loss,
   k_make_batch<<<(batch + 127) / 128, 128, 0, h->stream>>>(h->prims, h->tgt, h->nsnap, h->nc, (float)h->gamma, seed,
                                                            0, batch, h->X, h->T, nullptr, nullptr);
   gemm(h->stream, batch, NH, K1, h->X, K1, 0, h->W1b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status);
+       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status, h->ws);
   gemm(h->stream, batch, NH, NH, h->H1, NH, 0, h->W2b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status);
+       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status, h->ws);
   gemm(h->stream, batch, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0,
-       EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT}, h->status);
+       EpiArgs{kEpiBias, h->w + OB3, nullptr, h->Y, nullptr, NOUT}, h->status, h->ws);
   const int ne = batch * NOUT;
   k_loss<<<(ne + 255) / 256, 256, 0, h->stream>>>(h->Y, h->T, batch, h->dYf, h->dYb, h->loss);
   k_sumsq_targets<<<(ne + 255) / 256, 256, 0, h->stream>>>(h->T, batch, h->loss + 1);
@@ -1237,11 +1278,11 @@ int idfx_mlp_forward_device(idfx_mlp* h, const void* X, int batch, float* Y) {
   if (!h || !X || !Y || batch < 1 || batch > h->max_batch) return IDFX_ERR_STATE;
   cudaMemcpyAsync(h->X, X, sizeof(__nv_bfloat16) * (size_t)batch * K1, cudaMemcpyDeviceToDevice, h->stream);
   gemm(h->stream, batch, NH, K1, h->X, K1, 0, h->W1b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status);
+       EpiArgs{kEpiBiasSilu, h->w + OB1, nullptr, h->Z1, h->H1, NH}, h->status, h->ws);
   gemm(h->stream, batch, NH, NH, h->H1, NH, 0, h->W2b, NH, 0,
-       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status);
+       EpiArgs{kEpiBiasSilu, h->w + OB2, nullptr, h->Z2, h->H2, NH}, h->status, h->ws);
   gemm(h->stream, batch, NOUT, NH, h->H2, NH, 0, h->W3b, NOUT, 0, EpiArgs{kEpiBias, h->w + OB3, nullptr, Y, nullptr,
-                                                                           NOUT}, h->status);
+                                                                           NOUT}, h->status, h->ws);
   return sync_ok(h);
 }
 
