@@ -405,7 +405,14 @@ def run_ours(args, world, rank, local):
         mms = max_over_ranks([e0.elapsed_time(e1)], world)[0]
         mixed = {"value": whole_job_rate(cells, args.steps, world, mms * 1e-3), "unit": UNIT,
                  "ms_per_step": mms / args.steps,
-                 "dtype": "f32 recon+Riemann / f64 state", "segments": mblk.segments()}
+                 "dtype": "f32 recon+Riemann / f64 state", "segments": mblk.segments(),
+                 "sweep_kernels": mblk.sweep_kernels()}
+        # per-kernel time of the mixed cycle (separate run, events around each launch)
+        mblk.profile(True)
+        mblk.run(max_cycles=3)
+        mprof = mblk.profile_read()
+        mblk.profile(False)
+        mixed["kernel_ms_per_cycle"] = {k: v[0] / 3 for k, v in mprof.items() if v[1]}
         mblk.close()
 
     out = None

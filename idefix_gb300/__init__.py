@@ -87,7 +87,8 @@ EXPORTS = [
     "idfx_mlp_set_params", "idfx_mlp_get_params", "idfx_mlp_set_dataset_device", "idfx_mlp_train",
     "idfx_mlp_eval", "idfx_mlp_feature_range", "idfx_mlp_batch_device", "idfx_mlp_grad_device",
     "idfx_mlp_forward_device", "idfx_learn_coarsen_device", "idfx_measure_fp64_peak",
-    "idfx_gpu_autotune", "idfx_gpu_get_segments", "idfx_gpu_set_segments", "idfx_check_division",
+    "idfx_gpu_autotune", "idfx_gpu_get_segments", "idfx_gpu_set_segments", "idfx_gpu_get_sweep_kernels",
+    "idfx_gpu_set_sweep_kernels", "idfx_check_division",
     "idfx_check_conversions", "idfx_check_wait_timeout", "idfx_check_umma",
     "idfx_dump_write", "idfx_dump_read",
 ]
@@ -162,6 +163,8 @@ def load_library(path=LIB_PATH):
     lib.idfx_check_umma.argtypes = [ctypes.c_int, ctypes.c_int, fp, fp, fp]
     lib.idfx_gpu_get_segments.argtypes = [P, ctypes.POINTER(I)]
     lib.idfx_gpu_set_segments.argtypes = [P, ctypes.POINTER(I)]
+    lib.idfx_gpu_get_sweep_kernels.argtypes = [P, ctypes.POINTER(I)]
+    lib.idfx_gpu_set_sweep_kernels.argtypes = [P, ctypes.POINTER(I)]
     lib.idfx_gpu_set_learned.argtypes = [P, fp, fp, fp]
     lib.idfx_gpu_learned_states.argtypes = [P, P]
     lib.idfx_gpu_learned_stats.argtypes = [P, ctypes.POINTER(LL), ctypes.POINTER(LL)]
@@ -413,8 +416,21 @@ class GpuBlock:
         self.set_time(t, dt, ncycles)
 
     def autotune(self, reps=3):
-        """pick the march segment length of every sweep direction by timing"""
+        """pick the sweep kernel (march or, for the FP32 y / z sweeps of a 3-D
+        block, tile) and its segment length of every direction by timing"""
         self._check(self.lib.idfx_gpu_autotune(self.h, int(reps)))
+
+    SWEEP_KERNELS = ("march", "tile")
+
+    def sweep_kernels(self):
+        """the sweep kernel of every direction, "march" or "tile" """
+        k = (ctypes.c_int * 3)()
+        self._check(self.lib.idfx_gpu_get_sweep_kernels(self.h, k))
+        return [self.SWEEP_KERNELS[v] for v in k]
+
+    def set_sweep_kernels(self, kinds):
+        k = (ctypes.c_int * 3)(*[self.SWEEP_KERNELS.index(x) for x in (list(kinds) + ["march"] * (3 - len(kinds)))])
+        self._check(self.lib.idfx_gpu_set_sweep_kernels(self.h, k))
 
     def segments(self):
         seg = (ctypes.c_int * 3)()

@@ -14,6 +14,7 @@
 
 #include "../../include/idefix_gb300.h"
 #include "engine.hpp"
+#include "sweep_tile.cuh"
 
 using namespace idfx;
 
@@ -285,6 +286,20 @@ void launch_stage_ghosts(Engine& e, int flags) {
   mark_end(e);
 }
 void launch_ct(Engine& e, int combine, double wc, double w0) {
+  // mixed path: corner EMFs and face update in one pass (the corner EMFs
+  // stay on chip) - for the averages that do not read the face field; the
+  // uct_hll / uct_hlld corner EMFs reconstruct it, and the fused pass
+  // updates it while other tiles still read it
+  if (e.precision == IDFX_MIXED && e.g.emf != kEmfUctHll && e.g.emf != kEmfUctHlld) {
+    const Geo& g = e.g;
+    dim3 grid((unsigned)((g.n[0] + 1 + kCtTI - 1) / kCtTI), (unsigned)((g.n[1] + 1 + kCtTJ - 1) / kCtTJ),
+              (unsigned)(g.D == 3 ? (g.n[2] + 1 + kCtKSeg - 1) / kCtKSeg : 1));
+    mark_begin(e, kKCtFaces);
+    if (g.D == 2) k_ct_fused<2, float><<<grid, dim3(kCtTI, kCtTJ), 0, e.stream>>>(g, e.f, e.ctl, combine, wc, w0);
+    else k_ct_fused<3, float><<<grid, dim3(kCtTI, kCtTJ), 0, e.stream>>>(g, e.f, e.ctl, combine, wc, w0);
+    mark_end(e);
+    return;
+  }
   mark_begin(e, kKCtCorner);
   IDFX_DISPATCH_DE(k_ct_corner, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
   mark_end(e);
@@ -407,6 +422,63 @@ static bool boundaries_valid(const idfx_gpu_config* cfg) {
 }
 
 namespace idfx {
+
+const SweepTileMaps* sweep_tile_maps(Engine& e) {
+  if (e.tile_maps_tried) return e.tile_maps;
+  e.tile_maps_tried = true;
+  const Geo& g = e.g;
+  if (g.D != 3 || e.precision != IDFX_MIXED || g.nt[0] % 4 != 0 || !e.f.Vc32) return nullptr;
+  if ((reinterpret_cast<uintptr_t>(e.f.Vc32) | reinterpret_cast<uintptr_t>(e.f.Uc) |
+       reinterpret_cast<uintptr_t>(e.f.InvDt)) & 15)
+    return nullptr;
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const Encode enc = reinterpret_cast<Encode>(fn);
+  auto* m = new (std::nothrow) SweepTileMaps();
+  if (!m) return nullptr;
+  const cuuint64_t n0 = (cuuint64_t)g.nt[0], n1 = (cuuint64_t)g.nt[1], n2 = (cuuint64_t)g.nt[2];
+  const cuuint64_t nc = (cuuint64_t)g.ncell;
+  const cuuint32_t unit[4] = {1, 1, 1, 1};
+  bool ok = true;
+  for (int d = 0; d < 2; d++) {
+    // y sweep: a box of one y row and kTB z rows; z sweep: kTB y rows and one z row
+    const cuuint32_t by = (d == 0) ? 1 : kTB, bz = (d == 0) ? kTB : 1;
+    const cuuint64_t dims[4] = {n0, n1, n2, 8};
+    const cuuint64_t s4[3] = {n0 * 4, n0 * n1 * 4, nc * 4};
+    const cuuint32_t bv[4] = {kTX, by, bz, 8};
+    ok = ok && enc(&m->vc[d], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, e.f.Vc32, dims, s4, bv, unit,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    const cuuint64_t s8[3] = {n0 * 8, n0 * n1 * 8, nc * 8};
+    const cuuint32_t bu[4] = {kTX, by, bz, 5};
+    ok = ok && enc(&m->uc[d], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, e.f.Uc, dims, s8, bu, unit,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    const cuuint32_t bi[3] = {kTX, by, bz};
+    ok = ok && enc(&m->inv[d], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, e.f.InvDt, dims, s8, bi, unit,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  }
+  if (!ok) {
+    delete m;
+    return nullptr;
+  }
+  e.tile_maps = m;
+  return m;
+}
+
+bool tile_sweep_eligible(Engine& e, int dir) {
+  return (dir == 1 || dir == 2) && e.g.D == 3 && e.precision == IDFX_MIXED && e.g.order >= 2 && e.g.order <= 4 &&
+         sweep_tile_maps(e) != nullptr;
+}
 
 // Validation of a block configuration and the block's grid and geometry:
 // ghost zones (grid.cpp:60-65), cell widths (gridHost.cpp:80-86), face
@@ -659,16 +731,26 @@ int idfx_gpu_autotune(idfx_gpu* h, int reps) {
     // candidates timed in two passes (ascending, then descending), the best
     // of every launch kept per candidate, so that a drift of the clocks or
     // of the cache state during the search favours no candidate
-    int cand[8], nc = 0;
-    float cand_ms[8];
-    for (int s = 4; s <= 64 && s <= e.g.n[d] && nc < 8; s *= 2) {
+    // candidates: march segments 4..64, and for the FP32 y / z sweeps of a
+    // 3-D block the tile sweep with segments 16..256
+    int cand[16], kind[16], nc = 0;
+    float cand_ms[16];
+    for (int s = 4; s <= 64 && s <= e.g.n[d] && nc < 16; s *= 2) {
       cand[nc] = s;
+      kind[nc] = 0;
       cand_ms[nc++] = 1e30f;
     }
+    if (tile_sweep_eligible(e, d))
+      for (int s = 16; s <= 256 && (s <= e.g.n[d] || s == 16) && nc < 16; s *= 2) {
+        cand[nc] = s;
+        kind[nc] = 1;
+        cand_ms[nc++] = 1e30f;
+      }
     for (int pass = 0; pass < 2; pass++) {
       for (int q = 0; q < nc; q++) {
         const int c = pass == 0 ? q : nc - 1 - q;
         e.seg[d] = cand[c];
+        e.tile[d] = kind[c];
         launch_sweeps(e, 2, 0);  // warm-up
         for (int r = 0; r < reps; r++) {
           cudaEventRecord(a, e.stream);
@@ -684,7 +766,10 @@ int idfx_gpu_autotune(idfx_gpu* h, int reps) {
     int best = 0;
     for (int c = 1; c < nc; c++)
       if (cand_ms[c] < cand_ms[best]) best = c;
-    if (nc > 0) e.seg[d] = cand[best];
+    if (nc > 0) {
+      e.seg[d] = cand[best];
+      e.tile[d] = kind[best];
+    }
   }
   e.only_dir = -1;
   e.profile = prof;
@@ -711,6 +796,25 @@ int idfx_gpu_set_segments(idfx_gpu* h, const int* seg) {
 int idfx_gpu_get_segments(const idfx_gpu* h, int* seg) {
   if (!h || !seg) return IDFX_ERR_STATE;
   for (int d = 0; d < 3; d++) seg[d] = h->e.seg[d];
+  return IDFX_OK;
+}
+
+int idfx_gpu_get_sweep_kernels(const idfx_gpu* h, int* kind) {
+  if (!h || !kind) return IDFX_ERR_STATE;
+  for (int d = 0; d < 3; d++) kind[d] = h->e.tile[d] ? IDFX_SWEEP_TILE : IDFX_SWEEP_MARCH;
+  return IDFX_OK;
+}
+
+int idfx_gpu_set_sweep_kernels(idfx_gpu* h, const int* kind) {
+  if (!h || !kind) return IDFX_ERR_STATE;
+  Engine& e = h->e;
+  for (int d = 0; d < e.g.D; d++) {
+    if (kind[d] != IDFX_SWEEP_MARCH && kind[d] != IDFX_SWEEP_TILE) return IDFX_ERR_CONFIG;
+    if (kind[d] == IDFX_SWEEP_TILE && !tile_sweep_eligible(e, d))
+      return fail(e, IDFX_ERR_CONFIG, "the tile sweep serves the y and z sweeps of 3-D mixed-precision blocks "
+                                      "with PLM, LimO3 or PPM and nt0 a multiple of 4");
+  }
+  for (int d = 0; d < e.g.D; d++) e.tile[d] = kind[d] == IDFX_SWEEP_TILE ? 1 : 0;
   return IDFX_OK;
 }
 
@@ -756,6 +860,7 @@ int idfx_gpu_destroy(idfx_gpu* h) {
   }
   for (auto ev : e.free_events) cudaEventDestroy(ev);
   free_learned(e);
+  delete e.tile_maps;
   if (e.pool) cudaFree(e.pool);
   if (e.ctl) cudaFree(e.ctl);
   if (e.ctl_host) cudaFreeHost(e.ctl_host);

@@ -11,6 +11,8 @@
 
 namespace idfx {
 
+struct SweepTileMaps;  // tensor maps of the tile sweeps (sweep_tile.cuh)
+
 struct Engine {
   Geo g{};
   Fields f{};
@@ -39,6 +41,9 @@ struct Engine {
   std::vector<Mark> marks;
   std::vector<cudaEvent_t> free_events;
   void* learned = nullptr;   // network of the learned reconstruction (ORDER 5)
+  int tile[3] = {0, 0, 0};   // 1: the y / z sweep runs as the tile sweep (mixed 3-D), else the march
+  SweepTileMaps* tile_maps = nullptr;
+  bool tile_maps_tried = false;
 };
 
 // kernel classes reported by the per-kernel timing
@@ -66,6 +71,13 @@ void choose_segments(Engine& e);
 cudaEvent_t take_event(Engine& e);
 void mark_begin(Engine& e, int cls);
 void mark_end(Engine& e);
+
+// tensor maps of the tile sweeps, made on first use; null when the block
+// does not qualify (3-D mixed precision, nt0 a multiple of 4, 16-byte
+// aligned arrays) or the driver offers no tensor-map encoder
+const SweepTileMaps* sweep_tile_maps(Engine& e);
+// the y / z sweeps of this block can run as tile sweeps
+bool tile_sweep_eligible(Engine& e, int dir);
 
 // learned sweeps of one stage (ORDER 5: reconstruction with the network's
 // correction, Riemann solve and flux difference in one kernel per

@@ -1291,6 +1291,116 @@ __device__ __forceinline__ E riemann_edge(int order, const double* q, long long 
   return aL * vLv * bL + aR * vRv * bR;
 }
 
+// corner EMF components (corner_emfs MASK)
+enum { kCx = 1, kCy = 2, kCz = 4, kCxyz = 7 };
+
+// The corner EMFs of the edges at cell index c (face index fc): the
+// components in MASK (ez alone in 2-D).  Each component is computed
+// independently of the others.
+template <int D, typename E, int MASK>
+__device__ __forceinline__ void corner_emfs(const Geo& g, const Fields& f, long long c, long long fc, E& exv, E& eyv,
+                                            E& ezv) {
+  constexpr bool CX = (D == 3) && (MASK & kCx) != 0;
+  constexpr bool CY = (D == 3) && (MASK & kCy) != 0;
+  constexpr bool CZ = (MASK & kCz) != 0;
+  const long long si = 1, sj = g.s[1], sk = g.s[2];
+  const E* ezi = emf<E>(f.ezi);
+  const E* ezj = emf<E>(f.ezj);
+  const E *exj = emf<E>(f.exj), *exk = emf<E>(f.exk), *eyi = emf<E>(f.eyi), *eyk = emf<E>(f.eyk);
+  if (g.emf == kEmfUctHll || g.emf == kEmfUctHlld) {
+    const double* Vs1 = f.Vs;
+    const double* Vs2 = f.Vs + g.nface;
+    const E *aL0 = emf<E>(f.aL[0]), *aR0 = emf<E>(f.aR[0]), *dL0 = emf<E>(f.dL[0]), *dR0 = emf<E>(f.dR[0]);
+    const E *aL1 = emf<E>(f.aL[1]), *aR1 = emf<E>(f.aR[1]), *dL1 = emf<E>(f.dL[1]), *dR1 = emf<E>(f.dR[1]);
+    E phi, X;
+    if constexpr (CZ) {
+      X = riemann_edge<E>(g.order, Vs2, fc, 1, ezj, c, si, aL0, aR0, dL0, dR0, sj, phi);
+      ezv = X + phi;
+    }
+    if constexpr (D == 3) {
+      const double* Vs3 = f.Vs + 2 * g.nface;
+      const E *aL2 = emf<E>(f.aL[2]), *aR2 = emf<E>(f.aR[2]), *dL2 = emf<E>(f.dL[2]), *dR2 = emf<E>(f.dR[2]);
+      if constexpr (CY) {
+        X = riemann_edge<E>(g.order, Vs3, fc, 1, eyk, c, si, aL0, aR0, dL0, dR0, sk, phi);
+        eyv = X - phi;
+      }
+      if constexpr (CX) {
+        X = riemann_edge<E>(g.order, Vs3, fc, g.fs[1], exk, c, sj, aL1, aR1, dL1, dR1, sk, phi);
+        exv = X + phi;
+      }
+      if constexpr (CZ) {
+        X = riemann_edge<E>(g.order, Vs1, fc, g.fs[1], ezi, c, sj, aL1, aR1, dL1, dR1, si, phi);
+        ezv += X - phi;
+      }
+      if constexpr (CY) {
+        X = riemann_edge<E>(g.order, Vs1, fc, g.fs[2], eyi, c, sk, aL2, aR2, dL2, dR2, si, phi);
+        eyv += X + phi;
+      }
+      if constexpr (CX) {
+        X = riemann_edge<E>(g.order, Vs2, fc, g.fs[2], exj, c, sk, aL2, aR2, dL2, dR2, sj, phi);
+        exv += X - phi;
+      }
+    } else if constexpr (CZ) {
+      X = riemann_edge<E>(g.order, Vs1, fc, g.fs[1], ezi, c, sj, aL1, aR1, dL1, dR1, si, phi);
+      ezv += X - phi;
+    }
+    return;
+  }
+  const E* Ex1 = emf<E>(f.Ex1);
+  const E* Ex2 = emf<E>(f.Ex2);
+  const E* Ex3 = emf<E>(f.Ex3);
+  if (g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
+    const E w = E(0.25);
+    if (g.emf == kEmfArithmetic) {
+      if constexpr (CX) exv = w * (exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
+      if constexpr (CY) eyv = w * (eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
+      if constexpr (CZ) ezv = w * (ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
+    } else {
+      // CalcUCT0Average: face EMFs become 2 e - (cell EMF average), computed
+      // here for the four faces around the edge (calcCornerEmf.hpp:150-190)
+      const E two = E(2), h = E(0.5);
+      auto mz_i = [&](long long q) { E a = ezi[q] * two; return a - h * (Ex3[q - si] + Ex3[q]); };
+      auto mz_j = [&](long long q) { E a = ezj[q] * two; return a - h * (Ex3[q - sj] + Ex3[q]); };
+      auto mx_j = [&](long long q) { E a = exj[q] * two; return a - h * (Ex1[q - sj] + Ex1[q]); };
+      auto mx_k = [&](long long q) { E a = exk[q] * two; return a - h * (Ex1[q - sk] + Ex1[q]); };
+      auto my_i = [&](long long q) { E a = eyi[q] * two; return a - h * (Ex2[q - si] + Ex2[q]); };
+      auto my_k = [&](long long q) { E a = eyk[q] * two; return a - h * (Ex2[q - sk] + Ex2[q]); };
+      if constexpr (CX) exv = w * (mx_j(c) + mx_j(c - sk) + mx_k(c) + mx_k(c - sj));
+      if constexpr (CY) eyv = w * (my_i(c) + my_i(c - sk) + my_k(c) + my_k(c - si));
+      if constexpr (CZ) ezv = w * (mz_i(c) + mz_i(c - sj) + mz_j(c) + mz_j(c - si));
+    }
+    return;
+  }
+  // uct_contact (calcCornerEmf.hpp:224-282)
+  const E* wsx = emf<E>(f.svx);
+  const E* wsy = emf<E>(f.svy);
+  const E q4 = E(0.25);
+  if constexpr (CZ) {
+    const E ez_l2 = upwind_term(wsx[c - sj], ezj[c] - Ex3[c - sj], ezj[c - si] - Ex3[c - sj - si]);
+    const E ez_r2 = upwind_term(wsx[c], ezj[c] - Ex3[c], ezj[c - si] - Ex3[c - si]);
+    const E ez_l1 = upwind_term(wsy[c - si], ezi[c] - Ex3[c - si], ezi[c - sj] - Ex3[c - sj - si]);
+    const E ez_r1 = upwind_term(wsy[c], ezi[c] - Ex3[c], ezi[c - sj] - Ex3[c - sj]);
+    ezv = q4 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
+  }
+  if constexpr (D == 3) {
+    const E* wsz = emf<E>(f.svz);
+    if constexpr (CX) {
+      const E ex_l3 = upwind_term(wsy[c - sk], exk[c] - Ex1[c - sk], exk[c - sj] - Ex1[c - sk - sj]);
+      const E ex_r3 = upwind_term(wsy[c], exk[c] - Ex1[c], exk[c - sj] - Ex1[c - sj]);
+      const E ex_l2 = upwind_term(wsz[c - sj], exj[c] - Ex1[c - sj], exj[c - sk] - Ex1[c - sk - sj]);
+      const E ex_r2 = upwind_term(wsz[c], exj[c] - Ex1[c], exj[c - sk] - Ex1[c - sk]);
+      exv = q4 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
+    }
+    if constexpr (CY) {
+      const E ey_l3 = upwind_term(wsx[c - sk], eyk[c] - Ex2[c - sk], eyk[c - si] - Ex2[c - sk - si]);
+      const E ey_r3 = upwind_term(wsx[c], eyk[c] - Ex2[c], eyk[c - si] - Ex2[c - si]);
+      const E ey_l1 = upwind_term(wsz[c - si], eyi[c] - Ex2[c - si], eyi[c - sk] - Ex2[c - sk - si]);
+      const E ey_r1 = upwind_term(wsz[c], eyi[c] - Ex2[c], eyi[c - sk] - Ex2[c - sk]);
+      eyv = q4 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
+    }
+  }
+}
+
 template <int D, typename E = double>
 __device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const Ctl* ctl, dim3 bid) {
   if (ctl->done) return;
@@ -1303,96 +1413,13 @@ __device__ __forceinline__ void d_ct_corner(const Geo& g, const Fields& f, const
   const int j = g.beg[1] + (int)(r % ny);
   const int k = (D == 3) ? g.beg[2] + (int)(r / ny) : 0;
   const long long c = cidx(g, k, j, i);
-  const long long si = 1, sj = g.s[1], sk = g.s[2];
-  const E* ezi = emf<E>(f.ezi);
-  const E* ezj = emf<E>(f.ezj);
-  const E *exj = emf<E>(f.exj), *exk = emf<E>(f.exk), *eyi = emf<E>(f.eyi), *eyk = emf<E>(f.eyk);
-  E* ex = emf<E>(f.ex);
-  E* ey = emf<E>(f.ey);
-  E* ez = emf<E>(f.ez);
-  if (g.emf == kEmfUctHll || g.emf == kEmfUctHlld) {
-    const long long fc = fidx(g, k, j, i);
-    const double* Vs1 = f.Vs;
-    const double* Vs2 = f.Vs + g.nface;
-    const E *aL0 = emf<E>(f.aL[0]), *aR0 = emf<E>(f.aR[0]), *dL0 = emf<E>(f.dL[0]), *dR0 = emf<E>(f.dR[0]);
-    const E *aL1 = emf<E>(f.aL[1]), *aR1 = emf<E>(f.aR[1]), *dL1 = emf<E>(f.dL[1]), *dR1 = emf<E>(f.dR[1]);
-    E phi, X, ezv;
-    X = riemann_edge<E>(g.order, Vs2, fc, 1, ezj, c, si, aL0, aR0, dL0, dR0, sj, phi);
-    ezv = X + phi;
-    if constexpr (D == 3) {
-      const double* Vs3 = f.Vs + 2 * g.nface;
-      const E *aL2 = emf<E>(f.aL[2]), *aR2 = emf<E>(f.aR[2]), *dL2 = emf<E>(f.dL[2]), *dR2 = emf<E>(f.dR[2]);
-      E eyv, exv;
-      X = riemann_edge<E>(g.order, Vs3, fc, 1, eyk, c, si, aL0, aR0, dL0, dR0, sk, phi);
-      eyv = X - phi;
-      X = riemann_edge<E>(g.order, Vs3, fc, g.fs[1], exk, c, sj, aL1, aR1, dL1, dR1, sk, phi);
-      exv = X + phi;
-      X = riemann_edge<E>(g.order, Vs1, fc, g.fs[1], ezi, c, sj, aL1, aR1, dL1, dR1, si, phi);
-      ezv += X - phi;
-      X = riemann_edge<E>(g.order, Vs1, fc, g.fs[2], eyi, c, sk, aL2, aR2, dL2, dR2, si, phi);
-      eyv += X + phi;
-      X = riemann_edge<E>(g.order, Vs2, fc, g.fs[2], exj, c, sk, aL2, aR2, dL2, dR2, sj, phi);
-      exv += X - phi;
-      ex[c] = exv;
-      ey[c] = eyv;
-    } else {
-      X = riemann_edge<E>(g.order, Vs1, fc, g.fs[1], ezi, c, sj, aL1, aR1, dL1, dR1, si, phi);
-      ezv += X - phi;
-    }
-    ez[c] = ezv;
-    return;
-  }
-  const E* Ex1 = emf<E>(f.Ex1);
-  const E* Ex2 = emf<E>(f.Ex2);
-  const E* Ex3 = emf<E>(f.Ex3);
-  if (g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
-    const E w = E(0.25);
-    if (g.emf == kEmfArithmetic) {
-      if constexpr (D == 3) {
-        ex[c] = w * (exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
-        ey[c] = w * (eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
-      }
-      ez[c] = w * (ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
-    } else {
-      // CalcUCT0Average: face EMFs become 2 e - (cell EMF average), computed
-      // here for the four faces around the edge (calcCornerEmf.hpp:150-190)
-      const E two = E(2), h = E(0.5);
-      auto mz_i = [&](long long q) { E a = ezi[q] * two; return a - h * (Ex3[q - si] + Ex3[q]); };
-      auto mz_j = [&](long long q) { E a = ezj[q] * two; return a - h * (Ex3[q - sj] + Ex3[q]); };
-      if constexpr (D == 3) {
-        auto mx_j = [&](long long q) { E a = exj[q] * two; return a - h * (Ex1[q - sj] + Ex1[q]); };
-        auto mx_k = [&](long long q) { E a = exk[q] * two; return a - h * (Ex1[q - sk] + Ex1[q]); };
-        auto my_i = [&](long long q) { E a = eyi[q] * two; return a - h * (Ex2[q - si] + Ex2[q]); };
-        auto my_k = [&](long long q) { E a = eyk[q] * two; return a - h * (Ex2[q - sk] + Ex2[q]); };
-        ex[c] = w * (mx_j(c) + mx_j(c - sk) + mx_k(c) + mx_k(c - sj));
-        ey[c] = w * (my_i(c) + my_i(c - sk) + my_k(c) + my_k(c - si));
-      }
-      ez[c] = w * (mz_i(c) + mz_i(c - sj) + mz_j(c) + mz_j(c - si));
-    }
-    return;
-  }
-  // uct_contact (calcCornerEmf.hpp:224-282)
-  const E* wsx = emf<E>(f.svx);
-  const E* wsy = emf<E>(f.svy);
-  const E q4 = E(0.25);
-  const E ez_l2 = upwind_term(wsx[c - sj], ezj[c] - Ex3[c - sj], ezj[c - si] - Ex3[c - sj - si]);
-  const E ez_r2 = upwind_term(wsx[c], ezj[c] - Ex3[c], ezj[c - si] - Ex3[c - si]);
-  const E ez_l1 = upwind_term(wsy[c - si], ezi[c] - Ex3[c - si], ezi[c - sj] - Ex3[c - sj - si]);
-  const E ez_r1 = upwind_term(wsy[c], ezi[c] - Ex3[c], ezi[c - sj] - Ex3[c - sj]);
-  ez[c] = q4 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
+  E exv, eyv, ezv;
+  corner_emfs<D, E, kCxyz>(g, f, c, fidx(g, k, j, i), exv, eyv, ezv);
   if constexpr (D == 3) {
-    const E* wsz = emf<E>(f.svz);
-    const E ex_l3 = upwind_term(wsy[c - sk], exk[c] - Ex1[c - sk], exk[c - sj] - Ex1[c - sk - sj]);
-    const E ex_r3 = upwind_term(wsy[c], exk[c] - Ex1[c], exk[c - sj] - Ex1[c - sj]);
-    const E ex_l2 = upwind_term(wsz[c - sj], exj[c] - Ex1[c - sj], exj[c - sk] - Ex1[c - sk - sj]);
-    const E ex_r2 = upwind_term(wsz[c], exj[c] - Ex1[c], exj[c - sk] - Ex1[c - sk]);
-    ex[c] = q4 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
-    const E ey_l3 = upwind_term(wsx[c - sk], eyk[c] - Ex2[c - sk], eyk[c - si] - Ex2[c - sk - si]);
-    const E ey_r3 = upwind_term(wsx[c], eyk[c] - Ex2[c], eyk[c - si] - Ex2[c - si]);
-    const E ey_l1 = upwind_term(wsz[c - si], eyi[c] - Ex2[c - si], eyi[c - sk] - Ex2[c - sk - si]);
-    const E ey_r1 = upwind_term(wsz[c], eyi[c] - Ex2[c], eyi[c - sk] - Ex2[c - sk]);
-    ey[c] = q4 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
+    emf<E>(f.ex)[c] = exv;
+    emf<E>(f.ey)[c] = eyv;
   }
+  emf<E>(f.ez)[c] = ezv;
 }
 
 template <int D, typename E = double>
@@ -1416,8 +1443,57 @@ __device__ __forceinline__ double rk_combine(double u, double u0, double wc, dou
   return wc * u + w0 * u0;
 }
 
+// Face-field update of the faces at face index fc from the corner EMFs
+// around them: get(comp, off) gives corner EMF component comp (0: x, 1: y,
+// 2: z) of the edge position off (0: this one, 1: +i, 2: +j, 3: +k).
 // E: type of the corner EMFs; they are widened exactly to FP64 and the curl
 // and the face update are FP64 on both paths (div B stays at FP64 round-off)
+template <int D, typename E, typename Get>
+__device__ __forceinline__ void faces_from_corners(const Geo& g, const Fields& f, const Ctl* ctl, long long fc,
+                                                   bool in_i, bool in_j, bool in_k, int combine, double wc, double w0,
+                                                   Get get) {
+  auto Ex1 = [&](int o) { return to_f64(get(0, o)); };
+  auto Ex2 = [&](int o) { return to_f64(get(1, o)); };
+  auto Ex3 = [&](int o) { return to_f64(get(2, o)); };
+  const double dtdx1 = ctl->dtdx[0], dtdx2 = ctl->dtdx[1], dtdx3 = ctl->dtdx[2];
+  // BX1s: faces i in [beg, end], j, k active
+  if (in_j && in_k) {
+    double rhs;
+    // (0.0 - x: the reference's expression; the mixed path negates)
+    const double z = (sizeof(E) == 4) ? -0.0 : 0.0;
+    if constexpr (D == 2) {
+      rhs = z - dtdx2 * (Ex3(2) - Ex3(0));
+    } else {
+      rhs = z - dtdx2 * (Ex3(2) - Ex3(0)) + dtdx3 * (Ex2(3) - Ex2(0));
+    }
+    double* vs = f.Vs;
+    double b = vs[fc] + rhs;
+    if (combine) b = rk_combine<E>(b, f.Vs0[fc], wc, w0);
+    vs[fc] = b;
+  }
+  if (in_i && in_k) {
+    double rhs;
+    if constexpr (D == 2) {
+      rhs = dtdx1 * (Ex3(1) - Ex3(0));
+    } else {
+      rhs = dtdx1 * (Ex3(1) - Ex3(0)) - dtdx3 * (Ex1(3) - Ex1(0));
+    }
+    double* vs = f.Vs + g.nface;
+    double b = vs[fc] + rhs;
+    if (combine) b = rk_combine<E>(b, f.Vs0[g.nface + fc], wc, w0);
+    vs[fc] = b;
+  }
+  if constexpr (D == 3) {
+    if (in_i && in_j) {
+      const double rhs = -dtdx1 * (Ex2(1) - Ex2(0)) + dtdx2 * (Ex1(2) - Ex1(0));
+      double* vs = f.Vs + 2 * g.nface;
+      double b = vs[fc] + rhs;
+      if (combine) b = rk_combine<E>(b, f.Vs0[2 * g.nface + fc], wc, w0);
+      vs[fc] = b;
+    }
+  }
+}
+
 template <int D, typename E = double>
 __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc, double w0, dim3 bid) {
   if (ctl->done) return;
@@ -1430,57 +1506,124 @@ __device__ __forceinline__ void d_ct_faces(const Geo& g, const Fields& f, const 
   const int j = g.beg[1] + (int)(r % ny);
   const int k = (D == 3) ? g.beg[2] + (int)(r / ny) : 0;
   const long long c = cidx(g, k, j, i);
-  const long long fc = fidx(g, k, j, i);
-  const long long si = 1, sj = g.s[1], sk = g.s[2];
-  const E* e1 = emf<E>(f.ex);
-  const E* e2 = emf<E>(f.ey);
-  const E* e3 = emf<E>(f.ez);
-  auto Ex1 = [&](long long q) { return to_f64(e1[q]); };
-  auto Ex2 = [&](long long q) { return to_f64(e2[q]); };
-  auto Ex3 = [&](long long q) { return to_f64(e3[q]); };
-  const double dtdx1 = ctl->dtdx[0], dtdx2 = ctl->dtdx[1], dtdx3 = ctl->dtdx[2];
+  const long long off[4] = {0, 1, g.s[1], g.s[2]};
+  const E* e[3] = {emf<E>(f.ex), emf<E>(f.ey), emf<E>(f.ez)};
   const bool in_i = i < g.end[0], in_j = j < g.end[1], in_k = (D == 2) || k < g.end[2];
-  // BX1s: faces i in [beg, end], j, k active
-  if (in_j && in_k) {
-    double rhs;
-    // (0.0 - x: the reference's expression; the mixed path negates)
-    const double z = (sizeof(E) == 4) ? -0.0 : 0.0;
-    if constexpr (D == 2) {
-      rhs = z - dtdx2 * (Ex3(c + sj) - Ex3(c));
-    } else {
-      rhs = z - dtdx2 * (Ex3(c + sj) - Ex3(c)) + dtdx3 * (Ex2(c + sk) - Ex2(c));
-    }
-    double* vs = f.Vs;
-    double b = vs[fc] + rhs;
-    if (combine) b = rk_combine<E>(b, f.Vs0[fc], wc, w0);
-    vs[fc] = b;
-  }
-  if (in_i && in_k) {
-    double rhs;
-    if constexpr (D == 2) {
-      rhs = dtdx1 * (Ex3(c + si) - Ex3(c));
-    } else {
-      rhs = dtdx1 * (Ex3(c + si) - Ex3(c)) - dtdx3 * (Ex1(c + sk) - Ex1(c));
-    }
-    double* vs = f.Vs + g.nface;
-    double b = vs[fc] + rhs;
-    if (combine) b = rk_combine<E>(b, f.Vs0[g.nface + fc], wc, w0);
-    vs[fc] = b;
-  }
-  if constexpr (D == 3) {
-    if (in_i && in_j) {
-      const double rhs = -dtdx1 * (Ex2(c + si) - Ex2(c)) + dtdx2 * (Ex1(c + sj) - Ex1(c));
-      double* vs = f.Vs + 2 * g.nface;
-      double b = vs[fc] + rhs;
-      if (combine) b = rk_combine<E>(b, f.Vs0[2 * g.nface + fc], wc, w0);
-      vs[fc] = b;
-    }
-  }
+  faces_from_corners<D, E>(g, f, ctl, fidx(g, k, j, i), in_i, in_j, in_k, combine, wc, w0,
+                           [&](int comp, int o) { return e[comp][c + off[o]]; });
 }
 
 template <int D, typename E = double>
 __global__ void k_ct_faces(Geo g, Fields f, const Ctl* ctl, int combine, double wc, double w0) {
   d_ct_faces<D, E>(g, f, ctl, combine, wc, w0, blockIdx);
+}
+
+// ---------------------------------------------------------------------------
+// Corner EMFs fused with the face update (mixed path).  A CTA owns a tile of
+// kCtTI x kCtTJ edge columns (i, j) and marches a segment of k layers: per
+// layer it computes the corner EMFs of its edges - and of the +i column and
+// +j row beyond the tile, which its faces also need (warp 0 the row, the
+// first kCtTJ lanes of warp 1 the column) - into a shared-memory plane, and
+// updates the faces of the layer below from that plane and the k+1 values
+// kept in registers.  Two planes alternate, one barrier per layer.  The
+// arithmetic is corner_emfs and faces_from_corners, as in k_ct_corner +
+// k_ct_faces; the corner EMFs never reach global memory.  Only for the EMF
+// averages that do not read the face field (uct_contact, arithmetic, uct0):
+// the faces of a layer change while the corner EMFs of later layers and of
+// other tiles are still being computed.
+// ---------------------------------------------------------------------------
+constexpr int kCtTI = 32, kCtTJ = 8, kCtKSeg = 32;
+
+// the two alternating planes of corner EMFs (tile plus the +j row and the
+// +i column)
+template <typename E>
+struct CtPlanes {
+  E z[2][kCtTJ + 1][kCtTI + 1];
+  E y[2][kCtTJ][kCtTI + 1];
+  E x[2][kCtTJ + 1][kCtTI];
+};
+// where a thread of the fused CT kernel works
+struct CtPos {
+  int i, j, ti, tj;  // own edge column and its place in the tile
+  bool own;          // the own edge column exists
+  int hkind;         // halo edge: 1 = row beyond the tile (ez, ex), 2 = column (ez, ey), 0 = none
+  int hi, hj;
+  bool halo;         // the halo edge exists
+};
+
+// corner EMFs of layer k: the own edge into (ox, oy, oz) and plane b, the
+// halo edge into plane b
+template <int D, typename E>
+__device__ __forceinline__ void ct_layer(const Geo& g, const Fields& f, CtPlanes<E>& P, const CtPos& p, int k, int b,
+                                         E& ox, E& oy, E& oz) {
+  if (p.own) {
+    corner_emfs<D, E, kCxyz>(g, f, cidx(g, k, p.j, p.i), fidx(g, k, p.j, p.i), ox, oy, oz);
+    P.z[b][p.tj][p.ti] = oz;
+    if constexpr (D == 3) {
+      P.y[b][p.tj][p.ti] = oy;
+      P.x[b][p.tj][p.ti] = ox;
+    }
+  }
+  if (p.halo) {
+    E hx = E(0), hy = E(0), hz = E(0);
+    if (p.hkind == 1) {
+      corner_emfs<D, E, kCz | kCx>(g, f, cidx(g, k, p.hj, p.hi), fidx(g, k, p.hj, p.hi), hx, hy, hz);
+      P.z[b][kCtTJ][p.ti] = hz;
+      if constexpr (D == 3) P.x[b][kCtTJ][p.ti] = hx;
+    } else {
+      corner_emfs<D, E, kCz | kCy>(g, f, cidx(g, k, p.hj, p.hi), fidx(g, k, p.hj, p.hi), hx, hy, hz);
+      P.z[b][p.ti][kCtTI] = hz;
+      if constexpr (D == 3) P.y[b][p.ti][kCtTI] = hy;
+    }
+  }
+}
+
+template <int D, typename E>
+__global__ void __launch_bounds__(kCtTI * kCtTJ, 3) k_ct_fused(Geo g, Fields f, const Ctl* ctl, int combine, double wc,
+                                                           double w0) {
+  if (ctl->done) return;
+  __shared__ CtPlanes<E> P;
+  CtPos p;
+  p.ti = threadIdx.x;
+  p.tj = threadIdx.y;
+  const int i0 = g.beg[0] + (int)blockIdx.x * kCtTI, j0 = g.beg[1] + (int)blockIdx.y * kCtTJ;
+  p.i = i0 + p.ti;
+  p.j = j0 + p.tj;
+  const int ie = g.end[0], je = g.end[1];  // edge positions run over [beg, end]
+  p.own = p.i <= ie && p.j <= je;
+  // warp 0 takes the row j0 + kCtTJ, the first kCtTJ lanes of warp 1 the column i0 + kCtTI
+  p.hkind = (p.tj == 0) ? 1 : (p.tj == 1 && p.ti < kCtTJ) ? 2 : 0;
+  p.hi = (p.hkind == 1) ? p.i : i0 + kCtTI;
+  p.hj = (p.hkind == 1) ? j0 + kCtTJ : j0 + p.ti;
+  p.halo = p.hkind != 0 && p.hi <= ie && p.hj <= je;
+  const int i = p.i, j = p.j, ti = p.ti, tj = p.tj;
+  int k0 = 0, k1 = 1, ke = 0;
+  if constexpr (D == 3) {
+    ke = g.end[2];
+    k0 = g.beg[2] + (int)blockIdx.z * kCtKSeg;
+    k1 = min(k0 + kCtKSeg, ke + 1);  // face layers k0 .. k1-1
+  }
+  E cx = E(0), cy = E(0), cz = E(0);  // own corner EMFs of layer k
+  ct_layer<D, E>(g, f, P, p, k0, 0, cx, cy, cz);
+  __syncthreads();
+  for (int k = k0; k < k1; k++) {
+    const int b = (k - k0) & 1;
+    E nx = E(0), ny = E(0), nz = E(0);  // own corner EMFs of layer k + 1
+    if (D == 3 && k + 1 <= ke) ct_layer<D, E>(g, f, P, p, k + 1, b ^ 1, nx, ny, nz);
+    if (p.own) {
+      const bool in_i = i < ie, in_j = j < je, in_k = (D == 2) || k < ke;
+      faces_from_corners<D, E>(g, f, ctl, fidx(g, k, j, i), in_i, in_j, in_k, combine, wc, w0,
+                               [&](int comp, int o) -> E {
+                                 if (comp == 2) return o == 0 ? cz : (o == 1 ? P.z[b][tj][ti + 1] : P.z[b][tj + 1][ti]);
+                                 if (comp == 1) return o == 0 ? cy : (o == 1 ? P.y[b][tj][ti + 1] : ny);
+                                 return o == 0 ? cx : (o == 2 ? P.x[b][tj + 1][ti] : nx);
+                               });
+    }
+    cx = nx;
+    cy = ny;
+    cz = nz;
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -3,8 +3,25 @@
 #pragma once
 #include "engine.hpp"
 #include "ensemble.hpp"
+#include "sweep_tile.cuh"
 
 namespace idfx {
+
+// the FP32 y or z sweep of a 3-D block as the tile sweep
+template <int DIR, int ORDER, int SOLVER>
+void launch_tile(Engine& e, int invdt, int last, const SweepTileMaps* tm) {
+  const Geo& g = e.g;
+  constexpr int B = (DIR == 2) ? 1 : 2;
+  constexpr int smem = tile_smem<ORDER>();
+  static const bool smem_set =
+      cudaFuncSetAttribute(k_sweep_tile<DIR, ORDER, SOLVER>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) ==
+      cudaSuccess;
+  (void)smem_set;
+  dim3 grid((unsigned)((g.end[0] + g.ext + kTX - 1) / kTX), (unsigned)((g.n[B] + 2 * g.ext + kTB - 1) / kTB),
+            (unsigned)((g.n[DIR] + e.seg[DIR] - 1) / e.seg[DIR]));
+  k_sweep_tile<DIR, ORDER, SOLVER><<<grid, 32 * kTW, smem, e.stream>>>(
+      g, e.f, e.ctl, invdt, last, e.seg[DIR], tm->vc[DIR - 1], tm->uc[DIR - 1], tm->inv[DIR - 1]);
+}
 
 template <int D, int DIR, int ORDER, int SOLVER, typename T>
 void launch_dir(Engine& e, int invdt, int last) {
@@ -27,8 +44,16 @@ void launch_dir(Engine& e, int invdt, int last) {
       k_sweep_xwarp<D, ORDER, SOLVER, T><<<blocks, 32 * kXW, 0, e.stream>>>(g, e.f, e.ctl, invdt, last);
     }
   } else {
-    dim3 grid((unsigned)((cols + kTM - 1) / kTM), nseg, 1);
-    k_sweep_march<D, DIR, ORDER, SOLVER, T><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt, last, e.seg[DIR]);
+    const SweepTileMaps* tm = nullptr;
+    if constexpr (D == 3 && DIR >= 1 && sizeof(T) == 4 && ORDER >= 2 && ORDER <= 4)
+      if (e.tile[DIR]) tm = sweep_tile_maps(e);
+    if (tm) {
+      if constexpr (D == 3 && DIR >= 1 && sizeof(T) == 4 && ORDER >= 2 && ORDER <= 4)
+        launch_tile<DIR, ORDER, SOLVER>(e, invdt, last, tm);
+    } else {
+      dim3 grid((unsigned)((cols + kTM - 1) / kTM), nseg, 1);
+      k_sweep_march<D, DIR, ORDER, SOLVER, T><<<grid, kTM, 0, e.stream>>>(g, e.f, e.ctl, invdt, last, e.seg[DIR]);
+    }
   }
   mark_end(e);
 }

@@ -125,6 +125,9 @@ def run_lowbeta(n=384, cycles=200, seed=0, cfl=0.6, log=sys.stderr):
     for prec in ("fp64", "mixed"):
         blk = ig.GpuBlock(3, (n, n, n), order="limo3", cfl=cfl, first_dt=1e-4, precision=prec)
         blk.upload(Vc, Vs)
+        blk.autotune(2)  # sweep kernels and segments (the state is restored; results do not depend on it)
+        res[prec + "_sweep_kernels"] = blk.sweep_kernels()
+        res[prec + "_segments"] = blk.segments()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         blk.run(max_cycles=cycles)
@@ -152,24 +155,44 @@ def run_lowbeta(n=384, cycles=200, seed=0, cfl=0.6, log=sys.stderr):
     return res
 
 
-def run_cycles(n=128, cycles=2, precision="fp64", seed=1, order="plm", log=sys.stderr):
+def run_cycles(n=128, cycles=2, precision="fp64", seed=1, order="plm", profile=False, sweep=None, segments=None,
+               log=sys.stderr):
     """the 3-D turbulence workload (HLLD + CT uct_contact, RK2, CFL 0.6) at n^3
-    for a few cycles on one block, no autotuning, no other work: the target
-    of per-kernel profiles (ncu -k <kernel> on this command)"""
+    for a few cycles on one block, no other work: the target of per-kernel
+    profiles (ncu -k <kernel> on this command).  sweep: None (the default
+    kernels), "auto" (autotuned), or the kernel of the y and z sweeps
+    ("march", "tile"); segments: march / tile segment per direction.
+    profile: then as many cycles again with CUDA events around every launch,
+    reported as milliseconds per cycle by kernel class"""
     import torch
 
-    Vc, Vs = ic.turbulence_3d(n, seed=seed)
+    ng = 3 if order == "ppm" else 2
+    Vc, Vs = ic.turbulence_3d(n, seed=seed, nghost=ng)
     blk = ig.GpuBlock(3, (n, n, n), order=order, cfl=0.6, first_dt=1e-4, precision=precision)
     blk.upload(Vc, Vs)
+    if segments:
+        blk.set_segments(segments)
+    if sweep == "auto":
+        blk.autotune(2)
+    elif sweep:
+        blk.set_sweep_kernels(["march", sweep, sweep])
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     blk.run(max_cycles=cycles)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
     t, dt, nc = blk.get_time()
+    res = {"n": n, "cycles": nc, "precision": precision, "order": order, "t": t, "s": el,
+           "zone_cycles_per_s": n**3 * cycles / el, "segments": blk.segments(),
+           "sweep_kernels": blk.sweep_kernels()}
+    if profile:
+        blk.profile(True)
+        blk.run(max_cycles=cycles)
+        prof = blk.profile_read()
+        blk.profile(False)
+        res["kernel_ms_per_cycle"] = {k: v[0] / cycles for k, v in prof.items() if v[1]}
     blk.close()
-    return {"n": n, "cycles": nc, "precision": precision, "order": order, "t": t, "s": el,
-            "zone_cycles_per_s": n**3 * cycles / el}
+    return res
 
 
 def run_learned_cycles(n=32, cycles=4, seed=3, scale=0.05, log=sys.stderr):
@@ -484,6 +507,10 @@ if __name__ == "__main__":
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cycles", type=int, default=None, help="default: 500 (ensemble), 200 (lowbeta)")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="cycles: per-kernel milliseconds per cycle")
+    ap.add_argument("--sweep", choices=["march", "tile", "auto"], default=None,
+                    help="cycles: kernel of the y and z sweeps (auto: autotuned)")
+    ap.add_argument("--segments", default=None, help="cycles: comma-separated segment per direction")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--sizes", default=None, help="comma-separated box sizes of the ensemble (default: config 4's)")
     a = ap.parse_args()
@@ -495,7 +522,9 @@ if __name__ == "__main__":
     elif a.workload == "rotor":
         r = run_rotor(a.n if a.n != 384 else 512)
     elif a.workload == "cycles":
-        r = run_cycles(a.n, a.cycles or 2, a.precision, order=a.order)
+        segs = [int(x) for x in a.segments.split(",")] if a.segments else None
+        r = run_cycles(a.n, a.cycles or 2, a.precision, order=a.order, profile=a.profile, sweep=a.sweep,
+                       segments=segs)
     elif a.workload == "learned_cycles":
         r = run_learned_cycles(a.n if a.n != 384 else 32, a.cycles or 4)
     elif a.workload == "train":

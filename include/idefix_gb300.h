@@ -156,12 +156,21 @@ enum {
 int idfx_gpu_profile(idfx_gpu* h, int enable);
 int idfx_gpu_profile_read(idfx_gpu* h, double* ms, long long* launches, int nclasses);
 /* Autotuner (no counterpart in the reference): picks, per sweep direction,
- * the march segment length (cells per thread along the sweep) of the fastest
- * sweep, timed over reps launches; the state is saved and restored, and the
- * results do not depend on the choice.  get/set_segments read and set it. */
+ * the sweep kernel (below) and its segment length (cells per thread or per
+ * tile along the sweep) of the fastest sweep, timed over reps launches; the
+ * state is saved and restored, and the results do not depend on the choice.
+ * get/set_segments read and set the segment lengths. */
 int idfx_gpu_autotune(idfx_gpu* h, int reps);
 int idfx_gpu_get_segments(const idfx_gpu* h, int* seg);
 int idfx_gpu_set_segments(idfx_gpu* h, const int* seg);  /* 1..1024 cells per thread */
+/* Sweep kernel per direction (no counterpart in the reference): the
+ * per-thread march, or for the y and z sweeps of 3-D mixed-precision blocks
+ * (PLM, LimO3, PPM; nt0 a multiple of 4) the tile sweep, whose operands
+ * arrive in shared memory by tensor-map bulk copies.  Both give the same
+ * bits; the autotuner picks the faster one with its segment length. */
+enum { IDFX_SWEEP_MARCH = 0, IDFX_SWEEP_TILE = 1 };
+int idfx_gpu_get_sweep_kernels(const idfx_gpu* h, int* kind);
+int idfx_gpu_set_sweep_kernels(idfx_gpu* h, const int* kind);
 /* measured FP64 FMA throughput of the current device (thread operations
  * per second / 1e9), the roof of the FP64-bound sweeps; stream may be NULL */
 int idfx_measure_fp64_peak(double* gops, void* stream);

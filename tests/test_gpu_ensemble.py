@@ -126,6 +126,38 @@ def test_ensemble_3d_and_mixed_precision():
     _assert_same(res, boxes, cycles=5)
 
 
+# The single mixed-precision block computes the corner EMFs and the face
+# update in one fused pass over tiles of 32 x 8 edge columns marching
+# segments of 32 layers (uct_contact, arithmetic and uct0; uct_hll and
+# uct_hlld, whose corner EMFs read the face field, keep two passes); the
+# ensemble keeps the two separate passes.  Equal bits check the single block
+# against them, for every EMF average and for boxes whose edge counts end
+# inside a tile and a segment (and reach a second segment).
+@pytest.mark.parametrize("emf", ["uct_contact", "arithmetic", "uct0", "uct_hll", "uct_hlld"])
+def test_fused_ct_pass_matches_separate_passes_3d(emf):
+    boxes = []
+    for n, seed in ((40, 4), (33, 5), (9, 6)):
+        Vc, Vs = ic.turbulence_3d(n, seed=seed, kmax=3)
+        boxes.append((dict(dims=3, n=(n, n, n), cfl=0.6, precision="mixed", emf=emf), Vc, Vs))
+    res, err, _ = _ensemble(boxes, cycles=4)
+    assert err is None
+    _assert_same(res, boxes, cycles=4)
+
+
+@pytest.mark.parametrize("emf,order", [("uct_contact", "limo3"), ("uct_hlld", "ppm"), ("uct0", "plm"),
+                                       ("arithmetic", "plm")])
+def test_fused_ct_pass_matches_separate_passes_2d(emf, order):
+    ng = 3 if order == "ppm" else 2
+    boxes = []
+    for n, m, b, c in ((40, 1.2, 0.5, 0.6), (71, 0.7, 3.0, 0.8), (8, 1.0, 1.0, 0.5)):
+        Vc, Vs = ic.orszag_tang_like_2d(n, mach=m, beta=b, nghost=ng)
+        boxes.append((dict(dims=2, n=(n, n), cfl=c, precision="mixed", emf=emf, order=order, first_dt=1e-4),
+                      Vc, Vs))
+    res, err, _ = _ensemble(boxes, cycles=6)
+    assert err is None
+    _assert_same(res, boxes, cycles=6)
+
+
 def test_ensemble_failed_box_leaves_the_others_running():
     boxes = _mixed_boxes()
     # a first_dt far above the CFL step fails at the end of the first cycle

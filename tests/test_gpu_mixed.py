@@ -66,3 +66,47 @@ def test_mixed_turbulence_matches_fp64_closely(solver, order):
     err = _errors(mixed, fp64)
     assert err["RHO"][0] < 1e-5 and err["PRS"][0] < 1e-5, err
     assert divbm < 1e-10
+
+
+# The tile sweep (FP32 y and z sweeps of 3-D blocks, operands staged in
+# shared memory by tensor-map bulk copies) against the per-thread march:
+# the same arithmetic lane for lane, so the runs must be bit-identical - for
+# the three reconstruction orders it serves, segments that end inside the
+# block and cover it whole, and sizes whose columns end inside a 16-column
+# and an 8-row tile (stage 0 accumulates InvDt in the y and z sweeps, stage 1
+# does not).
+@pytest.mark.parametrize("order,n,seg", [("plm", 44, 32), ("plm", 32, 16), ("limo3", 36, 256), ("ppm", 30, 32)])
+def test_tile_sweep_matches_march(order, n, seg):
+    ng = 3 if order == "ppm" else 2
+    Vc, Vs = ic.turbulence_3d(n, seed=11, nghost=ng, kmax=4)
+    out = []
+    for kinds in (["march"] * 3, ["march", "tile", "tile"]):
+        blk = ig.GpuBlock(3, (n, n, n), order=order, cfl=0.6, first_dt=1e-4, precision="mixed")
+        blk.upload(Vc, Vs)
+        blk.set_segments([seg, seg, seg])
+        blk.set_sweep_kernels(kinds)
+        assert blk.sweep_kernels() == kinds
+        blk.run(max_cycles=3)
+        out.append((blk.download(), blk.get_time()))
+        blk.close()
+    (a, ta), (b, tb) = out
+    assert ta == tb
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_tile_sweep_refused_where_it_does_not_apply():
+    # 2-D, FP64, and the x direction run the march only
+    blk = ig.GpuBlock(2, (32, 32), precision="mixed")
+    with pytest.raises(ig.IdefixError):
+        blk.set_sweep_kernels(["march", "tile"])
+    blk.close()
+    blk = ig.GpuBlock(3, (16, 16, 16), precision="fp64")
+    with pytest.raises(ig.IdefixError):
+        blk.set_sweep_kernels(["march", "tile", "tile"])
+    blk.close()
+    blk = ig.GpuBlock(3, (16, 16, 16), precision="mixed")
+    with pytest.raises(ig.IdefixError):
+        blk.set_sweep_kernels(["tile", "march", "march"])
+    blk.set_sweep_kernels(["march", "tile", "march"])
+    assert blk.sweep_kernels() == ["march", "tile", "march"]
+    blk.close()

@@ -273,7 +273,7 @@ def test_autotuned_segments_keep_results(precision):
         blk.upload(Vc, Vs)
         if tune:
             blk.autotune(2)
-            assert all(s in (4, 8, 16, 32, 64) for s in blk.segments())
+            assert all(s in (4, 8, 16, 32, 64, 128, 256) for s in blk.segments())
         blk.run(max_cycles=3)
         out.append((blk.download(), blk.get_time()))
         blk.close()
