@@ -251,6 +251,20 @@ void launch_fill_faces(Engine& e, int save_begin) {
   IDFX_DISPATCH_D(k_fill_faces, grid, kThreads, e.g, e.f, e.ctl, save_begin);
   mark_end(e);
 }
+// the ghost faces alone (periodic block, no Runge-Kutta begin copy due)
+void launch_fill_face_ghosts(Engine& e) {
+  long long slab = 0;
+  for (int comp = 0; comp < e.g.D; comp++)
+    for (int dir = 0; dir < e.g.D; dir++) {
+      long long n = 2LL * e.g.ng;
+      for (int d = 0; d < e.g.D; d++)
+        if (d != dir) n *= (d == comp) ? e.g.nt[d] + 1 : e.g.nt[d];
+      if (n > slab) slab = n;
+    }
+  mark_begin(e, kKFillFaces);
+  IDFX_DISPATCH_D(k_fill_face_ghosts, dim3(nblocks(slab), e.g.D * e.g.D), kThreads, e.g, e.f, e.ctl);
+  mark_end(e);
+}
 // Boundary::SetBoundaries of a block with a reflective or outflow direction
 void launch_boundaries(Engine& e) {
   if (!e.g.nonper) return;
@@ -350,7 +364,10 @@ void queue_cycle(Engine& e, int use_tstop) {
   for (int stage = 0; stage < e.nstages; stage++) {
     const int save = (e.nstages > 1 && stage == 0);
     launch_boundaries(e);
-    launch_fill_faces(e, save);
+    // mixed path, periodic block: a Runge-Kutta begin copy of the faces that
+    // the previous cycle's last face update already wrote leaves the ghosts
+    if (fused && (!save || e.faces_saved)) launch_fill_face_ghosts(e);
+    else launch_fill_faces(e, save);
     // mixed path: Uc carried over from the previous stage end when it is
     // still the state Vc came from (Ctl::uc_fresh); the FP64 path rebuilds it
     // as the reference does
@@ -374,8 +391,13 @@ void queue_cycle(Engine& e, int use_tstop) {
         else
           k_faces_combine<double><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
       }
+      if (fused) e.faces_saved = false;
     } else {
-      launch_ct(e, combine, wc, w0);
+      // mixed path, periodic block: the last stage's face update also
+      // writes the next cycle's Runge-Kutta begin copy of the faces
+      const bool save_next = fused && e.nstages > 1 && stage == e.nstages - 1;
+      launch_ct(e, (combine ? kCtCombine : 0) | (save_next ? kCtSaveBegin : 0), wc, w0);
+      if (save_next) e.faces_saved = true;
     }
     const int out = fused ? (kSeOutputs | (cell_emf ? kSbCellEmf : 0) |
                              (e.nstages > 1 && stage == e.nstages - 1 ? kSeSaveBegin : 0))
@@ -974,6 +996,7 @@ static int run_cycles(idfx_gpu* h, double tstop, long long max_cycles) {
   e.ncycles = e.ctl_host->ncycles;
   ctl_push(e);
   e.stage_outputs = false;  // the run's first stage begin rebuilds from the stored state
+  e.faces_saved = false;    // and its first face fill takes the Runge-Kutta begin copy
   const int use_tstop = tstop >= 0.0;
   long long done = 0;
   const long long chunk = 64;  // host polls t / status every chunk of queued cycles

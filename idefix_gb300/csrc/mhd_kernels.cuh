@@ -169,6 +169,46 @@ __global__ void k_fill_faces(Geo g, Fields f, const Ctl* ctl, int save_begin) {
   d_fill_faces<D>(g, f, ctl, save_begin, blockIdx);
 }
 
+// The ghost faces alone (periodic blocks, when no Runge-Kutta begin copy is
+// due here: later stages, or a first stage whose copy the previous cycle's
+// last face update wrote): the two ghost slabs of direction dir for
+// component comp, bid.y = comp * D + dir, each over the full face box of the
+// other two directions.  Every source is an active face (wrapped in every
+// ghost direction, as k_fill_faces wraps), so no thread reads what another
+// writes; faces in two slabs get the same value from both.
+template <int D>
+__device__ __forceinline__ void d_fill_face_ghosts(const Geo& g, const Fields& f, const Ctl* ctl, dim3 bid) {
+  if (ctl->done) return;
+  const int comp = (int)bid.y / D, dir = (int)bid.y % D;
+  const int a = (dir == 0) ? 1 : 0, b = (dir == 2) ? 1 : 2;
+  int ext[3];  // the face box of component comp without its padding
+  for (int d = 0; d < 3; d++) ext[d] = (d < D) ? (d == comp ? g.nt[d] + 1 : g.nt[d]) : 1;
+  const long long per_side = (long long)g.ng * ext[a] * ext[b];
+  const long long tid = (long long)bid.x * blockDim.x + threadIdx.x;
+  if (tid >= 2 * per_side) return;
+  const int side = (int)(tid / per_side);
+  long long r = tid % per_side;
+  const int layer = (int)(r % g.ng);
+  r /= g.ng;
+  int idx[3];
+  idx[a] = (int)(r % ext[a]);
+  idx[b] = (int)(r / ext[a]);
+  // right ghosts start past the last evolved face (end along comp, end - 1 across)
+  idx[dir] = side ? g.end[dir] + (dir == comp ? 1 : 0) + layer : layer;
+  int src[3] = {idx[0], idx[1], idx[2]};
+  for (int d = 0; d < D; d++) {
+    const int hi = (d == comp) ? g.end[d] : g.end[d] - 1;
+    if (idx[d] < g.beg[d] || idx[d] > hi) src[d] = wrap(idx[d], g.ng, g.n[d]);
+  }
+  double* vs = f.Vs + (long long)comp * g.nface;
+  vs[fidx(g, idx[2], idx[1], idx[0])] = vs[fidx(g, src[2], src[1], src[0])];
+}
+
+template <int D>
+__global__ void k_fill_face_ghosts(Geo g, Fields f, const Ctl* ctl) {
+  d_fill_face_ghosts<D>(g, f, ctl, blockIdx);
+}
+
 // ---------------------------------------------------------------------------
 // Stage begin: ghost cells of Vc (periodic image), cell-centred field from
 // the faces (ReconstructVcField, boundary.hpp:388-404), conservative state of
@@ -1435,10 +1475,15 @@ __global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
 // Runge-Kutta combination wc u + w0 u0 (stateContainer AddAndStore).  The
 // FP64 path keeps the reference's expression; the mixed path (FP32 EMF
 // type) writes equal weights (RK2: 1/2, 1/2) as one product of the sum.
+// combine argument of the face update: kCtCombine = the Runge-Kutta
+// combination with Vs0; kCtSaveBegin (mixed path) = see faces_from_corners
+enum { kCtCombine = 1, kCtSaveBegin = 2 };
+
 template <typename E>
 __device__ __forceinline__ double rk_combine(double u, double u0, double wc, double w0) {
   if constexpr (sizeof(E) == 4) {
-    if (wc == w0) return wc * (u + u0);
+    // RK2's 1/2 (u + u0): the halving exact on the integer pipe
+    if (wc == w0) return wc == 0.5 ? half_of(u + u0) : wc * (u + u0);
   }
   return wc * u + w0 * u0;
 }
@@ -1456,11 +1501,41 @@ __device__ __forceinline__ void faces_from_corners(const Geo& g, const Fields& f
   auto Ex2 = [&](int o) { return to_f64(get(1, o)); };
   auto Ex3 = [&](int o) { return to_f64(get(2, o)); };
   const double dtdx1 = ctl->dtdx[0], dtdx2 = ctl->dtdx[1], dtdx3 = ctl->dtdx[2];
+  if constexpr (sizeof(E) == 4) {
+    // mixed path: the same FP64 curl, each term fused into the face value
+    // (Vs + c1 dE1 + c2 dE2 as two FMAs: 4 FP64 operations per face
+    // instead of 7; the FP64 pipe bounds this pass).  combine bit
+    // kCtSaveBegin: also write the updated face as the next cycle's
+    // Runge-Kutta begin copy (last stage of a cycle)
+    auto put = [&](int comp, double b) {
+      const long long q = comp * g.nface + fc;
+      if (combine & kCtCombine) b = rk_combine<E>(b, f.Vs0[q], wc, w0);
+      f.Vs[q] = b;
+      if (combine & kCtSaveBegin) f.Vs0[q] = b;
+    };
+    if (in_j && in_k) {
+      double b = fma(-dtdx2, Ex3(2) - Ex3(0), f.Vs[fc]);
+      if constexpr (D == 3) b = fma(dtdx3, Ex2(3) - Ex2(0), b);
+      put(0, b);
+    }
+    if (in_i && in_k) {
+      double b = fma(dtdx1, Ex3(1) - Ex3(0), f.Vs[g.nface + fc]);
+      if constexpr (D == 3) b = fma(-dtdx3, Ex1(3) - Ex1(0), b);
+      put(1, b);
+    }
+    if constexpr (D == 3) {
+      if (in_i && in_j) {
+        double b = fma(-dtdx1, Ex2(1) - Ex2(0), f.Vs[2 * g.nface + fc]);
+        b = fma(dtdx2, Ex1(2) - Ex1(0), b);
+        put(2, b);
+      }
+    }
+    return;
+  }
   // BX1s: faces i in [beg, end], j, k active
   if (in_j && in_k) {
     double rhs;
-    // (0.0 - x: the reference's expression; the mixed path negates)
-    const double z = (sizeof(E) == 4) ? -0.0 : 0.0;
+    const double z = 0.0;  // 0.0 - x: the reference's expression
     if constexpr (D == 2) {
       rhs = z - dtdx2 * (Ex3(2) - Ex3(0));
     } else {
@@ -1665,7 +1740,8 @@ __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const
     const double* vs = f.Vs + d * g.nface;
     U[v::BX1 + d] = 0.5 * (vs[fc] + vs[fc + g.fs[d]]);
   }
-  cons_to_prim<D, true>(g.gm1, V, U);
+  // mixed path (E = float): the fused FP64 pressure recovery
+  cons_to_prim<D, true, double, sizeof(E) == 4>(g.gm1, V, U);
 #pragma unroll
   for (int n = 0; n < NV; n++) {
     f.Uc[n * g.ncell + c] = U[n];

@@ -158,10 +158,34 @@ __device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V, T rgm1 = T
   U[v::ENG] = pq + T(0.5) * V[v::RHO] * kin + T(0.5) * mag;
 }
 
-template <int D, bool INTDIV = false, typename T>
+// FUSED (mixed path, FP64 state): the same FP64 pressure recovery with the
+// sums of squares and the two subtractions as fused multiply-adds
+// (p = (E - k m^2 - b^2 / 2) gm1 in 8 FP64 operations instead of 15, each
+// fused step rounding once); the bit-exact path keeps the reference's
+// operations
+template <int D, bool INTDIV = false, typename T, bool FUSED = false>
 __device__ __forceinline__ void cons_to_prim(T gm1, T* V, const T* U) {
   using v = Var<D>;
   auto q = [](T a, T b) { return INTDIV ? dvi(a, b) : dv(a, b); };
+  if constexpr (FUSED) {
+    V[v::RHO] = U[v::RHO];
+    V[v::MX1] = q(U[v::MX1], U[v::RHO]);
+    V[v::MX2] = q(U[v::MX2], U[v::RHO]);
+    if constexpr (D == 3) V[v::MX3] = q(U[v::MX3], U[v::RHO]);
+    V[v::BX1] = U[v::BX1];
+    V[v::BX2] = U[v::BX2];
+    if constexpr (D == 3) V[v::BX3] = U[v::BX3];
+    T m2 = fma(U[v::MX2], U[v::MX2], U[v::MX1] * U[v::MX1]);
+    T b2 = fma(U[v::BX2], U[v::BX2], U[v::BX1] * U[v::BX1]);
+    if constexpr (D == 3) {
+      m2 = fma(U[v::MX3], U[v::MX3], m2);
+      b2 = fma(U[v::BX3], U[v::BX3], b2);
+    }
+    const T e = fma(-q(T(0.5), U[v::RHO]), m2, U[v::ENG]);
+    V[v::PRS] = fma(T(-0.5), b2, e) * gm1;
+    if (V[v::PRS] <= T(0)) V[v::PRS] = T(kSmallPressureFix);
+    return;
+  }
   V[v::RHO] = U[v::RHO];
   V[v::MX1] = q(U[v::MX1], U[v::RHO]);
   V[v::MX2] = q(U[v::MX2], U[v::RHO]);
