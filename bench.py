@@ -294,7 +294,7 @@ def run_ours(args, world, rank, local):
     # the host->device copy of step k+1 and the device->host copy of step
     # k-1 overlap the cycle of step k.  Every byte of every step crosses the
     # host link inside the timed region.
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(3, min(args.steps, 20))
     h_in, h_out, d_in, d_out = [], [], [], []
     first = blk.download()
     for b in range(2):

@@ -108,6 +108,25 @@ __global__ void k_uc_field_all(Geo g, Fields f, int to_prim) {
   for (int n = 0; n < v::NV; n++) f.Vc[n * g.ncell + c] = V[n];
 }
 
+// the cell-centred field of Uc from the faces over the active cells, as the
+// stage end forms it (mixed path, whose stage ends do not store it)
+template <int D>
+__global__ void k_uc_field_active(Geo g, Fields f) {
+  using v = Var<D>;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long tot = (long long)g.n[0] * g.n[1] * (D == 3 ? g.n[2] : 1);
+  if (tid >= tot) return;
+  const int i = g.beg[0] + (int)(tid % g.n[0]);
+  const long long r = tid / g.n[0];
+  const int j = g.beg[1] + (int)(r % g.n[1]);
+  const int k = (D == 3) ? g.beg[2] + (int)(r / g.n[1]) : 0;
+  const long long c = cidx(g, k, j, i), fc = fidx(g, k, j, i);
+  for (int d = 0; d < D; d++) {
+    const double* vs = f.Vs + d * g.nface;
+    f.Uc[(v::BX1 + d) * g.ncell + c] = 0.5 * (vs[fc] + vs[fc + g.fs[d]]);
+  }
+}
+
 // E: type of the EMF buffers (FP32 on the mixed path)
 template <int D, typename E>
 __global__ void k_cell_emf_all(Geo g, Fields f) {
@@ -399,9 +418,10 @@ void queue_cycle(Engine& e, int use_tstop) {
       launch_ct(e, (combine ? kCtCombine : 0) | (save_next ? kCtSaveBegin : 0), wc, w0);
       if (save_next) e.faces_saved = true;
     }
-    const int out = fused ? (kSeOutputs | (cell_emf ? kSbCellEmf : 0) |
+    const int out = fused ? (kSeOutputs | kSeNoUcField | (cell_emf ? kSbCellEmf : 0) |
                              (e.nstages > 1 && stage == e.nstages - 1 ? kSeSaveBegin : 0))
                           : 0;
+    if (fused) e.uc_field_stale = true;
     mark_begin(e, kKStageEnd);
     IDFX_DISPATCH_DE(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0, out);
     mark_end(e);
@@ -949,6 +969,10 @@ int idfx_gpu_download_prim_device(idfx_gpu* h, double* Vc, double* Vs) {
 int idfx_gpu_download_cons(idfx_gpu* h, double* Uc) {
   if (!h || !Uc) return IDFX_ERR_STATE;
   Engine& e = h->e;
+  if (e.uc_field_stale) {  // mixed path: the field part of Uc from the faces
+    IDFX_DISPATCH_D(k_uc_field_active, nblocks(n_active(e.g)), kThreads, e.g, e.f);
+    e.uc_field_stale = false;
+  }
   IDFX_CK(cudaMemcpyAsync(Uc, e.f.Uc, sizeof(double) * (2 * e.g.D + 2) * e.g.ncell, cudaMemcpyDeviceToHost,
                           e.stream));
   IDFX_CK(cudaStreamSynchronize(e.stream));

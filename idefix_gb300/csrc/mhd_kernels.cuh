@@ -1711,7 +1711,10 @@ __global__ void __launch_bounds__(kCtTI * kCtTJ, 3) k_ct_fused(Geo g, Fields f, 
 // derives for the active cells - the FP32 primitives and (kSbCellEmf) the
 // cell EMF - and kSeSaveBegin the Runge-Kutta begin copy of the next cycle
 // (Uc0 = Uc), so that the next stage begin only fills the ghost cells.
-enum { kSeOutputs = 16, kSeSaveBegin = 32 };
+// kSeNoUcField: the cell-centred field is not stored into Uc (the mixed
+// path's sweeps and stage begins read the hydro variables of Uc alone; the
+// host rebuilds the field part from the faces before it hands Uc out).
+enum { kSeOutputs = 16, kSeSaveBegin = 32, kSeNoUcField = 64 };
 template <int D, typename E = double>
 __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const Ctl* ctl, int combine, double wc,
                                             double w0, dim3 bid, int out = 0) {
@@ -1744,7 +1747,7 @@ __device__ __forceinline__ void d_stage_end(const Geo& g, const Fields& f, const
   cons_to_prim<D, true, double, sizeof(E) == 4>(g.gm1, V, U);
 #pragma unroll
   for (int n = 0; n < NV; n++) {
-    f.Uc[n * g.ncell + c] = U[n];
+    if (n < v::BX1 || !(out & kSeNoUcField)) f.Uc[n * g.ncell + c] = U[n];
     f.Vc[n * g.ncell + c] = V[n];
   }
   if (out & kSeOutputs) cell_outputs<D, E>(f, g, c, V, (out & kSbCellEmf) != 0);

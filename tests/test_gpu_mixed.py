@@ -110,3 +110,28 @@ def test_tile_sweep_refused_where_it_does_not_apply():
     blk.set_sweep_kernels(["march", "tile", "march"])
     assert blk.sweep_kernels() == ["march", "tile", "march"]
     blk.close()
+
+
+def test_mixed_download_cons_holds_the_cell_field():
+    # the mixed path's stage ends leave the field part of Uc unstored; the
+    # conserved state handed out must still hold the cell-centred field of
+    # the faces (ReconstructVcField) and the hydro state the primitives came
+    # from
+    n = (24, 24, 24)
+    Vc, Vs = ic.turbulence_3d(24, seed=5, kmax=3)
+    blk = ig.GpuBlock(3, n, precision="mixed", cfl=0.6, first_dt=1e-4)
+    blk.upload(Vc, Vs)
+    blk.run(max_cycles=3)
+    U = blk.download_cons()
+    gVc, gVs = blk.download()
+    blk.close()
+    g = blk.ng
+    a = (slice(g, g + n[2]), slice(g, g + n[1]), slice(g, g + n[0]))
+    bx = 0.5 * (gVs[0][a] + gVs[0][a[0], a[1], slice(g + 1, g + n[0] + 1)])
+    by = 0.5 * (gVs[1][a] + gVs[1][a[0], slice(g + 1, g + n[1] + 1), a[2]])
+    bz = 0.5 * (gVs[2][a] + gVs[2][slice(g + 1, g + n[2] + 1), a[1], a[2]])
+    assert np.array_equal(U[5][a], bx) and np.array_equal(U[6][a], by) and np.array_equal(U[7][a], bz)
+    assert np.array_equal(U[5][a], gVc[5][a]) and np.array_equal(U[7][a], gVc[7][a])
+    assert np.array_equal(U[0][a], gVc[0][a])  # density: the same value in both
+    # velocity: the correctly rounded quotient ConsToPrim takes
+    assert np.array_equal(U[1][a] / U[0][a], gVc[1][a]) and np.array_equal(U[3][a] / U[0][a], gVc[3][a])
