@@ -1653,6 +1653,38 @@ __device__ __forceinline__ void ct_layer(const Geo& g, const Fields& f, CtPlanes
   }
 }
 
+// L2 prefetch of what the corner EMFs (uct_contact, arithmetic, uct0) and
+// the face update of cell c / face fc read at that cell: the fused pass
+// marches layers, so two layers ahead the lines reach L2 before the loads
+// (its warps otherwise wait on DRAM latency at 3 CTAs per SM)
+template <typename E>
+__device__ __forceinline__ void ct_prefetch(const Geo& g, const Fields& f, long long c, long long fc, bool faces0) {
+  // one lane in eight: the lanes of a warp hold consecutive cells, so eight
+  // FP32 values (or four FP64) share a 32-byte sector
+  if (threadIdx.x & 7) return;
+  prefetch_l2(emf<E>(f.ezi) + c);
+  prefetch_l2(emf<E>(f.ezj) + c);
+  prefetch_l2(emf<E>(f.exj) + c);
+  prefetch_l2(emf<E>(f.exk) + c);
+  prefetch_l2(emf<E>(f.eyi) + c);
+  prefetch_l2(emf<E>(f.eyk) + c);
+  prefetch_l2(emf<E>(f.Ex1) + c);
+  prefetch_l2(emf<E>(f.Ex2) + c);
+  prefetch_l2(emf<E>(f.Ex3) + c);
+  prefetch_l2(emf<E>(f.svx) + c);
+  prefetch_l2(emf<E>(f.svy) + c);
+  prefetch_l2(emf<E>(f.svz) + c);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    prefetch_l2(f.Vs + d * g.nface + fc);
+    prefetch_l2(f.Vs + d * g.nface + fc + 4);
+    if (faces0) {
+      prefetch_l2(f.Vs0 + d * g.nface + fc);
+      prefetch_l2(f.Vs0 + d * g.nface + fc + 4);
+    }
+  }
+}
+
 template <int D, typename E>
 __global__ void __launch_bounds__(kCtTI * kCtTJ, 3) k_ct_fused(Geo g, Fields f, const Ctl* ctl, int combine, double wc,
                                                            double w0) {
@@ -1684,6 +1716,11 @@ __global__ void __launch_bounds__(kCtTI * kCtTJ, 3) k_ct_fused(Geo g, Fields f, 
   for (int k = k0; k < k1; k++) {
     const int b = (k - k0) & 1;
     E nx = E(0), ny = E(0), nz = E(0);  // own corner EMFs of layer k + 1
+    if (D == 3 && k + 2 <= ke) {
+      const bool f0 = (combine & (kCtCombine | kCtSaveBegin)) != 0;
+      if (p.own) ct_prefetch<E>(g, f, cidx(g, k + 2, j, i), fidx(g, k + 2, j, i), f0);
+      if (p.halo) ct_prefetch<E>(g, f, cidx(g, k + 2, p.hj, p.hi), fidx(g, k + 2, p.hj, p.hi), false);
+    }
     if (D == 3 && k + 1 <= ke) ct_layer<D, E>(g, f, P, p, k + 1, b ^ 1, nx, ny, nz);
     if (p.own) {
       const bool in_i = i < ie, in_j = j < je, in_k = (D == 2) || k < ke;

@@ -186,6 +186,22 @@ def test_ensemble_2d_mixed_precision():
     _assert_same(res, boxes, cycles=6)
 
 
+# The single mixed block carries its state from stage to stage differently
+# from the ensemble: its stage ends write the next stage's inputs (and leave
+# the field part of Uc unstored), its last face update of a cycle writes the
+# faces' Runge-Kutta begin copy, and its later stage begins and face fills
+# pass over the ghosts alone.  Equal bits check those paths with the
+# diagnostics on (the NaN check reads the primitives), RK3 (other stage
+# weights) and boxes that stop at tstop after different cycle counts.
+@pytest.mark.parametrize("kw,stop", [(dict(log_period=3, check_nan_period=2, nstages=3), dict(cycles=7)),
+                                     (dict(log_period=4, check_nan_period=3), dict(tstop=0.05))])
+def test_ensemble_mixed_precision_with_diagnostics_and_tstop(kw, stop):
+    boxes = _mixed_boxes(precision="mixed", **kw)
+    res, err, _ = _ensemble(boxes, **stop)
+    assert err is None
+    _assert_same(res, boxes, **stop)
+
+
 def test_ensemble_with_shock_flattening():
     boxes = _mixed_boxes(shock_flattening=0.0)
     res, err, _ = _ensemble(boxes, cycles=8)

@@ -135,3 +135,34 @@ def test_mixed_download_cons_holds_the_cell_field():
     assert np.array_equal(U[0][a], gVc[0][a])  # density: the same value in both
     # velocity: the correctly rounded quotient ConsToPrim takes
     assert np.array_equal(U[1][a] / U[0][a], gVc[1][a]) and np.array_equal(U[3][a] / U[0][a], gVc[3][a])
+
+
+def test_mixed_runs_in_pieces_match_one_run():
+    # within a run the mixed path carries its state through the stage ends
+    # (the next stage's inputs, the faces' Runge-Kutta begin copy) and
+    # rebuilds the field part of Uc only when Uc is handed out; a run cut
+    # into pieces - each starting with the full stage begin and face fill -
+    # with or without downloads between them, and the NaN check on, must
+    # give the bits of one uninterrupted run
+    n = (24, 24, 24)
+    Vc, Vs = ic.turbulence_3d(24, seed=7, kmax=3)
+    kw = dict(precision="mixed", cfl=0.6, first_dt=1e-4, check_nan_period=4, log_period=5)
+
+    def run(pieces, peek):
+        blk = ig.GpuBlock(3, n, **kw)
+        blk.upload(Vc, Vs)
+        for p in pieces:
+            blk.run(max_cycles=p)
+            if peek:
+                blk.download()
+                blk.download_cons()
+        out = blk.download()
+        tm = blk.get_time()
+        blk.close()
+        return out, tm
+
+    (a, b), t0 = run([7], False)
+    for pieces, peek in (([3, 4], False), ([2, 1, 4], True)):
+        (c, d), t1 = run(pieces, peek)
+        assert t1 == t0
+        assert np.array_equal(a, c) and np.array_equal(b, d), (pieces, peek)
