@@ -743,6 +743,22 @@ __device__ __forceinline__ void d_sweep_march(const Geo& g, const Fields& f, con
     const bool more = c < m1;
     double curU[v::BX1];
     double curI = 0.0;
+    if constexpr (!PF && DIR != 0) {
+      // FP64: the same L2 prefetch along y and z, kPrefetch steps ahead (the
+      // step's loads are otherwise issued right before their use; measured:
+      // y and z sweeps 35.15 -> 34.90 ms per 256^3 cycle, an L1 prefetch
+      // no better)
+      if (c + kPrefetch + H + 1 < g.nt[DIR]) {
+#pragma unroll
+        for (int n = 0; n < NV; n++)
+          if (n != dd::BXn) prefetch_l2(vcT + n * g.ncell + cc + (kPrefetch + H + 1) * sd);
+        prefetch_l2(vs + f0 + (long long)(c + 1 + kPrefetch - m0) * fsd);
+        if (active_col) {
+#pragma unroll
+          for (int n = 0; n < v::BX1; n++) prefetch_l2(f.Uc + n * g.ncell + cc + kPrefetch * sd);
+        }
+      }
+    }
     if constexpr (PF) {
       // L2 prefetch kPrefetch steps ahead along y (measured: +11 % on the
       // FP32 y sweep; along x consecutive steps share cache lines and the
@@ -1656,7 +1672,8 @@ __device__ __forceinline__ void ct_layer(const Geo& g, const Fields& f, CtPlanes
 // L2 prefetch of what the corner EMFs (uct_contact, arithmetic, uct0) and
 // the face update of cell c / face fc read at that cell: the fused pass
 // marches layers, so two layers ahead the lines reach L2 before the loads
-// (its warps otherwise wait on DRAM latency at 3 CTAs per SM)
+// (its warps otherwise wait on DRAM latency at 3 CTAs per SM; measured:
+// 1.99 -> 1.87 ms per 256^3 mixed cycle, the same with an L1 prefetch)
 template <typename E>
 __device__ __forceinline__ void ct_prefetch(const Geo& g, const Fields& f, long long c, long long fc, bool faces0) {
   // one lane in eight: the lanes of a warp hold consecutive cells, so eight
