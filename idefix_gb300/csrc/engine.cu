@@ -383,9 +383,9 @@ void queue_cycle(Engine& e, int use_tstop) {
   for (int stage = 0; stage < e.nstages; stage++) {
     const int save = (e.nstages > 1 && stage == 0);
     launch_boundaries(e);
-    // mixed path, periodic block: a Runge-Kutta begin copy of the faces that
-    // the previous cycle's last face update already wrote leaves the ghosts
-    if (fused && (!save || e.faces_saved)) launch_fill_face_ghosts(e);
+    // periodic block: a Runge-Kutta begin copy of the faces that the
+    // previous cycle's last face update already wrote leaves the ghosts
+    if (!g.nonper && (!save || e.faces_saved)) launch_fill_face_ghosts(e);
     else launch_fill_faces(e, save);
     // mixed path: Uc carried over from the previous stage end when it is
     // still the state Vc came from (Ctl::uc_fresh); the FP64 path rebuilds it
@@ -410,11 +410,11 @@ void queue_cycle(Engine& e, int use_tstop) {
         else
           k_faces_combine<double><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
       }
-      if (fused) e.faces_saved = false;
+      e.faces_saved = false;
     } else {
-      // mixed path, periodic block: the last stage's face update also
-      // writes the next cycle's Runge-Kutta begin copy of the faces
-      const bool save_next = fused && e.nstages > 1 && stage == e.nstages - 1;
+      // periodic block: the last stage's face update also writes the next
+      // cycle's Runge-Kutta begin copy of the faces
+      const bool save_next = !g.nonper && e.nstages > 1 && stage == e.nstages - 1;
       launch_ct(e, (combine ? kCtCombine : 0) | (save_next ? kCtSaveBegin : 0), wc, w0);
       if (save_next) e.faces_saved = true;
     }

@@ -29,7 +29,7 @@ struct Engine {
   int seg[3] = {32, 32, 32}; // marching segment per direction
   int only_dir = -1;         // >= 0: sweeps launch that direction alone (autotuner)
   bool stage_outputs = false;  // mixed path: a stage end queued in this run wrote the next stage's inputs
-  bool faces_saved = false;    // mixed path: the last face update queued wrote the next cycle's Vs0
+  bool faces_saved = false;    // periodic block: the last face update queued wrote the next cycle's Vs0
   bool uc_field_stale = false; // mixed path: stage ends queued without the field part of Uc
   std::string err;
   double* pool = nullptr;    // one allocation for every field

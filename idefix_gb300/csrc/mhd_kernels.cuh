@@ -1492,7 +1492,9 @@ __global__ void k_ct_corner(Geo g, Fields f, const Ctl* ctl) {
 // FP64 path keeps the reference's expression; the mixed path (FP32 EMF
 // type) writes equal weights (RK2: 1/2, 1/2) as one product of the sum.
 // combine argument of the face update: kCtCombine = the Runge-Kutta
-// combination with Vs0; kCtSaveBegin (mixed path) = see faces_from_corners
+// combination with Vs0; kCtSaveBegin = also write the updated face as the
+// next cycle's Runge-Kutta begin copy (last stage of a cycle, periodic
+// blocks: the next cycle's face fill then passes over the ghosts alone)
 enum { kCtCombine = 1, kCtSaveBegin = 2 };
 
 template <typename E>
@@ -1520,9 +1522,7 @@ __device__ __forceinline__ void faces_from_corners(const Geo& g, const Fields& f
   if constexpr (sizeof(E) == 4) {
     // mixed path: the same FP64 curl, each term fused into the face value
     // (Vs + c1 dE1 + c2 dE2 as two FMAs: 4 FP64 operations per face
-    // instead of 7; the FP64 pipe bounds this pass).  combine bit
-    // kCtSaveBegin: also write the updated face as the next cycle's
-    // Runge-Kutta begin copy (last stage of a cycle)
+    // instead of 7; the FP64 pipe bounds this pass)
     auto put = [&](int comp, double b) {
       const long long q = comp * g.nface + fc;
       if (combine & kCtCombine) b = rk_combine<E>(b, f.Vs0[q], wc, w0);
@@ -1559,8 +1559,9 @@ __device__ __forceinline__ void faces_from_corners(const Geo& g, const Fields& f
     }
     double* vs = f.Vs;
     double b = vs[fc] + rhs;
-    if (combine) b = rk_combine<E>(b, f.Vs0[fc], wc, w0);
+    if (combine & kCtCombine) b = rk_combine<E>(b, f.Vs0[fc], wc, w0);
     vs[fc] = b;
+    if (combine & kCtSaveBegin) f.Vs0[fc] = b;
   }
   if (in_i && in_k) {
     double rhs;
@@ -1571,16 +1572,18 @@ __device__ __forceinline__ void faces_from_corners(const Geo& g, const Fields& f
     }
     double* vs = f.Vs + g.nface;
     double b = vs[fc] + rhs;
-    if (combine) b = rk_combine<E>(b, f.Vs0[g.nface + fc], wc, w0);
+    if (combine & kCtCombine) b = rk_combine<E>(b, f.Vs0[g.nface + fc], wc, w0);
     vs[fc] = b;
+    if (combine & kCtSaveBegin) f.Vs0[g.nface + fc] = b;
   }
   if constexpr (D == 3) {
     if (in_i && in_j) {
       const double rhs = -dtdx1 * (Ex2(1) - Ex2(0)) + dtdx2 * (Ex1(2) - Ex1(0));
       double* vs = f.Vs + 2 * g.nface;
       double b = vs[fc] + rhs;
-      if (combine) b = rk_combine<E>(b, f.Vs0[2 * g.nface + fc], wc, w0);
+      if (combine & kCtCombine) b = rk_combine<E>(b, f.Vs0[2 * g.nface + fc], wc, w0);
       vs[fc] = b;
+      if (combine & kCtSaveBegin) f.Vs0[2 * g.nface + fc] = b;
     }
   }
 }
