@@ -13,6 +13,7 @@
 #include <string>
 
 #include "../../include/idefix_gb300.h"
+#include "ct_tile.cuh"
 #include "engine.hpp"
 #include "sweep_tile.cuh"
 
@@ -328,8 +329,18 @@ void launch_ct(Engine& e, int combine, double wc, double w0) {
     dim3 grid((unsigned)((g.n[0] + 1 + kCtTI - 1) / kCtTI), (unsigned)((g.n[1] + 1 + kCtTJ - 1) / kCtTJ),
               (unsigned)(g.D == 3 ? (g.n[2] + 1 + kCtKSeg - 1) / kCtKSeg : 1));
     mark_begin(e, kKCtFaces);
-    if (g.D == 2) k_ct_fused<2, float><<<grid, dim3(kCtTI, kCtTJ), 0, e.stream>>>(g, e.f, e.ctl, combine, wc, w0);
-    else k_ct_fused<3, float><<<grid, dim3(kCtTI, kCtTJ), 0, e.stream>>>(g, e.f, e.ctl, combine, wc, w0);
+    const CtTileMap* cm = (g.D == 3) ? ct_tile_map(e) : nullptr;
+    if (cm) {
+      // the corner EMFs' inputs staged by tensor-map copies (ct_tile.cuh)
+      static const bool smem_set = cudaFuncSetAttribute(k_ct_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                        ct_tile_smem()) == cudaSuccess;
+      (void)smem_set;
+      k_ct_tile<<<grid, dim3(kCtTI, kCtTJ), ct_tile_smem(), e.stream>>>(g, e.f, e.ctl, combine, wc, w0, cm->emf);
+    } else if (g.D == 2) {
+      k_ct_fused<2, float><<<grid, dim3(kCtTI, kCtTJ), 0, e.stream>>>(g, e.f, e.ctl, combine, wc, w0);
+    } else {
+      k_ct_fused<3, float><<<grid, dim3(kCtTI, kCtTJ), 0, e.stream>>>(g, e.f, e.ctl, combine, wc, w0);
+    }
     mark_end(e);
     return;
   }
@@ -464,6 +475,49 @@ static bool boundaries_valid(const idfx_gpu_config* cfg) {
 }
 
 namespace idfx {
+
+// the staged fused CT pass: a 4-D tensor map (x, y, z, array) over the
+// twelve FP32 EMF inputs of the corner EMFs, consecutive arrays of the pool;
+// null where the block does not allow it (then the unstaged fused pass runs)
+const CtTileMap* ct_tile_map(Engine& e) {
+  if (e.ct_map_tried) return e.ct_map;
+  e.ct_map_tried = true;
+  const Geo& g = e.g;
+  const Fields& f = e.f;
+  if (g.D != 3 || e.precision != IDFX_MIXED || g.nt[0] % 4 != 0) return nullptr;
+  const double* arr[kEaN] = {f.ezi, f.ezj, f.exj, f.exk, f.eyi, f.eyk, f.svx, f.svy, f.svz, f.Ex1, f.Ex2, f.Ex3};
+  for (int q = 0; q < kEaN; q++)
+    if (arr[q] != f.ezi + (long long)q * g.ncell) return nullptr;  // evenly spaced, in this order
+  if ((reinterpret_cast<uintptr_t>(f.ezi) & 15) || (g.ncell * 8) % 16) return nullptr;
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  const Encode enc = reinterpret_cast<Encode>(fn);
+  auto* m = new (std::nothrow) CtTileMap();
+  if (!m) return nullptr;
+  const cuuint64_t n0 = (cuuint64_t)g.nt[0], n1 = (cuuint64_t)g.nt[1], n2 = (cuuint64_t)g.nt[2];
+  const cuuint64_t dims[4] = {n0, n1, n2, (cuuint64_t)kEaN};
+  // FP32 values in the arrays' FP64-sized slots: rows of nt0 floats, arrays
+  // ncell doubles apart
+  const cuuint64_t strides[3] = {n0 * 4, n0 * n1 * 4, (cuuint64_t)g.ncell * 8};
+  const cuuint32_t box[4] = {kCsX, kCsY, 1, kEaN};
+  const cuuint32_t unit[4] = {1, 1, 1, 1};
+  if (enc(&m->emf, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<double*>(f.ezi), dims, strides, box, unit,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
+    delete m;
+    return nullptr;
+  }
+  e.ct_map = m;
+  return m;
+}
 
 const SweepTileMaps* sweep_tile_maps(Engine& e) {
   if (e.tile_maps_tried) return e.tile_maps;
@@ -903,6 +957,7 @@ int idfx_gpu_destroy(idfx_gpu* h) {
   for (auto ev : e.free_events) cudaEventDestroy(ev);
   free_learned(e);
   delete e.tile_maps;
+  delete e.ct_map;
   if (e.pool) cudaFree(e.pool);
   if (e.ctl) cudaFree(e.ctl);
   if (e.ctl_host) cudaFreeHost(e.ctl_host);

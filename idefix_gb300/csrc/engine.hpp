@@ -12,6 +12,7 @@
 namespace idfx {
 
 struct SweepTileMaps;  // tensor maps of the tile sweeps (sweep_tile.cuh)
+struct CtTileMap;      // tensor map of the staged fused CT pass (ct_tile.cuh)
 
 struct Engine {
   Geo g{};
@@ -46,6 +47,8 @@ struct Engine {
   int tile[3] = {0, 0, 0};   // 1: the y / z sweep runs as the tile sweep (mixed 3-D), else the march
   SweepTileMaps* tile_maps = nullptr;
   bool tile_maps_tried = false;
+  CtTileMap* ct_map = nullptr;
+  bool ct_map_tried = false;
 };
 
 // kernel classes reported by the per-kernel timing
@@ -78,6 +81,7 @@ void mark_end(Engine& e);
 // does not qualify (3-D mixed precision, nt0 a multiple of 4, 16-byte
 // aligned arrays) or the driver offers no tensor-map encoder
 const SweepTileMaps* sweep_tile_maps(Engine& e);
+const CtTileMap* ct_tile_map(Engine& e);
 // the y / z sweeps of this block can run as tile sweeps
 bool tile_sweep_eligible(Engine& e, int dir);
 

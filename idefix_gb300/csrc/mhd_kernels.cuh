@@ -1353,6 +1353,80 @@ enum { kCx = 1, kCy = 2, kCz = 4, kCxyz = 7 };
 // The corner EMFs of the edges at cell index c (face index fc): the
 // components in MASK (ez alone in 2-D).  Each component is computed
 // independently of the others.
+// the EMF inputs of the averages, in the order of their arrays in a block's
+// pool (the tensor map of the staged fused CT pass relies on it)
+enum { kEaZi = 0, kEaZj, kEaXj, kEaXk, kEaYi, kEaYk, kEaSx, kEaSy, kEaSz, kEaC1, kEaC2, kEaC3, kEaN };
+
+// corner EMF averages that read face and cell EMFs only (arithmetic, uct0,
+// uct_contact; calcCornerEmf.hpp:14-282): get(array, di, dj, dk) is the
+// input of that array at the edge's cell shifted by (di, dj, dk) (each -1
+// or 0), from global memory or from a staged tile - the arithmetic is one
+template <int D, typename E, int MASK, typename Get>
+__device__ __forceinline__ void corner_emfs_avg(int emf_mode, Get get, E& exv, E& eyv, E& ezv) {
+  constexpr bool CX = (D == 3) && (MASK & kCx) != 0;
+  constexpr bool CY = (D == 3) && (MASK & kCy) != 0;
+  constexpr bool CZ = (MASK & kCz) != 0;
+  auto ezi = [&](int di, int dj, int dk) { return get(kEaZi, di, dj, dk); };
+  auto ezj = [&](int di, int dj, int dk) { return get(kEaZj, di, dj, dk); };
+  auto exj = [&](int di, int dj, int dk) { return get(kEaXj, di, dj, dk); };
+  auto exk = [&](int di, int dj, int dk) { return get(kEaXk, di, dj, dk); };
+  auto eyi = [&](int di, int dj, int dk) { return get(kEaYi, di, dj, dk); };
+  auto eyk = [&](int di, int dj, int dk) { return get(kEaYk, di, dj, dk); };
+  auto Ex1 = [&](int di, int dj, int dk) { return get(kEaC1, di, dj, dk); };
+  auto Ex2 = [&](int di, int dj, int dk) { return get(kEaC2, di, dj, dk); };
+  auto Ex3 = [&](int di, int dj, int dk) { return get(kEaC3, di, dj, dk); };
+  if (emf_mode == kEmfArithmetic || emf_mode == kEmfUct0) {
+    const E w = E(0.25);
+    if (emf_mode == kEmfArithmetic) {
+      if constexpr (CX) exv = w * (exj(0, 0, 0) + exj(0, 0, -1) + exk(0, 0, 0) + exk(0, -1, 0));
+      if constexpr (CY) eyv = w * (eyi(0, 0, 0) + eyi(0, 0, -1) + eyk(0, 0, 0) + eyk(-1, 0, 0));
+      if constexpr (CZ) ezv = w * (ezi(0, 0, 0) + ezi(0, -1, 0) + ezj(0, 0, 0) + ezj(-1, 0, 0));
+    } else {
+      // CalcUCT0Average: face EMFs become 2 e - (cell EMF average), computed
+      // here for the four faces around the edge (calcCornerEmf.hpp:150-190)
+      const E two = E(2), h = E(0.5);
+      auto mz_i = [&](int dj) { E a = ezi(0, dj, 0) * two; return a - h * (Ex3(-1, dj, 0) + Ex3(0, dj, 0)); };
+      auto mz_j = [&](int di) { E a = ezj(di, 0, 0) * two; return a - h * (Ex3(di, -1, 0) + Ex3(di, 0, 0)); };
+      auto mx_j = [&](int dj, int dk) { E a = exj(0, dj, dk) * two; return a - h * (Ex1(0, dj - 1, dk) + Ex1(0, dj, dk)); };
+      auto mx_k = [&](int dj, int dk) { E a = exk(0, dj, dk) * two; return a - h * (Ex1(0, dj, dk - 1) + Ex1(0, dj, dk)); };
+      auto my_i = [&](int di, int dk) { E a = eyi(di, 0, dk) * two; return a - h * (Ex2(di - 1, 0, dk) + Ex2(di, 0, dk)); };
+      auto my_k = [&](int di, int dk) { E a = eyk(di, 0, dk) * two; return a - h * (Ex2(di, 0, dk - 1) + Ex2(di, 0, dk)); };
+      if constexpr (CX) exv = w * (mx_j(0, 0) + mx_j(0, -1) + mx_k(0, 0) + mx_k(-1, 0));
+      if constexpr (CY) eyv = w * (my_i(0, 0) + my_i(0, -1) + my_k(0, 0) + my_k(-1, 0));
+      if constexpr (CZ) ezv = w * (mz_i(0) + mz_i(-1) + mz_j(0) + mz_j(-1));
+    }
+    return;
+  }
+  // uct_contact (calcCornerEmf.hpp:224-282)
+  auto wsx = [&](int di, int dj, int dk) { return get(kEaSx, di, dj, dk); };
+  auto wsy = [&](int di, int dj, int dk) { return get(kEaSy, di, dj, dk); };
+  const E q4 = E(0.25);
+  if constexpr (CZ) {
+    const E ez_l2 = upwind_term(wsx(0, -1, 0), ezj(0, 0, 0) - Ex3(0, -1, 0), ezj(-1, 0, 0) - Ex3(-1, -1, 0));
+    const E ez_r2 = upwind_term(wsx(0, 0, 0), ezj(0, 0, 0) - Ex3(0, 0, 0), ezj(-1, 0, 0) - Ex3(-1, 0, 0));
+    const E ez_l1 = upwind_term(wsy(-1, 0, 0), ezi(0, 0, 0) - Ex3(-1, 0, 0), ezi(0, -1, 0) - Ex3(-1, -1, 0));
+    const E ez_r1 = upwind_term(wsy(0, 0, 0), ezi(0, 0, 0) - Ex3(0, 0, 0), ezi(0, -1, 0) - Ex3(0, -1, 0));
+    ezv = q4 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi(0, 0, 0) + ezi(0, -1, 0) + ezj(0, 0, 0) + ezj(-1, 0, 0));
+  }
+  if constexpr (D == 3) {
+    auto wsz = [&](int di, int dj, int dk) { return get(kEaSz, di, dj, dk); };
+    if constexpr (CX) {
+      const E ex_l3 = upwind_term(wsy(0, 0, -1), exk(0, 0, 0) - Ex1(0, 0, -1), exk(0, -1, 0) - Ex1(0, -1, -1));
+      const E ex_r3 = upwind_term(wsy(0, 0, 0), exk(0, 0, 0) - Ex1(0, 0, 0), exk(0, -1, 0) - Ex1(0, -1, 0));
+      const E ex_l2 = upwind_term(wsz(0, -1, 0), exj(0, 0, 0) - Ex1(0, -1, 0), exj(0, 0, -1) - Ex1(0, -1, -1));
+      const E ex_r2 = upwind_term(wsz(0, 0, 0), exj(0, 0, 0) - Ex1(0, 0, 0), exj(0, 0, -1) - Ex1(0, 0, -1));
+      exv = q4 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj(0, 0, 0) + exj(0, 0, -1) + exk(0, 0, 0) + exk(0, -1, 0));
+    }
+    if constexpr (CY) {
+      const E ey_l3 = upwind_term(wsx(0, 0, -1), eyk(0, 0, 0) - Ex2(0, 0, -1), eyk(-1, 0, 0) - Ex2(-1, 0, -1));
+      const E ey_r3 = upwind_term(wsx(0, 0, 0), eyk(0, 0, 0) - Ex2(0, 0, 0), eyk(-1, 0, 0) - Ex2(-1, 0, 0));
+      const E ey_l1 = upwind_term(wsz(-1, 0, 0), eyi(0, 0, 0) - Ex2(-1, 0, 0), eyi(0, 0, -1) - Ex2(-1, 0, -1));
+      const E ey_r1 = upwind_term(wsz(0, 0, 0), eyi(0, 0, 0) - Ex2(0, 0, 0), eyi(0, 0, -1) - Ex2(0, 0, -1));
+      eyv = q4 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi(0, 0, 0) + eyi(0, 0, -1) + eyk(0, 0, 0) + eyk(-1, 0, 0));
+    }
+  }
+}
+
 template <int D, typename E, int MASK>
 __device__ __forceinline__ void corner_emfs(const Geo& g, const Fields& f, long long c, long long fc, E& exv, E& eyv,
                                             E& ezv) {
@@ -1402,59 +1476,13 @@ __device__ __forceinline__ void corner_emfs(const Geo& g, const Fields& f, long 
     }
     return;
   }
-  const E* Ex1 = emf<E>(f.Ex1);
-  const E* Ex2 = emf<E>(f.Ex2);
-  const E* Ex3 = emf<E>(f.Ex3);
-  if (g.emf == kEmfArithmetic || g.emf == kEmfUct0) {
-    const E w = E(0.25);
-    if (g.emf == kEmfArithmetic) {
-      if constexpr (CX) exv = w * (exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
-      if constexpr (CY) eyv = w * (eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
-      if constexpr (CZ) ezv = w * (ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
-    } else {
-      // CalcUCT0Average: face EMFs become 2 e - (cell EMF average), computed
-      // here for the four faces around the edge (calcCornerEmf.hpp:150-190)
-      const E two = E(2), h = E(0.5);
-      auto mz_i = [&](long long q) { E a = ezi[q] * two; return a - h * (Ex3[q - si] + Ex3[q]); };
-      auto mz_j = [&](long long q) { E a = ezj[q] * two; return a - h * (Ex3[q - sj] + Ex3[q]); };
-      auto mx_j = [&](long long q) { E a = exj[q] * two; return a - h * (Ex1[q - sj] + Ex1[q]); };
-      auto mx_k = [&](long long q) { E a = exk[q] * two; return a - h * (Ex1[q - sk] + Ex1[q]); };
-      auto my_i = [&](long long q) { E a = eyi[q] * two; return a - h * (Ex2[q - si] + Ex2[q]); };
-      auto my_k = [&](long long q) { E a = eyk[q] * two; return a - h * (Ex2[q - sk] + Ex2[q]); };
-      if constexpr (CX) exv = w * (mx_j(c) + mx_j(c - sk) + mx_k(c) + mx_k(c - sj));
-      if constexpr (CY) eyv = w * (my_i(c) + my_i(c - sk) + my_k(c) + my_k(c - si));
-      if constexpr (CZ) ezv = w * (mz_i(c) + mz_i(c - sj) + mz_j(c) + mz_j(c - si));
-    }
-    return;
-  }
-  // uct_contact (calcCornerEmf.hpp:224-282)
-  const E* wsx = emf<E>(f.svx);
-  const E* wsy = emf<E>(f.svy);
-  const E q4 = E(0.25);
-  if constexpr (CZ) {
-    const E ez_l2 = upwind_term(wsx[c - sj], ezj[c] - Ex3[c - sj], ezj[c - si] - Ex3[c - sj - si]);
-    const E ez_r2 = upwind_term(wsx[c], ezj[c] - Ex3[c], ezj[c - si] - Ex3[c - si]);
-    const E ez_l1 = upwind_term(wsy[c - si], ezi[c] - Ex3[c - si], ezi[c - sj] - Ex3[c - sj - si]);
-    const E ez_r1 = upwind_term(wsy[c], ezi[c] - Ex3[c], ezi[c - sj] - Ex3[c - sj]);
-    ezv = q4 * (ez_l2 + ez_r2 + ez_l1 + ez_r1 + ezi[c] + ezi[c - sj] + ezj[c] + ezj[c - si]);
-  }
-  if constexpr (D == 3) {
-    const E* wsz = emf<E>(f.svz);
-    if constexpr (CX) {
-      const E ex_l3 = upwind_term(wsy[c - sk], exk[c] - Ex1[c - sk], exk[c - sj] - Ex1[c - sk - sj]);
-      const E ex_r3 = upwind_term(wsy[c], exk[c] - Ex1[c], exk[c - sj] - Ex1[c - sj]);
-      const E ex_l2 = upwind_term(wsz[c - sj], exj[c] - Ex1[c - sj], exj[c - sk] - Ex1[c - sk - sj]);
-      const E ex_r2 = upwind_term(wsz[c], exj[c] - Ex1[c], exj[c - sk] - Ex1[c - sk]);
-      exv = q4 * (ex_l3 + ex_r3 + ex_l2 + ex_r2 + exj[c] + exj[c - sk] + exk[c] + exk[c - sj]);
-    }
-    if constexpr (CY) {
-      const E ey_l3 = upwind_term(wsx[c - sk], eyk[c] - Ex2[c - sk], eyk[c - si] - Ex2[c - sk - si]);
-      const E ey_r3 = upwind_term(wsx[c], eyk[c] - Ex2[c], eyk[c - si] - Ex2[c - si]);
-      const E ey_l1 = upwind_term(wsz[c - si], eyi[c] - Ex2[c - si], eyi[c - sk] - Ex2[c - sk - si]);
-      const E ey_r1 = upwind_term(wsz[c], eyi[c] - Ex2[c], eyi[c - sk] - Ex2[c - sk]);
-      eyv = q4 * (ey_l3 + ey_r3 + ey_l1 + ey_r1 + eyi[c] + eyi[c - sk] + eyk[c] + eyk[c - si]);
-    }
-  }
+  // arithmetic, uct0, uct_contact: the inputs at this cell and its -i, -j,
+  // -k neighbours, by array (kEa*) and offset
+  const E* a[12] = {ezi, ezj, exj, exk, eyi, eyk, emf<E>(f.svx), emf<E>(f.svy), emf<E>(f.svz),
+                    emf<E>(f.Ex1), emf<E>(f.Ex2), emf<E>(f.Ex3)};
+  corner_emfs_avg<D, E, MASK>(g.emf, [&](int q, int di, int dj, int dk) -> E {
+    return a[q][c + di * si + dj * sj + dk * sk];
+  }, exv, eyv, ezv);
 }
 
 template <int D, typename E = double>
