@@ -111,11 +111,24 @@ __device__ __forceinline__ T dvi(T a, T b) {
   }
 }
 
+// a b + c: one fused multiply-add on the FP32 (mixed) path; on the FP64
+// path the product and the sum, rounded separately as the reference
+// evaluates them (the library is built without FMA contraction), so that
+// every FP64 expression written with it keeps the reference's bits
+template <typename T>
+__device__ __forceinline__ T mad(T a, T b, T c) {
+  if constexpr (sizeof(T) == 4) {
+    return fmaf(a, b, c);
+  } else {
+    return a * b + c;
+  }
+}
+
 // sum of squares of the first D entries, in reference order
 template <int D, typename T>
 __device__ __forceinline__ T sumsq(T a, T b, T c) {
-  T s = a * a + b * b;
-  if constexpr (D == 3) s = s + c * c;
+  T s = mad(b, b, a * a);
+  if constexpr (D == 3) s = mad(c, c, s);
   return s;
 }
 
@@ -155,7 +168,7 @@ __device__ __forceinline__ void prim_to_cons(T gm1, T* U, const T* V, T rgm1 = T
     (void)rgm1;
     pq = dv(V[v::PRS], gm1);
   }
-  U[v::ENG] = pq + T(0.5) * V[v::RHO] * kin + T(0.5) * mag;
+  U[v::ENG] = mad(T(0.5), mag, mad(T(0.5) * V[v::RHO], kin, pq));
 }
 
 // FUSED (mixed path, FP64 state): the same FP64 pressure recovery with the
@@ -214,12 +227,12 @@ __device__ __forceinline__ void cons_to_prim(T gm1, T* V, const T* U) {
 template <int D, int DIR, typename T>
 __device__ __forceinline__ T flux_bt(const T* V) {
   using d = Dir<D, DIR>;
-  return V[d::Xn] * V[d::BXt] - V[d::BXn] * V[d::Xt];
+  return mad(V[d::Xn], V[d::BXt], -(V[d::BXn] * V[d::Xt]));
 }
 template <int D, int DIR, typename T>
 __device__ __forceinline__ T flux_bb(const T* V) {
   using d = Dir<D, DIR>;
-  return V[d::Xn] * V[d::BXb] - V[d::BXn] * V[d::Xb];
+  return mad(V[d::Xn], V[d::BXb], -(V[d::BXn] * V[d::Xb]));
 }
 
 // physical MHD flux along DIR (flux.hpp:28-95); U is read before F is written
@@ -232,22 +245,22 @@ __device__ __forceinline__ void phys_flux(T* F, const T* V, const T* U) {
   T u3 = T(0);
   if constexpr (D == 3) u3 = U[v::MX3];
   F[v::RHO] = uXn;
-  F[v::MX1] = u1 * V[d::Xn] - V[d::BXn] * V[v::BX1];
-  F[v::MX2] = u2 * V[d::Xn] - V[d::BXn] * V[v::BX2];
-  if constexpr (D == 3) F[v::MX3] = u3 * V[d::Xn] - V[d::BXn] * V[v::BX3];
+  F[v::MX1] = mad(u1, V[d::Xn], -(V[d::BXn] * V[v::BX1]));
+  F[v::MX2] = mad(u2, V[d::Xn], -(V[d::BXn] * V[v::BX2]));
+  if constexpr (D == 3) F[v::MX3] = mad(u3, V[d::Xn], -(V[d::BXn] * V[v::BX3]));
   F[d::BXn] = T(0);
   F[d::BXt] = flux_bt<D, DIR>(V);
   if constexpr (D == 3) F[d::BXb] = flux_bb<D, DIR>(V);
   T Bmag2, vB;
   if constexpr (D == 3) {
     Bmag2 = sumsq<3>(V[v::BX1], V[v::BX2], V[v::BX3]);
-    vB = V[v::MX1] * V[v::BX1] + V[v::MX2] * V[v::BX2] + V[v::MX3] * V[v::BX3];
+    vB = mad(V[v::MX3], V[v::BX3], mad(V[v::MX2], V[v::BX2], V[v::MX1] * V[v::BX1]));
   } else {
     Bmag2 = sumsq<2>(V[v::BX1], V[v::BX2], T(0));
-    vB = V[v::MX1] * V[v::BX1] + V[v::MX2] * V[v::BX2];
+    vB = mad(V[v::MX2], V[v::BX2], V[v::MX1] * V[v::BX1]);
   }
-  const T ptot = V[v::PRS] + T(0.5) * Bmag2;
-  F[v::ENG] = (uE + ptot) * V[d::Xn] - V[d::BXn] * (vB);
+  const T ptot = mad(T(0.5), Bmag2, V[v::PRS]);
+  F[v::ENG] = mad(uE + ptot, V[d::Xn], -(V[d::BXn] * (vB)));
   F[d::Xn] += ptot;
 }
 
@@ -406,8 +419,8 @@ struct Recon {
       const T dvm = w[1] - w[0];
       const T dvp = w[2] - w[1];
       const T d = shock ? lim_minmod(dvp, dvm) : lim_vanleer(dvp, dvm, ipipe);
-      vr = w[1] + T(0.5) * d;
-      vl = w[1] - T(0.5) * d;
+      vr = mad(T(0.5), d, w[1]);
+      vl = mad(T(-0.5), d, w[1]);
     } else if constexpr (ORDER == 3) {
       const T dm = w[1] - w[0];
       const T dp = w[2] - w[1];
@@ -480,10 +493,10 @@ __device__ __forceinline__ T fast_speed(T gamma, const T* v) {
   const T b2 = v[d::BXt];
   T b3 = T(0);
   if constexpr (D == 3) b3 = v[d::BXb];
-  const T Btmag2 = b2 * b2 + b3 * b3;
-  const T Bmag2 = b1 * b1 + Btmag2;
+  const T Btmag2 = mad(b3, b3, b2 * b2);
+  const T Bmag2 = mad(b1, b1, Btmag2);
   T c = gpr - Bmag2;
-  c = gpr + Bmag2 + sqr(c * c + T(4) * gpr * Btmag2);
+  c = gpr + Bmag2 + sqr(mad(T(4) * gpr, Btmag2, c * c));
   c = sqr(dv(T(0.5) * c, v[vv::RHO]));
   return c;
 }
@@ -678,12 +691,12 @@ __device__ __forceinline__ void riemann_hlld(T gamma, T rgm1, const T* vL, const
     uss[ENG] = us[ENG] + times_sign(sq * scrh, sgn, sgnb);
     const T S1 = sideL ? S1L : S1R;
 #pragma unroll
-    for (int n = 0; n < NV; n++) F[n] = F[n] + S1 * (uss[n] - us[n]);
+    for (int n = 0; n < NV; n++) F[n] = mad(S1, uss[n] - us[n], F[n]);
   }
   // F += s (us - u) of the chosen side: single star F = Fs + s (us - u),
   // double star F = (Fs + S1 (uss - us)) + s (us - u), the reference's order
 #pragma unroll
-  for (int n = 0; n < NV; n++) F[n] = F[n] + s * (us[n] - uS[n]);
+  for (int n = 0; n < NV; n++) F[n] = mad(s, us[n] - uS[n], F[n]);
 }
 
 // HLL (hllMHD.hpp:154-453; the Hall whistler term is not part of ideal MHD)
