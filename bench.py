@@ -42,11 +42,15 @@ H100_PUBLISHED = 3.079643e8  # doc/source/bench.json:84-90 (128^3 per GPU, FP64,
 BYTES_PER_ZONE_CYCLE = 320.0  # 8 FP64 state values x 5 transfers per RK2 cycle
 # FP64 thread instructions (dadd + dmul + dfma + the rest of the FP64 pipe,
 # predicated on) per active cell of one sweep launch, and DRAM bytes per
-# active cell of one sweep launch: ncu on the 128^3 case of this workload
-# (stage 0, the three sweep launches of the first warm-up cycle).  Both scale with the
-# cells processed; at 256^3 the CT-extension columns add 1.6 % instead of 3.1 %.
-FP64_INST_PER_CELL = {"sweep_x": 539.1, "sweep_y": 526.2, "sweep_z": 532.8}
-DRAM_BYTES_PER_CELL = {"sweep_x": 193.7, "sweep_y": 172.6, "sweep_z": 171.7}
+# active cell of one sweep launch, with the march segment of this workload at
+# 256^3 (64 cells): ncu on the 128^3 case with segments 64 (stage 0, the
+# three sweep launches of the first cycle), scaled to 256^3 by the columns a
+# sweep processes (the CT-extension columns add 1.6 % of the cells at 256^3
+# against 3.1 % at 128^3; per processed column-cell the counts are the same
+# at one segment length).  Shorter segments reconstruct more cells twice:
+# at 128^3 with segments 8 the same sweeps take 526-539 instructions per cell.
+FP64_INST_PER_CELL = {"sweep_x": 473.7, "sweep_y": 463.0, "sweep_z": 466.1}
+DRAM_BYTES_PER_CELL = {"sweep_x": 224.3, "sweep_y": 176.9, "sweep_z": 177.1}
 # FP64 operations per active zone and RK2 cycle of the reference algorithm on
 # this workload at 256^3, each add/sub, mul, div and sqrt counted once
 # (1465.5 + 1662.8 + 215.5 + 35.8): the operation-counting build of the CPU
@@ -385,7 +389,8 @@ def run_ours(args, world, rank, local):
         fp64_roof = {"achieved": ach, "peak": fp64_peak, "unit": "G FP64 thread-op/s", "frac": ach / fp64_peak,
                      "kernel": dom, "inst_per_cell": FP64_INST_PER_CELL[dom],
                      "peak_kind": "measured in this run (DFMA, idfx_measure_fp64_peak)",
-                     "inst_source": "ncu FP64-pipe thread instructions per active cell, 128^3 stage-0 sweep"}
+                     "inst_source": "ncu FP64-pipe thread instructions per active cell, 128^3 stage-0 sweep "
+                                    "with segments 64, scaled to 256^3 by the processed columns"}
 
     # the same workload in the mixed precision mode (FP32 reconstruction and
     # Riemann solve, FP64 state), for reference beside the FP64 headline
@@ -440,7 +445,8 @@ def run_ours(args, world, rank, local):
                          "frac": (achieved_gbs / hbm_peak) if achieved_gbs else None,
                          "traffic": traffic, "kernel": dom, "peak_kind": peak_kind,
                          "bytes_per_cell": sweep_bytes_per_cell,
-                         "traffic_note": "ncu dram read+write per active cell of the 128^3 sweep x 256^3 cells",
+                         "traffic_note": "ncu dram read+write per active cell of the 128^3 sweep (segments 64), "
+                                         "scaled to 256^3 by the processed columns, x 256^3 cells",
                          "note": "FP64-issue bound (GB300 FP64 ~1.2 TFLOP/s): see fp64_roofline"},
             "fp64_roofline": fp64_roof,
             "fp64_flop": fp64_flop_roof(value / world, fp64_peak) if args.precision == "fp64" else None,
