@@ -5,6 +5,7 @@
 // queued without host synchronisation; the host mirrors only the cycle count
 // (to schedule the divB / NaN diagnostics exactly when the reference does).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cmath>
 #include <cstdio>
@@ -232,6 +233,17 @@ __global__ void k_faces_combine(Geo g, Fields f, Ctl* ctl, double wc, double w0)
 // ---------------------------------------------------------------------------
 // launch helpers
 // ---------------------------------------------------------------------------
+// A profiler range named as the reference's region for the same work
+// (idfx::pushRegion / popRegion, which reach NVTX through Kokkos' profiling
+// hooks): Nsight shows the library's launches under the reference's names.
+// Host-side ranges around the launches they queue; no cost without a tool.
+struct Region {
+  explicit Region(const char* name) { nvtxRangePushA(name); }
+  ~Region() { nvtxRangePop(); }
+  Region(const Region&) = delete;
+  Region& operator=(const Region&) = delete;
+};
+
 void launch_sweeps(Engine& e, int invdt, int fold_max) {
   switch (e.g.solver) {
     case kHLLD: launch_sweeps_hlld(e, invdt, fold_max); break;
@@ -328,6 +340,8 @@ void launch_ct(Engine& e, int combine, double wc, double w0) {
     const Geo& g = e.g;
     dim3 grid((unsigned)((g.n[0] + 1 + kCtTI - 1) / kCtTI), (unsigned)((g.n[1] + 1 + kCtTJ - 1) / kCtTJ),
               (unsigned)(g.D == 3 ? (g.n[2] + 1 + kCtKSeg - 1) / kCtKSeg : 1));
+    // (the corner EMFs are computed inside the face update's pass)
+    const Region r("ConstrainedTransport::EvolveMagField");
     mark_begin(e, kKCtFaces);
     const CtTileMap* cm = (g.D == 3) ? ct_tile_map(e) : nullptr;
     if (cm) {
@@ -344,9 +358,13 @@ void launch_ct(Engine& e, int combine, double wc, double w0) {
     mark_end(e);
     return;
   }
-  mark_begin(e, kKCtCorner);
-  IDFX_DISPATCH_DE(k_ct_corner, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
-  mark_end(e);
+  {
+    const Region r("ConstrainedTransport::CalcCornerEMF");
+    mark_begin(e, kKCtCorner);
+    IDFX_DISPATCH_DE(k_ct_corner, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl);
+    mark_end(e);
+  }
+  const Region r("ConstrainedTransport::EvolveMagField");
   mark_begin(e, kKCtFaces);
   IDFX_DISPATCH_DE(k_ct_faces, nblocks(n_edges(e.g)), kThreads, e.g, e.f, e.ctl, combine, wc, w0);
   mark_end(e);
@@ -385,6 +403,7 @@ void launch_divb_check(Engine& e) {
 
 // queue one TimeIntegrator::Cycle
 void queue_cycle(Engine& e, int use_tstop) {
+  const Region cycle_region("TimeIntegrator::Cycle");
   const Geo& g = e.g;
   const bool cell_emf = (g.emf == kEmfContact || g.emf == kEmfUct0);
   const bool fused = (e.precision == IDFX_MIXED) && !g.nonper;
@@ -393,11 +412,14 @@ void queue_cycle(Engine& e, int use_tstop) {
   const bool nan_check = e.check_nan_period > 0 && e.ncycles % e.check_nan_period == 0;
   for (int stage = 0; stage < e.nstages; stage++) {
     const int save = (e.nstages > 1 && stage == 0);
-    launch_boundaries(e);
-    // periodic block: a Runge-Kutta begin copy of the faces that the
-    // previous cycle's last face update already wrote leaves the ghosts
-    if (!g.nonper && (!save || e.faces_saved)) launch_fill_face_ghosts(e);
-    else launch_fill_faces(e, save);
+    {
+      const Region r("Boundary::SetBoundaries");
+      launch_boundaries(e);
+      // periodic block: a Runge-Kutta begin copy of the faces that the
+      // previous cycle's last face update already wrote leaves the ghosts
+      if (!g.nonper && (!save || e.faces_saved)) launch_fill_face_ghosts(e);
+      else launch_fill_faces(e, save);
+    }
     // mixed path: Uc carried over from the previous stage end when it is
     // still the state Vc came from (Ctl::uc_fresh); the FP64 path rebuilds it
     // as the reference does
@@ -406,36 +428,51 @@ void queue_cycle(Engine& e, int use_tstop) {
     // mixed path, periodic block: once a stage end of this run has written
     // the active cells' FP32 primitives, cell EMF and Runge-Kutta begin copy,
     // the stage begin fills the ghost cells alone
-    if (fused && e.stage_outputs) launch_stage_ghosts(e, sb_flags);
-    else launch_stage_begin(e, sb_flags);
-    if (e.f.shock) launch_find_shock(e);  // RiemannSolver::CalcFlux (calcFlux.hpp:33)
-    launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
+    {
+      const Region r("Fluid::ConvertPrimToCons");
+      if (fused && e.stage_outputs) launch_stage_ghosts(e, sb_flags);
+      else launch_stage_begin(e, sb_flags);
+    }
     const int combine = stage > 0;
     const double wc = combine ? e.wc[stage - 1] : 1.0, w0 = combine ? e.w0[stage - 1] : 0.0;
-    if (nan_check) {
-      launch_ct(e, 0, 1.0, 0.0);
-      launch_nan_check(e);
-      if (combine) {
-        if (e.precision == IDFX_MIXED)
-          k_faces_combine<float><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
-        else
-          k_faces_combine<double><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
+    {
+      const Region stage_region("Fluid::EvolveStage");
+      {
+        const Region r("RiemannSolver::CalcFlux");
+        if (e.f.shock) launch_find_shock(e);  // RiemannSolver::CalcFlux (calcFlux.hpp:33)
+        launch_sweeps(e, stage == 0 ? 1 : 0, stage == 0);
       }
-      e.faces_saved = false;
-    } else {
-      // periodic block: the last stage's face update also writes the next
-      // cycle's Runge-Kutta begin copy of the faces
-      const bool save_next = !g.nonper && e.nstages > 1 && stage == e.nstages - 1;
-      launch_ct(e, (combine ? kCtCombine : 0) | (save_next ? kCtSaveBegin : 0), wc, w0);
-      if (save_next) e.faces_saved = true;
+      if (nan_check) {
+        launch_ct(e, 0, 1.0, 0.0);
+        {
+          const Region rn("Fluid::CheckNan");
+          launch_nan_check(e);
+        }
+        if (combine) {
+          if (e.precision == IDFX_MIXED)
+            k_faces_combine<float><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
+          else
+            k_faces_combine<double><<<nblocks(g.nface * g.D), kThreads, 0, e.stream>>>(g, e.f, e.ctl, wc, w0);
+        }
+        e.faces_saved = false;
+      } else {
+        // periodic block: the last stage's face update also writes the next
+        // cycle's Runge-Kutta begin copy of the faces
+        const bool save_next = !g.nonper && e.nstages > 1 && stage == e.nstages - 1;
+        launch_ct(e, (combine ? kCtCombine : 0) | (save_next ? kCtSaveBegin : 0), wc, w0);
+        if (save_next) e.faces_saved = true;
+      }
     }
     const int out = fused ? (kSeOutputs | kSeNoUcField | (cell_emf ? kSbCellEmf : 0) |
                              (e.nstages > 1 && stage == e.nstages - 1 ? kSeSaveBegin : 0))
                           : 0;
     if (fused) e.uc_field_stale = true;
-    mark_begin(e, kKStageEnd);
-    IDFX_DISPATCH_DE(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0, out);
-    mark_end(e);
+    {
+      const Region r("Fluid::ConvertConsToPrim");
+      mark_begin(e, kKStageEnd);
+      IDFX_DISPATCH_DE(k_stage_end, nblocks(n_active(g)), kThreads, g, e.f, e.ctl, combine, wc, w0, out);
+      mark_end(e);
+    }
     if (fused) e.stage_outputs = true;
   }
   k_cycle_end<<<1, 1, 0, e.stream>>>(e.ctl);
